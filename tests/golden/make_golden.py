@@ -1,0 +1,182 @@
+"""Generate the golden fixtures in tests/golden/ from the femx reference.
+
+Runs in the development container only (it needs the reference sources):
+builds the reference library and driver with oracle/ref/Makefile into
+oracle/_ref/, writes seeded inputs, runs the driver and stores inputs and the
+reference's outputs as compressed .npz files next to this script.
+
+    python tests/golden/make_golden.py [--ref /path/to/reference]
+
+Cases
+  kat          known-answer cases of the reference's unit tests
+  p1_32        32x32 structured P1 Poisson, kappa = 1, Fourier source,
+               homogeneous Dirichlet on all edges (the CPU-runnable config)
+  p1_jit9      9x9 jittered mesh with permuted node/element ids, random
+               kappa, u, lam, x and a linear Dirichlet lift g = 0.5 + x - 2y
+  th_4         4x4 structured Taylor-Hood P2/P1, random state, nu = 1e-2
+  th_jit3      3x3 jittered, permuted Taylor-Hood mesh, nu = 1e-3
+  inverse_12   12x12 Poisson inverse: femx ReducedFunctional gradient with
+               DenseLinearSolver, misfit 0.5|u - d|^2, kappa = exp(m)
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from femx_gb300 import meshes  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+
+
+def build(ref: str):
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), f"REF={ref}", "-j8"])
+
+
+def write(d, name, arr):
+    np.ascontiguousarray(arr).tofile(os.path.join(d, name + ".bin"))
+
+
+def read(d, name, dtype):
+    return np.fromfile(os.path.join(d, name + ".bin"), dtype=dtype)
+
+
+def run(kind, d, params=None):
+    if params:
+        with open(os.path.join(d, "params.txt"), "w") as fh:
+            for k, v in params.items():
+                fh.write(f"{k} {v!r}\n")
+    out = subprocess.run([DRIVER, kind, d], check=True, capture_output=True, text=True)
+    return out.stdout
+
+
+KAT_NAMES = {
+    "shared_row_ptr": np.int32, "shared_col_ind": np.int32, "shared_jac_map": np.int32,
+    "rect_row_ptr": np.int32, "rect_col_ind": np.int32, "rect_jac_map": np.int32,
+}
+for tag in ("bc1_", "bc02_"):
+    for nm in ("rows1", "rows0", "res", "fwd_vals", "fwd_rhs"):
+        KAT_NAMES[tag + nm] = np.float64
+
+MAP_OUT = {"row_ptr": np.int32, "col_ind": np.int32, "jac_offsets": np.int32, "jac_map": np.int32}
+BC_OUT = {"bc_rows": np.int32, "bc_diag": np.int32, "bc_col_offsets": np.int32,
+          "bc_col_entries": np.int32, "bc_col_rows": np.int32, "bc_mask": np.int32}
+
+
+def case_kat(tmp):
+    d = os.path.join(tmp, "kat")
+    os.makedirs(d)
+    run("kat", d)
+    return {k: read(d, k, t) for k, t in KAT_NAMES.items()}
+
+
+def case_p1(tmp, name, coords, conn, kappa, f, u, x, lam, g):
+    d = os.path.join(tmp, name)
+    os.makedirs(d)
+    for nm, arr in (("coords", coords), ("conn", conn), ("kappa", kappa), ("f", f), ("u", u),
+                    ("x", x), ("lam", lam)):
+        write(d, nm, arr)
+    run("p1", d, {"g0": g[0], "gx": g[1], "gy": g[2]})
+    out = dict(coords=coords, conn=conn, kappa=kappa, f=f, u=u, x=x, lam=lam,
+               g=np.array(g, dtype=np.float64))
+    for k, t in {**MAP_OUT, **BC_OUT, "bc_dofs": np.int32}.items():
+        out[k] = read(d, k, t)
+    for k in ("res", "vals", "bc_vals", "y_matvec", "y_matvec_t", "vals_rows1", "res_replaced",
+              "vals_fwd", "rhs_fwd", "g_u", "g_m"):
+        out[k] = read(d, k, np.float64)
+    return out
+
+
+def case_th(tmp, name, coords3, conn3, nu, seed):
+    rng = np.random.default_rng(seed)
+    cp2, conn6, nv = meshes.p2_mesh(coords3, conn3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    state = rng.standard_normal(nd)
+    d = os.path.join(tmp, name)
+    os.makedirs(d)
+    write(d, "coords", cp2)
+    write(d, "conn6", conn6)
+    write(d, "elem_dofs", dofs)
+    write(d, "state", state)
+    run("th", d, {"nu": nu, "num_dofs": nd})
+    out = dict(coords=cp2, conn6=conn6, elem_dofs=dofs, state=state, nu=np.float64(nu),
+               num_dofs=np.int64(nd))
+    for k, t in MAP_OUT.items():
+        out[k] = read(d, k, t)
+    out["res"] = read(d, "res", np.float64)
+    out["vals"] = read(d, "vals", np.float64)
+    return out
+
+
+def case_inverse(tmp, nx, seed):
+    coords, conn = meshes.structured_tri(nx)
+    f = meshes.fourier_source(coords, seed)
+    m_true = meshes.grf_centroids(coords, conn, seed + 1, ell=0.2, grid=64)
+    d = os.path.join(tmp, f"inverse_{nx}_true")
+    os.makedirs(d)
+    write(d, "coords", coords)
+    write(d, "conn", conn)
+    write(d, "m", m_true)
+    write(d, "d", np.zeros(coords.shape[0]))
+    write(d, "f", f)
+    run("inverse", d)
+    u_true = read(d, "u", np.float64)
+    rng = np.random.default_rng(seed + 2)
+    data = u_true + 1e-3 * rng.standard_normal(u_true.shape)
+    m = 0.5 * m_true + 0.1
+    d2 = os.path.join(tmp, f"inverse_{nx}")
+    os.makedirs(d2)
+    for nm, arr in (("coords", coords), ("conn", conn), ("m", m), ("d", data), ("f", f)):
+        write(d2, nm, arr)
+    run("inverse", d2)
+    return dict(coords=coords, conn=conn, m=m, d=data, f=f,
+                value=read(d2, "value", np.float64), grad=read(d2, "grad", np.float64),
+                u=read(d2, "u", np.float64))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default="/root/reference")
+    args = ap.parse_args()
+    build(args.ref)
+    with tempfile.TemporaryDirectory() as tmp:
+        np.savez_compressed(os.path.join(HERE, "kat.npz"), **case_kat(tmp))
+
+        coords, conn = meshes.structured_tri(32)
+        n, e = coords.shape[0], conn.shape[0]
+        rng = np.random.default_rng(1)
+        f = meshes.fourier_source(coords, 1)
+        np.savez_compressed(os.path.join(HERE, "p1_32.npz"), **case_p1(
+            tmp, "p1_32", coords, conn, np.ones(e), f, np.zeros(n), rng.standard_normal(n),
+            rng.standard_normal(n), (0.0, 0.0, 0.0)))
+
+        coords, conn = meshes.jittered_tri(9, seed=7)
+        n, e = coords.shape[0], conn.shape[0]
+        rng = np.random.default_rng(9)
+        np.savez_compressed(os.path.join(HERE, "p1_jit9.npz"), **case_p1(
+            tmp, "p1_jit9", coords, conn, np.exp(rng.standard_normal(e)),
+            meshes.fourier_source(coords, 3), rng.standard_normal(n), rng.standard_normal(n),
+            rng.standard_normal(n), (0.5, 1.0, -2.0)))
+
+        c3, k3 = meshes.structured_tri(4)
+        np.savez_compressed(os.path.join(HERE, "th_4.npz"), **case_th(tmp, "th_4", c3, k3, 1e-2, 4))
+        c3, k3 = meshes.jittered_tri(3, seed=11)
+        np.savez_compressed(os.path.join(HERE, "th_jit3.npz"),
+                            **case_th(tmp, "th_jit3", c3, k3, 1e-3, 5))
+
+        np.savez_compressed(os.path.join(HERE, "inverse_12.npz"), **case_inverse(tmp, 12, 20))
+    for fn in sorted(os.listdir(HERE)):
+        if fn.endswith(".npz"):
+            print(fn, os.path.getsize(os.path.join(HERE, fn)), "bytes")
+
+
+if __name__ == "__main__":
+    main()
