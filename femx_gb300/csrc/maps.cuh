@@ -1,0 +1,70 @@
+// maps.cuh — the device-resident AssemblyMap and BoundaryMap handles.
+#pragma once
+
+#include "common.cuh"
+
+// femx AssemblyMap<Device> (femx/assembly/AssemblyMap.hpp:78-206) plus the
+// CSR pattern it owns (CsrPattern.hpp:42-217). All arrays are device memory
+// owned by the handle.
+struct gbfem_assembly_map
+{
+  int                num_elems  = 0;
+  int                num_res    = 0;
+  int                num_states = 0;
+  int                nnz        = 0;
+  int                jac_nnz    = 0;
+  int                max_res = 0, max_state = 0, max_jac = 0;
+  int                uniform_res   = -1; // rows per element when uniform
+  int                uniform_state = -1; // cols per element when uniform
+  bool               same_dofs     = false; // res tables == state tables
+  unsigned long long layout_id     = 0;
+
+  int* res_offsets   = nullptr;
+  int* res_dofs      = nullptr;
+  int* state_offsets = nullptr;
+  int* state_dofs    = nullptr;
+  int* jac_offsets   = nullptr;
+  int* jac_map       = nullptr;
+  int* row_ptr       = nullptr;
+  int* col_ind       = nullptr;
+
+  // Status word written by hot-path kernels that meet invalid data
+  // (degenerate elements); read by gbfem_assembly_map_check().
+  gbfem::DeviceStatus* status = nullptr;
+
+  ~gbfem_assembly_map();
+};
+
+// femx BoundaryMap<Device> (femx/assembly/BoundaryMap.hpp:69-175) plus a
+// row-grouped view of the constrained-column entries that lets the lifting
+// run one thread per affected row, without atomics, applying subtractions
+// in constraint order (identical to BoundaryMap.cpp:224-238).
+struct gbfem_boundary_map
+{
+  int                num_rows = 0, num_cols = 0, nnz = 0, num_bcs = 0;
+  int                num_col_entries = 0;
+  unsigned long long layout_id       = 0;
+
+  int* bc_rows     = nullptr;
+  int* diag        = nullptr;
+  int* col_offsets = nullptr;
+  int* col_entries = nullptr;
+  int* col_rows    = nullptr;
+  int* bc_mask     = nullptr;
+  int* row_begin   = nullptr; // CSR extent of each constrained row
+  int* row_end     = nullptr;
+
+  // Lifting list: unconstrained rows touching constrained columns.
+  int  num_lift_rows = 0;
+  int* lift_rows     = nullptr; // [num_lift_rows]
+  int* lift_offsets  = nullptr; // [num_lift_rows + 1]
+  int* lift_k        = nullptr; // CSR slot, sorted by constraint index
+  int* lift_ib       = nullptr; // constraint index of that column
+
+  ~gbfem_boundary_map();
+};
+
+namespace gbfem
+{
+unsigned long long nextLayoutId();
+}

@@ -1,0 +1,45 @@
+// measure.cu — FP64 FMA throughput probe (see include/gbfem_measure.h).
+#include "common.cuh"
+#include "gbfem_measure.h"
+
+namespace
+{
+__global__ void fp64FmaProbe(int iters, double* out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double    a[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+  {
+    a[i] = 1.0 + 1.0e-9 * (t + i);
+  }
+  const double m = 0.999999999, c = 1.0e-12;
+  for (int it = 0; it < iters; ++it)
+  {
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+    {
+      a[i] = fma(a[i], m, c);
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+  {
+    s += a[i];
+  }
+  out[t] = s;
+}
+} // namespace
+
+extern "C" int gbfem_probe_fp64_fma(int blocks, int threads, int iters,
+                                    double* out, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(blocks > 0 && threads > 0 && threads <= 1024 && iters > 0 && out,
+            "probe arguments are invalid");
+    fp64FmaProbe<<<blocks, threads, 0, asStream(stream)>>>(iters, out);
+    cudaCheck(cudaGetLastError(), "probe launch");
+  });
+}

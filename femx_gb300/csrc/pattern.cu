@@ -1,0 +1,463 @@
+// pattern.cu — GPU build of femx's AssemblyMap: element DOF tables in,
+// CSR pattern + jac_map out, bit-identical to makeAssemblyMap
+// (femx/assembly/AssemblyMap.cpp:54-176).
+//
+// The reference forms the COO list of every element block, sorts it globally
+// and merges duplicates. Here each CSR row owns its candidate columns:
+//   1. count, per row, the candidate columns contributed by element blocks;
+//   2. bucket every (element, row, col) candidate under its row;
+//   3. per row (one warp): mark the first occurrence of each column, count
+//      the distinct columns -> row_ptr by scan;
+//   4. per row: rank each candidate among the distinct columns; the rank is
+//      its CSR slot, written to jac_map at the candidate's local entry.
+// The result depends only on the set of (row, col) pairs, so it equals the
+// reference's sort-based result exactly, whatever the bucketing order.
+#include <algorithm>
+#include <atomic>
+#include <climits>
+
+#include "maps.cuh"
+
+namespace
+{
+
+using gbfem::DeviceStatus;
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kStageCap      = 512; // candidates staged in shared memory per warp
+
+__global__ void countCandidates(int ne, int num_res, int num_states,
+                                const int* __restrict__ ro,
+                                const int* __restrict__ rd,
+                                const int* __restrict__ so,
+                                const int* __restrict__ sd,
+                                long long* __restrict__ elem_jac,
+                                int* __restrict__ row_cand,
+                                int* __restrict__ stats, DeviceStatus* st)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne)
+  {
+    return;
+  }
+  const int r0 = ro[e], r1 = ro[e + 1], s0 = so[e], s1 = so[e + 1];
+  const int nr = r1 - r0, nc = s1 - s0;
+  if (nr < 0 || nc < 0 || (e == 0 && (r0 != 0 || s0 != 0)))
+  {
+    gbfem::devFail(st, gbfem::kDevNegativeLocal, e);
+    elem_jac[e] = 0;
+    return;
+  }
+  elem_jac[e] = static_cast<long long>(nr) * nc;
+  atomicMax(&stats[0], nr);
+  atomicMax(&stats[1], nc);
+  atomicMin(&stats[2], nr);
+  atomicMin(&stats[3], nc);
+  for (int i = r0; i < r1; ++i)
+  {
+    const int dof = rd[i];
+    if (dof < 0 || dof >= num_res)
+    {
+      gbfem::devFail(st, gbfem::kDevResDofRange, i);
+      continue;
+    }
+    atomicAdd(&row_cand[dof], nc);
+  }
+  for (int j = s0; j < s1; ++j)
+  {
+    const int dof = sd[j];
+    if (dof < 0 || dof >= num_states)
+    {
+      gbfem::devFail(st, gbfem::kDevStateDofRange, j);
+    }
+  }
+}
+
+__global__ void bucketCandidates(int ne, const int* __restrict__ ro,
+                                 const int* __restrict__ rd,
+                                 const int* __restrict__ so,
+                                 const int* __restrict__ sd,
+                                 const int* __restrict__ jac_offsets,
+                                 const int* __restrict__ cand_off,
+                                 int* __restrict__ cursor,
+                                 int* __restrict__ cand_col,
+                                 int* __restrict__ cand_src)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne)
+  {
+    return;
+  }
+  const int r0 = ro[e], nr = ro[e + 1] - r0;
+  const int s0 = so[e], nc = so[e + 1] - s0;
+  const int j0 = jac_offsets[e];
+  for (int i = 0; i < nr; ++i)
+  {
+    const int row  = rd[r0 + i];
+    const int slot = cand_off[row] + atomicAdd(&cursor[row], nc);
+    for (int j = 0; j < nc; ++j)
+    {
+      cand_col[slot + j] = sd[s0 + j];
+      cand_src[slot + j] = j0 + i * nc + j;
+    }
+  }
+}
+
+// Phase 3: first-occurrence flags and distinct-column count per row.
+__global__ void markDistinct(int num_res, const int* __restrict__ cand_off,
+                             const int* __restrict__ cand_col,
+                             unsigned char* __restrict__ first,
+                             int* __restrict__ row_nnz)
+{
+  __shared__ int stage[kWarpsPerBlock][kStageCap];
+  const int      lane = threadIdx.x & 31;
+  const int      w    = threadIdx.x >> 5;
+  const int      row  = blockIdx.x * kWarpsPerBlock + w;
+  if (row >= num_res)
+  {
+    return;
+  }
+  const int  beg    = cand_off[row];
+  const int  n      = cand_off[row + 1] - beg;
+  const int* src    = cand_col + beg;
+  const bool staged = n <= kStageCap;
+  if (staged)
+  {
+    for (int k = lane; k < n; k += 32)
+    {
+      stage[w][k] = src[k];
+    }
+    __syncwarp();
+    src = stage[w];
+  }
+  int count = 0;
+  for (int k = lane; k < n; k += 32)
+  {
+    const int c  = src[k];
+    bool      fr = true;
+    for (int j = 0; j < k; ++j)
+    {
+      if (src[j] == c)
+      {
+        fr = false;
+        break;
+      }
+    }
+    first[beg + k] = fr ? 1 : 0;
+    count += fr ? 1 : 0;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1)
+  {
+    count += __shfl_xor_sync(0xffffffffu, count, off);
+  }
+  if (lane == 0)
+  {
+    row_nnz[row] = count;
+  }
+}
+
+// Phase 4: rank among distinct columns -> CSR slot; write col_ind, jac_map.
+__global__ void rankColumns(int num_res, const int* __restrict__ cand_off,
+                            const int* __restrict__ cand_col,
+                            const int* __restrict__ cand_src,
+                            const unsigned char* __restrict__ first,
+                            const int* __restrict__ row_ptr,
+                            int* __restrict__ col_ind,
+                            int* __restrict__ jac_map)
+{
+  __shared__ int stage[kWarpsPerBlock][kStageCap];
+  __shared__ unsigned char fstage[kWarpsPerBlock][kStageCap];
+  const int                lane = threadIdx.x & 31;
+  const int                w    = threadIdx.x >> 5;
+  const int                row  = blockIdx.x * kWarpsPerBlock + w;
+  if (row >= num_res)
+  {
+    return;
+  }
+  const int            beg    = cand_off[row];
+  const int            n      = cand_off[row + 1] - beg;
+  const int*           src    = cand_col + beg;
+  const unsigned char* fl     = first + beg;
+  const bool           staged = n <= kStageCap;
+  if (staged)
+  {
+    for (int k = lane; k < n; k += 32)
+    {
+      stage[w][k]  = src[k];
+      fstage[w][k] = fl[k];
+    }
+    __syncwarp();
+    src = stage[w];
+    fl  = fstage[w];
+  }
+  const int base = row_ptr[row];
+  for (int k = lane; k < n; k += 32)
+  {
+    const int c    = src[k];
+    int       rank = 0;
+    for (int j = 0; j < n; ++j)
+    {
+      rank += (fl[j] != 0 && src[j] < c) ? 1 : 0;
+    }
+    const int pos          = base + rank;
+    jac_map[cand_src[beg + k]] = pos;
+    if (fl[k] != 0)
+    {
+      col_ind[pos] = c;
+    }
+  }
+}
+
+__global__ void compareTables(long long n, const int* __restrict__ a,
+                              const int* __restrict__ b, int* __restrict__ diff)
+{
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i < n && a[i] != b[i])
+  {
+    *diff = 1;
+  }
+}
+
+template <class T>
+void copyIn(T*& dst, const T* src, long long n, cudaStream_t s)
+{
+  dst = gbfem::deviceAlloc<T>(n);
+  if (n > 0)
+  {
+    gbfem::cudaCheck(cudaMemcpyAsync(dst, src, sizeof(T) * n,
+                                     cudaMemcpyDeviceToDevice, s),
+                     "AssemblyMap table copy");
+  }
+}
+
+struct Scratch
+{
+  void* p[8] = {};
+  ~Scratch()
+  {
+    for (void* q : p)
+    {
+      gbfem::deviceFree(q);
+    }
+  }
+};
+
+} // namespace
+
+gbfem_assembly_map::~gbfem_assembly_map()
+{
+  for (int* p : {res_offsets, res_dofs, state_offsets, state_dofs, jac_offsets,
+                 jac_map, row_ptr, col_ind})
+  {
+    gbfem::deviceFree(p);
+  }
+  gbfem::deviceFree(status);
+}
+
+namespace gbfem
+{
+unsigned long long nextLayoutId()
+{
+  static std::atomic<unsigned long long> next{1};
+  return next++;
+}
+} // namespace gbfem
+
+extern "C" int gbfem_assembly_map_create(int num_res, int num_states,
+                                         int num_elems, const int* res_offsets,
+                                         const int* res_dofs,
+                                         const int* state_offsets,
+                                         const int* state_dofs, void* stream,
+                                         gbfem_assembly_map** out)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(out != nullptr, "AssemblyMap output handle is null");
+    *out = nullptr;
+    require(num_res >= 0 && num_states >= 0,
+            "AssemblyMap global dimensions must be non-negative");
+    require(num_elems >= 0, "AssemblyMap residual/state element counts differ");
+    require(num_elems == 0 || (res_offsets && res_dofs && state_offsets && state_dofs),
+            "AssemblyMap element tables must not be null");
+    cudaStream_t s = asStream(stream);
+    auto* m        = new gbfem_assembly_map;
+    try
+    {
+      m->num_elems  = num_elems;
+      m->num_res    = num_res;
+      m->num_states = num_states;
+      m->layout_id  = nextLayoutId();
+      m->status     = deviceAlloc<DeviceStatus>(1);
+      cudaCheck(cudaMemsetAsync(m->status, 0, sizeof(DeviceStatus), s), "memset");
+
+      int tot[2] = {0, 0};
+      if (num_elems > 0)
+      {
+        cudaCheck(cudaMemcpyAsync(&tot[0], res_offsets + num_elems, sizeof(int),
+                                  cudaMemcpyDeviceToHost, s),
+                  "AssemblyMap offsets readback");
+        cudaCheck(cudaMemcpyAsync(&tot[1], state_offsets + num_elems, sizeof(int),
+                                  cudaMemcpyDeviceToHost, s),
+                  "AssemblyMap offsets readback");
+        cudaCheck(cudaStreamSynchronize(s), "AssemblyMap offsets readback");
+        require(tot[0] >= 0 && tot[1] >= 0,
+                "AssemblyMap local dimensions must be non-negative");
+      }
+      copyIn(m->res_offsets, res_offsets, num_elems + 1LL, s);
+      copyIn(m->state_offsets, state_offsets, num_elems + 1LL, s);
+      copyIn(m->res_dofs, res_dofs, tot[0], s);
+      copyIn(m->state_dofs, state_dofs, tot[1], s);
+      if (num_elems == 0)
+      {
+        cudaCheck(cudaMemsetAsync(m->res_offsets, 0, sizeof(int), s), "memset");
+        cudaCheck(cudaMemsetAsync(m->state_offsets, 0, sizeof(int), s), "memset");
+      }
+      m->row_ptr     = deviceAlloc<int>(num_res + 1LL);
+      m->jac_offsets = deviceAlloc<int>(num_elems + 1LL);
+
+      Scratch sc;
+      auto* status   = deviceAlloc<DeviceStatus>(1);
+      sc.p[0]        = status;
+      auto* elem_jac = deviceAlloc<long long>(std::max(num_elems, 1));
+      sc.p[1]        = elem_jac;
+      auto* row_cand = deviceAlloc<int>(num_res + 1LL);
+      sc.p[2]        = row_cand;
+      auto* cand_off = deviceAlloc<int>(num_res + 1LL);
+      sc.p[3]        = cand_off;
+      auto* stats    = deviceAlloc<int>(4);
+      sc.p[4]        = stats;
+      const int stats_init[4] = {0, 0, INT_MAX, INT_MAX};
+      cudaCheck(cudaMemcpyAsync(stats, stats_init, sizeof(stats_init),
+                                cudaMemcpyHostToDevice, s),
+                "stats init");
+      cudaCheck(cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s), "memset");
+      cudaCheck(cudaMemsetAsync(row_cand, 0, sizeof(int) * (num_res + 1LL), s),
+                "memset");
+      if (num_elems > 0)
+      {
+        countCandidates<<<blocksFor(num_elems, 256), 256, 0, s>>>(
+            num_elems, num_res, num_states, m->res_offsets, m->res_dofs,
+            m->state_offsets, m->state_dofs, elem_jac, row_cand, stats, status);
+        cudaCheck(cudaGetLastError(), "AssemblyMap count launch");
+      }
+      checkDeviceStatus(status, s);
+      int st_h[4] = {0, 0, 0, 0};
+      cudaCheck(cudaMemcpy(st_h, stats, sizeof(st_h), cudaMemcpyDeviceToHost),
+                "stats readback");
+      if (num_elems > 0)
+      {
+        m->max_res       = st_h[0];
+        m->max_state     = st_h[1];
+        m->uniform_res   = st_h[0] == st_h[2] ? st_h[0] : -1;
+        m->uniform_state = st_h[1] == st_h[3] ? st_h[1] : -1;
+        const long long mj = static_cast<long long>(st_h[0]) * st_h[1];
+        require(mj <= INT_MAX, "AssemblyMap local Jacobian is too large");
+        m->max_jac = static_cast<int>(mj);
+      }
+      // jac_offsets = exclusive scan of element block sizes (checked to fit)
+      const long long jac_nnz =
+          num_elems > 0 ? exclusiveScan64to32(elem_jac, m->jac_offsets, num_elems, s) : 0;
+      if (num_elems == 0)
+      {
+        cudaCheck(cudaMemsetAsync(m->jac_offsets, 0, sizeof(int), s), "memset");
+      }
+      m->jac_nnz = static_cast<int>(jac_nnz);
+      exclusiveScan(row_cand, cand_off, num_res, s);
+
+      m->jac_map    = deviceAlloc<int>(jac_nnz);
+      auto* cand_col = deviceAlloc<int>(jac_nnz);
+      sc.p[5]        = cand_col;
+      auto* cand_src = deviceAlloc<int>(jac_nnz);
+      sc.p[6]        = cand_src;
+      auto* first    = deviceAlloc<unsigned char>(jac_nnz);
+      sc.p[7]        = first;
+      cudaCheck(cudaMemsetAsync(row_cand, 0, sizeof(int) * (num_res + 1LL), s),
+                "memset");
+      if (num_elems > 0)
+      {
+        bucketCandidates<<<blocksFor(num_elems, 256), 256, 0, s>>>(
+            num_elems, m->res_offsets, m->res_dofs, m->state_offsets,
+            m->state_dofs, m->jac_offsets, cand_off, row_cand, cand_col,
+            cand_src);
+        cudaCheck(cudaGetLastError(), "AssemblyMap bucket launch");
+      }
+      const unsigned rblocks = blocksFor(num_res, kWarpsPerBlock);
+      if (num_res > 0)
+      {
+        markDistinct<<<rblocks, 32 * kWarpsPerBlock, 0, s>>>(
+            num_res, cand_off, cand_col, first, row_cand);
+        cudaCheck(cudaGetLastError(), "AssemblyMap distinct launch");
+      }
+      const long long nnz = exclusiveScan(row_cand, m->row_ptr, num_res, s);
+      m->nnz              = static_cast<int>(nnz);
+      m->col_ind          = deviceAlloc<int>(nnz);
+      if (num_res > 0)
+      {
+        rankColumns<<<rblocks, 32 * kWarpsPerBlock, 0, s>>>(
+            num_res, cand_off, cand_col, cand_src, first, m->row_ptr,
+            m->col_ind, m->jac_map);
+        cudaCheck(cudaGetLastError(), "AssemblyMap rank launch");
+      }
+      // Identical residual and state tables (square scalar/mixed layouts)
+      // let element kernels read one DOF table instead of two.
+      if (tot[0] == tot[1])
+      {
+        int* diff = deviceAlloc<int>(1);
+        cudaCheck(cudaMemsetAsync(diff, 0, sizeof(int), s), "memset");
+        compareTables<<<blocksFor(num_elems + 1LL, 256), 256, 0, s>>>(
+            num_elems + 1LL, m->res_offsets, m->state_offsets, diff);
+        if (tot[0] > 0)
+        {
+          compareTables<<<blocksFor(tot[0], 256), 256, 0, s>>>(
+              tot[0], m->res_dofs, m->state_dofs, diff);
+        }
+        int diff_h = 1;
+        cudaCheck(cudaMemcpyAsync(&diff_h, diff, sizeof(int),
+                                  cudaMemcpyDeviceToHost, s),
+                  "AssemblyMap compare readback");
+        cudaCheck(cudaStreamSynchronize(s), "AssemblyMap compare");
+        deviceFree(diff);
+        m->same_dofs = diff_h == 0;
+      }
+      cudaCheck(cudaStreamSynchronize(s), "AssemblyMap build");
+    }
+    catch (...)
+    {
+      delete m;
+      throw;
+    }
+    *out = m;
+  });
+}
+
+extern "C" int gbfem_assembly_map_get_view(const gbfem_assembly_map* m,
+                                           gbfem_assembly_map_view* info)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(m != nullptr && info != nullptr, "AssemblyMap handle is null");
+    info->num_elems     = m->num_elems;
+    info->num_res       = m->num_res;
+    info->num_states    = m->num_states;
+    info->nnz           = m->nnz;
+    info->jac_nnz       = m->jac_nnz;
+    info->max_res       = m->max_res;
+    info->max_state     = m->max_state;
+    info->max_jac       = m->max_jac;
+    info->layout_id     = m->layout_id;
+    info->res_offsets   = m->res_offsets;
+    info->res_dofs      = m->res_dofs;
+    info->state_offsets = m->state_offsets;
+    info->state_dofs    = m->state_dofs;
+    info->jac_offsets   = m->jac_offsets;
+    info->jac_map       = m->jac_map;
+    info->row_ptr       = m->row_ptr;
+    info->col_ind       = m->col_ind;
+  });
+}
+
+extern "C" void gbfem_assembly_map_destroy(gbfem_assembly_map* m)
+{
+  delete m;
+}

@@ -1,0 +1,187 @@
+/*
+ * gbfem.h — C ABI of libgbfem, the GB300 (sm_103a) implementation of femx's
+ * data-parallel assembly path.
+ *
+ * Conventions (femx v0.4.0 semantics, femx/common/Types.hpp:17-19):
+ *   - Real = double, Index = int32. Array arguments are DEVICE pointers unless
+ *     stated otherwise; sizes are element counts.
+ *   - Every call returns GBFEM_OK (0) or an error code; the message of the
+ *     last failure on the calling thread is gbfem_last_error(). The messages
+ *     are the ones femx's require() throws (femx/common/Checks.hpp:11-17).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream). Hot-path calls
+ *     (assemble, boundary operations, SpMV, VJP) only enqueue work: they do not
+ *     synchronize, allocate or read back, so they can be captured in CUDA
+ *     graphs. Map creation is setup: it allocates and synchronizes `stream`.
+ *   - Handles own their device buffers; the caller owns the stream and every
+ *     array it passes in.
+ */
+#ifndef GBFEM_H
+#define GBFEM_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define GBFEM_API __attribute__((visibility("default")))
+#else
+#define GBFEM_API
+#endif
+
+#define GBFEM_OK 0
+#define GBFEM_EINVAL 1 /* invalid argument: sizes, aliasing, layout (require) */
+#define GBFEM_ECUDA 2  /* CUDA runtime failure */
+#define GBFEM_EDATA 3  /* invalid mesh / DOF data found on the device */
+#define GBFEM_ENOMEM 4 /* device allocation failed */
+
+/* Arithmetic of the element kernels. FP64: plain double everywhere (the
+ * drop-in). FP32_QUAD: element quadrature in float, accumulation, scatter and
+ * all global vectors in double. */
+#define GBFEM_PREC_FP64 0
+#define GBFEM_PREC_FP32_QUAD 1
+
+GBFEM_API const char* gbfem_last_error(void);
+GBFEM_API int         gbfem_version(void);
+
+/* ---------------------------------------------------------------------------
+ * AssemblyMap — replaces femx::assembly::makeAssemblyMap(num_res, num_states,
+ * res_dofs, state_dofs) (femx/assembly/AssemblyMap.hpp:230-234,
+ * AssemblyMap.cpp:54-176) and copy(Host -> Device) (AssemblyMap.cpp:201-235).
+ * The CSR pattern (union of every element block, rows sorted by column,
+ * duplicates merged) and jac_map (row-major local entry -> CSR slot) are built
+ * on the GPU and are bit-identical to the reference's. Inputs are the element
+ * DOF tables in femx's flattened form (AssemblyMapView, AssemblyMap.hpp:21-68).
+ * ------------------------------------------------------------------------ */
+typedef struct gbfem_assembly_map gbfem_assembly_map;
+
+typedef struct
+{
+  int                num_elems, num_res, num_states;
+  int                nnz, jac_nnz, max_res, max_state, max_jac;
+  unsigned long long layout_id; /* femx CsrPattern::layoutId analogue */
+  const int *        res_offsets, *res_dofs, *state_offsets, *state_dofs;
+  const int *        jac_offsets, *jac_map, *row_ptr, *col_ind;
+} gbfem_assembly_map_view;
+
+GBFEM_API int  gbfem_assembly_map_create(int num_res, int num_states, int num_elems,
+                               const int* res_offsets, const int* res_dofs,
+                               const int* state_offsets, const int* state_dofs,
+                               void* stream, gbfem_assembly_map** out);
+GBFEM_API int  gbfem_assembly_map_get_view(const gbfem_assembly_map* map,
+                                 gbfem_assembly_map_view* view);
+GBFEM_API void gbfem_assembly_map_destroy(gbfem_assembly_map* map);
+/* Reads and clears the map's device status word, set by a hot-path kernel
+ * that met invalid data (a degenerate element: femx throws "Singular 2D
+ * Jacobian." from ElementValues::invJacobian, ElementValues.cpp:210-229).
+ * Synchronizes `stream`; returns GBFEM_EDATA with the message if set. */
+GBFEM_API int  gbfem_assembly_map_check(const gbfem_assembly_map* map, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * BoundaryMap — replaces femx::assembly::makeBoundaryMap(dofs, pattern)
+ * (femx/assembly/BoundaryMap.hpp:183-184, BoundaryMap.cpp:59-139) plus
+ * copy(Host -> Device) (:141-170). Built on the GPU; bc_rows, diag,
+ * col_offsets, col_entries, col_rows and bc_mask are bit-identical to the
+ * reference's. `dofs` keeps its input order (it defines bc_vals order).
+ * ------------------------------------------------------------------------ */
+typedef struct gbfem_boundary_map gbfem_boundary_map;
+
+typedef struct
+{
+  int                num_rows, num_cols, nnz, num_bcs, num_col_entries;
+  unsigned long long layout_id;
+  const int *        bc_rows, *diag, *col_offsets, *col_entries, *col_rows;
+  const int*         bc_mask;
+} gbfem_boundary_map_view;
+
+GBFEM_API int  gbfem_boundary_map_create(int num_bcs, const int* dofs, int rows, int cols,
+                               const int* row_ptr, const int* col_ind,
+                               unsigned long long layout_id, void* stream,
+                               gbfem_boundary_map** out);
+GBFEM_API int  gbfem_boundary_map_get_view(const gbfem_boundary_map* bc,
+                                 gbfem_boundary_map_view* view);
+GBFEM_API void gbfem_boundary_map_destroy(gbfem_boundary_map* bc);
+
+/* replaceRows(map, jac, diag, ctx): BoundaryMap.hpp:215-226,
+ * BoundaryMap.cu:122-141 (replaceRowsKernel). Zero constrained rows, set the
+ * diagonal to `diag`; columns untouched. */
+GBFEM_API int gbfem_replace_rows(const gbfem_boundary_map* bc, double* vals, double diag,
+                       void* stream);
+/* replaceRes(map, state, bc_vals, res, ctx): BoundaryMap.hpp:246-250,
+ * BoundaryMap.cu:69-80,155-173. res[bc_row] = state[bc_row] - bc_vals[ib]. */
+GBFEM_API int gbfem_replace_res(const gbfem_boundary_map* bc, const double* state,
+                      const double* bc_vals, double* res, void* stream);
+/* zeroBoundary(map, vals, ctx): BoundaryMap.hpp:255-258, BoundaryMap.cu:82-94. */
+GBFEM_API int gbfem_zero_boundary(const gbfem_boundary_map* bc, double* v, void* stream);
+/* prepareForwardSolve(map, solve_mat, rhs, bc_vals, ctx): BoundaryMap.hpp:
+ * 287-291, BoundaryMap.cpp:218-247, BoundaryMap.cu:192-211. Lifting
+ * rhs[r] -= A[r][c] g_c on unconstrained rows, constrained columns zeroed,
+ * constrained rows -> identity, rhs[bc] = g. Subtractions are applied in
+ * constraint order, so rhs matches the CPU reference bit for bit. */
+GBFEM_API int gbfem_prepare_forward_solve(const gbfem_boundary_map* bc, double* vals,
+                                double* rhs, const double* bc_vals,
+                                void* stream);
+
+/* ---------------------------------------------------------------------------
+ * CSR SpMV — replaces MatrixHandler<CudaCsrBackend>::matvec / matvecT
+ * (femx/linalg/handler/MatrixHandler.hpp:270-317, MatrixHandler.cu:335-398,
+ * 514-542; host semantics MatrixHandler.cpp:157-198):
+ *   y = alpha A x + beta y,   y = alpha A^T x + beta y.
+ * ------------------------------------------------------------------------ */
+GBFEM_API int gbfem_spmv(int rows, int cols, const int* row_ptr, const int* col_ind,
+               const double* vals, const double* x, double* y, double alpha,
+               double beta, void* stream);
+GBFEM_API int gbfem_spmv_t(int rows, int cols, const int* row_ptr, const int* col_ind,
+                 const double* vals, const double* x, double* y, double alpha,
+                 double beta, void* stream);
+
+/* y = a x + b y — VectorHandler<Cuda>::axpby (femx/linalg/handler/
+ * VectorHandler.cu:124-136), used by the state solvers for rhs = -res
+ * (femx/state/StateSolver.hpp:90-108). y is not read when b == 0. */
+GBFEM_API int gbfem_axpby(int n, double a, const double* x, double b, double* y,
+                void* stream);
+
+/* ---------------------------------------------------------------------------
+ * kappa-weighted P1 Poisson assembly — replaces assembly::assemble(op, geom,
+ * map, state, res, jac, ctx) (femx/assembly/CudaAssembly.hpp:319-364, CPU
+ * contract Assembly.hpp:153-226) for the element operator
+ *   K_e = kappa_e int grad N_i . grad N_j,  res_e = K_e u_e - int f_h N_i,
+ * f_h the P1 interpolant of nodal values f_nodal (NULL = no load).
+ * coords: node-major [num_nodes][2]; conn: [num_elems][3] geometry
+ * connectivity, or NULL when it equals the map's DOF table (scalar P1 space,
+ * FESpace.cpp:27-54). res [num_res] and vals [nnz] are overwritten; vals may
+ * be NULL (residual only, like assembleResidual, CudaAssembly.hpp:420-472).
+ * ------------------------------------------------------------------------ */
+GBFEM_API int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
+                            const double* coords, const int* conn,
+                            const double* kappa, const double* f_nodal,
+                            const double* u, double* res, double* vals,
+                            int precision, void* stream);
+
+/* Residual VJPs of the same operator, the transpose actions behind
+ * Residual::applyParamJacT and the state adjoint (femx/state/Residual.hpp:
+ * 55-59, femx/inverse/ReducedFunctional.hpp:94-117), without forming the
+ * Jacobian: g_u = sum_e K_e^T lam_e, g_m[e] = kappa_e lam_e^T Khat_e u_e
+ * (kappa = exp(m)). Element quadrature is recomputed. g_u [num_states] and
+ * g_m [num_elems] are overwritten; either may be NULL. */
+GBFEM_API int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
+                       const double* coords, const int* conn,
+                       const double* kappa, const double* u, const double* lam,
+                       double* g_u, double* g_m, int precision, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Taylor-Hood P2/P1 steady Navier-Stokes Newton residual + Jacobian through
+ * the same assemble contract (CudaAssembly.hpp:319-364). The map's element
+ * DOF tables follow MixedFESpace (velocity 2*node+comp, then pressure), 15 per
+ * element; conn6 [num_elems][6] = [v0 v1 v2 m01 m12 m20] in P2-node ids;
+ * coords [num_p2_nodes][2]. vals may be NULL (residual only).
+ * ------------------------------------------------------------------------ */
+GBFEM_API int gbfem_assemble_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
+                         const double* coords, const int* conn6, double nu,
+                         const double* state, double* res, double* vals,
+                         int precision, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBFEM_H */

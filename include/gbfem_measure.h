@@ -1,0 +1,26 @@
+/*
+ * gbfem_measure.h — measurement support for libgbfem's benchmark. Not part
+ * of the femx drop-in surface and without a counterpart in the reference:
+ * femx publishes no rooflines. It lets the benchmark measure the FP64 FMA
+ * ceiling of the GPU it runs on, the roof for the FP64-bound element kernels.
+ */
+#ifndef GBFEM_MEASURE_H
+#define GBFEM_MEASURE_H
+
+#include "gbfem.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Runs `blocks` x `threads` threads, each doing `iters` x 8 independent FP64
+ * FMAs; writes one value per thread to `out` (device, blocks*threads
+ * doubles) so the work is not elided. FLOPs = 16 * iters * blocks * threads. */
+GBFEM_API int gbfem_probe_fp64_fma(int blocks, int threads, int iters,
+                                   double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -22,7 +22,8 @@ def build(force: bool = False) -> str:
     """Compile liboracle.so with g++ (portable flags: x86 and aarch64)."""
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC):
         subprocess.check_call([
-            "g++", "-std=c++17", "-O2", "-fPIC", "-shared", SRC, "-o", LIB_PATH,
+            "g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", SRC, "-o",
+            LIB_PATH,
         ])
     return LIB_PATH
 

@@ -1,0 +1,366 @@
+"""GPU parity: libgbfem (through its C ABI) against the CPU oracle and the
+reference's golden vectors.
+
+Gates (femx semantics):
+  * CSR row_ptr/col_ind, jac_map, Dirichlet sets and BoundaryMap arrays:
+    bit-exact.
+  * FP64 values/residuals/VJPs: ||d||_inf / ||ref||_inf <= 1e-12.
+  * FP32-quadrature values: <= 1e-6.
+  * prepareForwardSolve on identical inputs: bit-exact (vals and rhs).
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from conftest import load_golden, rel_inf  # noqa: E402
+from femx_gb300 import assembly as A  # noqa: E402
+from femx_gb300 import meshes  # noqa: E402
+from oracle import pyoracle as orc  # noqa: E402
+
+TOL64 = 1e-12
+TOL32 = 1e-6
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from femx_gb300 import build
+    build.build()
+
+
+def dev(a, dtype=None):
+    a = np.ascontiguousarray(a)
+    t = torch.from_numpy(a)
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def gpu_map(num_res, num_states, ro, rd, so, sd):
+    return A.makeAssemblyMap(num_res, num_states, dev(ro, torch.int32), dev(rd, torch.int32),
+                             dev(so, torch.int32), dev(sd, torch.int32))
+
+
+def assert_map_equal(m, ref_row_ptr, ref_col_ind, ref_jac_map):
+    p = m.pattern()
+    np.testing.assert_array_equal(host(p.row_ptr), ref_row_ptr)
+    np.testing.assert_array_equal(host(p.col_ind), ref_col_ind)
+    np.testing.assert_array_equal(host(m.view()["jac_map"]), ref_jac_map)
+
+
+# ---------------------------------------------------------------- patterns
+
+def test_known_answer_maps():
+    kat = load_golden("kat")
+    m = gpu_map(3, 3, [0, 2, 4], [0, 1, 1, 2], [0, 2, 4], [0, 1, 1, 2])
+    assert_map_equal(m, kat["shared_row_ptr"], kat["shared_col_ind"], kat["shared_jac_map"])
+    m = gpu_map(2, 2, [0, 2, 3], [0, 1, 1], [0, 1, 3], [0, 0, 1])
+    assert_map_equal(m, kat["rect_row_ptr"], kat["rect_col_ind"], kat["rect_jac_map"])
+    np.testing.assert_array_equal(host(m.view()["jac_offsets"]), [0, 2, 4])
+
+
+@pytest.mark.parametrize("case", ["p1_32", "p1_jit9"])
+def test_p1_pattern_matches_reference(case):
+    g = load_golden(case)
+    offs, dofs = meshes.scalar_elem_dofs(g["conn"])
+    n = g["coords"].shape[0]
+    m = gpu_map(n, n, offs, dofs, offs, dofs)
+    assert_map_equal(m, g["row_ptr"], g["col_ind"], g["jac_map"])
+    np.testing.assert_array_equal(host(m.view()["jac_offsets"]), g["jac_offsets"])
+
+
+@pytest.mark.parametrize("case", ["th_4", "th_jit3"])
+def test_th_pattern_matches_reference(case):
+    g = load_golden(case)
+    nd = int(g["num_dofs"])
+    offs = (np.arange(g["conn6"].shape[0] + 1) * 15).astype(np.int32)
+    m = gpu_map(nd, nd, offs, g["elem_dofs"], offs, g["elem_dofs"])
+    assert_map_equal(m, g["row_ptr"], g["col_ind"], g["jac_map"])
+
+
+@pytest.mark.parametrize("nx,jitter", [(96, False), (64, True)])
+def test_p1_pattern_matches_oracle_larger(nx, jitter):
+    coords, conn = meshes.jittered_tri(nx, seed=nx) if jitter else meshes.structured_tri(nx)
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    n = coords.shape[0]
+    ref = orc.AssemblyMap(n, n, offs, dofs, offs, dofs)
+    m = gpu_map(n, n, offs, dofs, offs, dofs)
+    assert_map_equal(m, ref.row_ptr, ref.col_ind, ref.jac_map)
+
+
+def test_th_pattern_matches_oracle_16():
+    c3, k3 = meshes.jittered_tri(16, seed=3)
+    cp2, conn6, _ = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    ref = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    assert_map_equal(m, ref.row_ptr, ref.col_ind, ref.jac_map)
+
+
+def test_rectangular_variable_blocks_match_oracle():
+    rng = np.random.default_rng(5)
+    e, nr_glob, ns_glob = 300, 120, 90
+    nrs = rng.integers(0, 5, size=e)
+    nss = rng.integers(1, 6, size=e)
+    ro = np.concatenate([[0], np.cumsum(nrs)]).astype(np.int32)
+    so = np.concatenate([[0], np.cumsum(nss)]).astype(np.int32)
+    rd = rng.integers(0, nr_glob, size=ro[-1]).astype(np.int32)  # duplicates allowed
+    sd = rng.integers(0, ns_glob, size=so[-1]).astype(np.int32)
+    ref = orc.AssemblyMap(nr_glob, ns_glob, ro, rd, so, sd)
+    m = gpu_map(nr_glob, ns_glob, ro, rd, so, sd)
+    assert_map_equal(m, ref.row_ptr, ref.col_ind, ref.jac_map)
+    assert m.maxRes() == ref.max_res and m.maxState() == ref.max_state
+    assert m.maxJac() == ref.max_jac
+
+
+def test_empty_map():
+    m = gpu_map(4, 4, [0], [], [0], [])
+    assert m.numElems() == 0 and m.pattern().nnz == 0
+    np.testing.assert_array_equal(host(m.pattern().row_ptr), [0, 0, 0, 0, 0])
+
+
+def test_map_rejects_bad_dofs():
+    with pytest.raises(A.GbfemError, match="residual DOF is out of range"):
+        gpu_map(2, 2, [0, 1], [2], [0, 1], [0])
+    with pytest.raises(A.GbfemError, match="state DOF is out of range"):
+        gpu_map(2, 2, [0, 1], [0], [0, 1], [-1])
+    with pytest.raises(A.GbfemError, match="non-negative"):
+        gpu_map(2, 2, [0, 2, 1], [0, 1], [0, 1, 2], [0, 1])
+
+
+# ---------------------------------------------------------------- boundary
+
+DENSE_ROW_PTR = np.array([0, 3, 6, 9], np.int32)
+DENSE_COL_IND = np.array([0, 1, 2, 0, 1, 2, 0, 1, 2], np.int32)
+DENSE_VALS = np.array([4.0, 1.0, 2.0, 3.0, 5.0, 6.0, 7.0, 8.0, 9.0])
+
+
+def dense_pattern():
+    return A.CsrPattern(3, 3, dev(DENSE_ROW_PTR), dev(DENSE_COL_IND), 0)
+
+
+@pytest.mark.parametrize("bcs,g,tag", [([1], [2.0], "bc1_"), ([0, 2], [2.0, -1.0], "bc02_")])
+def test_boundary_known_answers(bcs, g, tag):
+    kat = load_golden("kat")
+    pat = dense_pattern()
+    bc = A.makeBoundaryMap(dev(np.array(bcs, np.int32)), pat)
+    for d, key in ((1.0, "rows1"), (0.0, "rows0")):
+        mat = A.CsrMatrix(pat, dev(DENSE_VALS))
+        A.replaceRows(bc, mat, d)
+        np.testing.assert_array_equal(host(mat.vals), kat[tag + key])
+    res = dev(np.array([10.0, 20.0, 30.0]))
+    A.replaceRes(bc, dev(np.array([4.0, 7.0, 9.0])), dev(np.array(g)), res)
+    np.testing.assert_array_equal(host(res), kat[tag + "res"])
+    mat = A.CsrMatrix(pat, dev(DENSE_VALS))
+    rhs = dev(np.array([10.0, 20.0, 30.0]))
+    A.prepareForwardSolve(bc, mat, rhs, dev(np.array(g)))
+    np.testing.assert_array_equal(host(mat.vals), kat[tag + "fwd_vals"])
+    np.testing.assert_array_equal(host(rhs), kat[tag + "fwd_rhs"])
+
+
+def test_boundary_rejects_bad_input():
+    pat = dense_pattern()
+    with pytest.raises(A.GbfemError, match="must be unique"):
+        A.makeBoundaryMap(dev(np.array([1, 1], np.int32)), pat)
+    with pytest.raises(A.GbfemError, match="out of range"):
+        A.makeBoundaryMap(dev(np.array([3], np.int32)), pat)
+    nodiag = A.CsrPattern(2, 2, dev(np.array([0, 1, 2], np.int32)),
+                          dev(np.array([1, 0], np.int32)), 0)
+    with pytest.raises(A.GbfemError, match="no diagonal entry"):
+        A.makeBoundaryMap(dev(np.array([0], np.int32)), nodiag)
+    bc = A.makeBoundaryMap(dev(np.array([1], np.int32)), pat)
+    other = A.CsrMatrix(A.CsrPattern(3, 3, pat.row_ptr, pat.col_ind, 99), dev(DENSE_VALS))
+    with pytest.raises(A.GbfemError, match="does not match the mapped CSR layout"):
+        A.replaceRows(bc, other, 1.0)
+
+
+# ---------------------------------------------------------------- P1 Poisson
+
+def p1_setup(coords, conn):
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    n = coords.shape[0]
+    return gpu_map(n, n, offs, dofs, offs, dofs), orc.AssemblyMap(n, n, offs, dofs, offs, dofs)
+
+
+def p1_gpu(m, coords, kappa, f, u, precision="fp64"):
+    res = torch.zeros(m.numRes(), dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleP1Kappa(m, dev(coords), dev(kappa), None if f is None else dev(f), dev(u), res,
+                      jac, precision=precision)
+    m.check()
+    return host(res), host(jac.vals), jac, res
+
+
+@pytest.mark.parametrize("case", ["p1_32", "p1_jit9"])
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32_quad", TOL32)])
+def test_p1_assembly_matches_reference(case, precision, tol):
+    g = load_golden(case)
+    m, _ = p1_setup(g["coords"], g["conn"])
+    res, vals, _, _ = p1_gpu(m, g["coords"], g["kappa"], g["f"], g["u"], precision)
+    assert rel_inf(res, g["res"]) <= tol
+    assert rel_inf(vals, g["vals"]) <= tol
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32_quad", TOL32)])
+def test_p1_assembly_grf_kappa_matches_oracle(precision, tol):
+    coords, conn = meshes.jittered_tri(128, seed=2)
+    e, n = conn.shape[0], coords.shape[0]
+    kappa = np.exp(meshes.grf_centroids(coords, conn, seed=2, ell=0.05))
+    f = meshes.fourier_source(coords, 1)
+    u = np.random.default_rng(0).standard_normal(n)
+    m, om = p1_setup(coords, conn)
+    q = orc.P1Quad(coords, conn)
+    rres, rvals = orc.assemble_p1_kappa(om, q, kappa, f, u)
+    res, vals, _, _ = p1_gpu(m, coords, kappa, f, u, precision)
+    assert rel_inf(res, rres) <= tol
+    assert rel_inf(vals, rvals) <= tol
+    # residual-only call gives the same residual
+    r2 = torch.zeros(n, dtype=torch.float64, device="cuda")
+    A.assembleP1Kappa(m, dev(coords), dev(kappa), dev(f), dev(u), r2, None, precision=precision)
+    assert rel_inf(host(r2), rres) <= tol
+
+
+def test_p1_separate_connectivity_matches():
+    g = load_golden("p1_jit9")
+    m, _ = p1_setup(g["coords"], g["conn"])
+    res = torch.zeros(m.numRes(), dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleP1Kappa(m, dev(g["coords"]), dev(g["kappa"]), dev(g["f"]), dev(g["u"]), res, jac,
+                      conn=dev(g["conn"], torch.int32))
+    assert rel_inf(host(res), g["res"]) <= TOL64
+    assert rel_inf(host(jac.vals), g["vals"]) <= TOL64
+
+
+def test_p1_degenerate_element_is_reported():
+    coords, conn = meshes.structured_tri(4)
+    coords = coords.copy()
+    conn = conn.copy()
+    conn[5] = [conn[5][0], conn[5][0], conn[5][2]]  # zero-area element
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    n = coords.shape[0]
+    m = gpu_map(n, n, offs, dofs, offs, dofs)
+    res = torch.zeros(n, dtype=torch.float64, device="cuda")
+    A.assembleP1Kappa(m, dev(coords), dev(np.ones(conn.shape[0])), None, dev(np.zeros(n)), res)
+    with pytest.raises(A.GbfemError, match="Singular 2D Jacobian"):
+        m.check()
+    m.check()  # the status word was cleared
+
+
+@pytest.mark.parametrize("case", ["p1_32", "p1_jit9"])
+def test_boundary_map_and_operations_match_reference(case):
+    g = load_golden(case)
+    m, om = p1_setup(g["coords"], g["conn"])
+    dofs_bc = meshes.dirichlet_dofs(g["coords"], meshes.boundary_nodes(g["coords"]))
+    np.testing.assert_array_equal(dofs_bc, g["bc_dofs"])
+    bc = A.makeBoundaryMap(dev(dofs_bc), m.pattern())
+    v = bc.view()
+    for key, ref in (("bc_rows", "bc_rows"), ("diag", "bc_diag"), ("col_offsets", "bc_col_offsets"),
+                     ("col_entries", "bc_col_entries"), ("col_rows", "bc_col_rows"),
+                     ("bc_mask", "bc_mask")):
+        np.testing.assert_array_equal(host(v[key]), g[ref])
+    pat = m.pattern()
+    # replaceRows on the reference's own matrix values: bit-exact
+    mat = A.CsrMatrix(pat, dev(g["vals"]))
+    A.replaceRows(bc, mat, 1.0)
+    np.testing.assert_array_equal(host(mat.vals), g["vals_rows1"])
+    res = dev(g["res"])
+    A.replaceRes(bc, dev(g["u"]), dev(g["bc_vals"]), res)
+    np.testing.assert_array_equal(host(res), g["res_replaced"])
+    mat = A.CsrMatrix(pat, dev(g["vals"]))
+    rhs = dev(-g["res"])
+    A.prepareForwardSolve(bc, mat, rhs, dev(g["bc_vals"]))
+    np.testing.assert_array_equal(host(mat.vals), g["vals_fwd"])
+    np.testing.assert_array_equal(host(rhs), g["rhs_fwd"])
+    z = dev(g["u"])
+    A.zeroBoundary(bc, z)
+    expect = g["u"].copy()
+    expect[g["bc_dofs"]] = 0.0
+    np.testing.assert_array_equal(host(z), expect)
+
+
+# ---------------------------------------------------------------- SpMV
+
+@pytest.mark.parametrize("case", ["p1_32", "p1_jit9"])
+def test_spmv_matches_reference(case):
+    g = load_golden(case)
+    m, _ = p1_setup(g["coords"], g["conn"])
+    mat = A.CsrMatrix(m.pattern(), dev(g["vals"]))
+    n = g["coords"].shape[0]
+    y = torch.zeros(n, dtype=torch.float64, device="cuda")
+    A.matvec(mat, dev(g["x"]), y)
+    assert rel_inf(host(y), g["y_matvec"]) <= 1e-13
+    yt = torch.zeros(n, dtype=torch.float64, device="cuda")
+    A.matvecT(mat, dev(g["x"]), yt)
+    assert rel_inf(host(yt), g["y_matvec_t"]) <= 1e-13
+    # alpha/beta semantics
+    y0 = np.random.default_rng(1).standard_normal(n)
+    y = dev(y0)
+    A.matvec(mat, dev(g["x"]), y, alpha=2.0, beta=-0.5)
+    assert rel_inf(host(y), orc.matvec(g["row_ptr"], g["col_ind"], g["vals"], g["x"], y0, 2.0,
+                                       -0.5)) <= 1e-13
+    y = dev(y0)
+    A.matvecT(mat, dev(g["x"]), y, alpha=-1.0, beta=3.0)
+    assert rel_inf(host(y), orc.matvec_t(g["row_ptr"], g["col_ind"], g["vals"], g["x"], n, y0,
+                                         -1.0, 3.0)) <= 1e-13
+
+
+# ---------------------------------------------------------------- VJP
+
+@pytest.mark.parametrize("case", ["p1_32", "p1_jit9"])
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32_quad", TOL32)])
+def test_vjp_matches_reference(case, precision, tol):
+    g = load_golden(case)
+    m, _ = p1_setup(g["coords"], g["conn"])
+    n, e = g["coords"].shape[0], g["conn"].shape[0]
+    g_u = torch.zeros(n, dtype=torch.float64, device="cuda")
+    g_m = torch.zeros(e, dtype=torch.float64, device="cuda")
+    A.vjpP1Kappa(m, dev(g["coords"]), dev(g["kappa"]), dev(g["u"]), dev(g["lam"]), g_u, g_m,
+                 precision=precision)
+    assert rel_inf(host(g_u), g["g_u"]) <= tol
+    assert rel_inf(host(g_m), g["g_m"]) <= tol
+
+
+# ---------------------------------------------------------------- Taylor-Hood
+
+def th_gpu(g_coords, conn6, elem_dofs, nd, nu, state, precision="fp64"):
+    offs = (np.arange(conn6.shape[0] + 1) * 15).astype(np.int32)
+    m = gpu_map(nd, nd, offs, elem_dofs, offs, elem_dofs)
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleTaylorHood(m, dev(g_coords), dev(conn6, torch.int32), nu, dev(state), res, jac,
+                         precision=precision)
+    m.check()
+    return m, host(res), host(jac.vals)
+
+
+@pytest.mark.parametrize("case", ["th_4", "th_jit3"])
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32_quad", TOL32)])
+def test_taylor_hood_matches_reference(case, precision, tol):
+    g = load_golden(case)
+    _, res, vals = th_gpu(g["coords"], g["conn6"], g["elem_dofs"], int(g["num_dofs"]),
+                          float(g["nu"]), g["state"], precision)
+    assert rel_inf(res, g["res"]) <= tol
+    assert rel_inf(vals, g["vals"]) <= tol
+
+
+def test_taylor_hood_cavity_matches_oracle():
+    c3, k3 = meshes.structured_tri(24)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    vel = meshes.stream_velocity(cp2, seed=3)
+    state = np.concatenate([vel.reshape(-1), np.random.default_rng(3).standard_normal(nv)])
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-3, state)
+    for precision, tol in (("fp64", TOL64), ("fp32_quad", TOL32)):
+        _, res, vals = th_gpu(cp2, conn6, dofs, nd, 1e-3, state, precision)
+        assert rel_inf(res, rres) <= tol
+        assert rel_inf(vals, rvals) <= tol
