@@ -67,7 +67,7 @@ class _CudaArray:
 
     def __init__(self, ptr, n, typestr):
         self.__cuda_array_interface__ = {
-            "shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), True),
+            "shape": (int(n),), "typestr": typestr, "data": (int(ptr or 0), False),
             "version": 3, "strides": None,
         }
 

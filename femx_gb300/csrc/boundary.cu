@@ -17,6 +17,34 @@ namespace
 {
 using gbfem::DeviceStatus;
 
+// femx's CsrPattern validates monotone row pointers and column ranges on
+// construction (femx/linalg/CsrPattern.hpp:42-217); a caller-supplied
+// pattern is checked here before any column index is used.
+__global__ void validatePattern(int rows, int cols, const int* __restrict__ row_ptr,
+                                const int* __restrict__ col_ind, DeviceStatus* st)
+{
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows)
+  {
+    return;
+  }
+  const int k0 = row_ptr[r], k1 = row_ptr[r + 1];
+  if (k1 < k0 || (r == 0 && k0 != 0))
+  {
+    gbfem::devFail(st, gbfem::kDevPatternInvalid, r);
+    return;
+  }
+  for (int k = k0; k < k1; ++k)
+  {
+    const int c = col_ind[k];
+    if (c < 0 || c >= cols)
+    {
+      gbfem::devFail(st, gbfem::kDevPatternInvalid, r);
+      return;
+    }
+  }
+}
+
 __global__ void flagConstraints(int nb, int rows, const int* __restrict__ dofs,
                                 int* __restrict__ bc_by_col,
                                 int* __restrict__ bc_rows,
@@ -369,6 +397,13 @@ extern "C" int gbfem_boundary_map_create(int num_bcs, const int* dofs, int rows,
       sc.p[6]         = row_rank;
 
       cudaCheck(cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s), "memset");
+      if (rows > 0)
+      {
+        validatePattern<<<blocksFor(rows, 256), 256, 0, s>>>(rows, cols, row_ptr,
+                                                             col_ind, status);
+        cudaCheck(cudaGetLastError(), "BoundaryMap pattern check launch");
+      }
+      checkDeviceStatus(status, s);
       if (cols > 0)
       {
         cudaCheck(cudaMemsetAsync(bc_by_col, 0xff, sizeof(int) * cols, s), "memset");

@@ -119,6 +119,8 @@ enum DeviceErr : int
   kDevBcDupDiag         = 7,
   kDevSingularJacobian  = 8,
   kDevRowOverflow       = 9,
+  kDevPatternInvalid    = 10,
+  kDevNodeRange         = 11,
 };
 
 __device__ inline void devFail(DeviceStatus* st, int code, int index)

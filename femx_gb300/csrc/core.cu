@@ -220,6 +220,10 @@ const char* deviceErrorMessage(int code)
     return "Singular 2D Jacobian.";
   case kDevRowOverflow:
     return "AssemblyMap row exceeds the supported candidate count";
+  case kDevPatternInvalid:
+    return "CSR pattern row pointers or column indices are invalid";
+  case kDevNodeRange:
+    return "Geometry element connectivity is out of range";
   default:
     return "unknown device error";
   }

@@ -23,6 +23,7 @@ using gbfem::DeviceStatus;
 struct P1Args
 {
   int                  ne;
+  int                  num_nodes;
   const int*           dofs;   // res/state DOF table [ne][3]
   const int*           conn;   // geometry connectivity, or == dofs
   const double2*       coords; // [num_nodes]
@@ -85,6 +86,13 @@ __global__ void __launch_bounds__(256) p1AssembleKernel(P1Args a)
     n0 = a.conn[3 * e + 0];
     n1 = a.conn[3 * e + 1];
     n2 = a.conn[3 * e + 2];
+    if (static_cast<unsigned>(n0) >= static_cast<unsigned>(a.num_nodes)
+        || static_cast<unsigned>(n1) >= static_cast<unsigned>(a.num_nodes)
+        || static_cast<unsigned>(n2) >= static_cast<unsigned>(a.num_nodes))
+    {
+      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+      return;
+    }
   }
   ElemK<T> K;
   if (!elementK<T>(a.coords[n0], a.coords[n1], a.coords[n2], a.kappa[e], K))
@@ -140,6 +148,13 @@ __global__ void __launch_bounds__(256)
     n0 = a.conn[3 * e + 0];
     n1 = a.conn[3 * e + 1];
     n2 = a.conn[3 * e + 2];
+    if (static_cast<unsigned>(n0) >= static_cast<unsigned>(a.num_nodes)
+        || static_cast<unsigned>(n1) >= static_cast<unsigned>(a.num_nodes)
+        || static_cast<unsigned>(n2) >= static_cast<unsigned>(a.num_nodes))
+    {
+      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+      return;
+    }
   }
   ElemK<T> K;
   if (!elementK<T>(a.coords[n0], a.coords[n1], a.coords[n2], a.kappa[e], K))
@@ -204,7 +219,8 @@ P1Args makeArgs(const gbfem_assembly_map* map, int num_nodes,
   require(conn != nullptr || num_nodes == map->num_states,
           "Geometry and AssemblyMap have different node counts");
   P1Args a{};
-  a.ne      = map->num_elems;
+  a.ne        = map->num_elems;
+  a.num_nodes = num_nodes;
   a.dofs    = map->state_dofs;
   a.conn    = conn;
   a.coords  = reinterpret_cast<const double2*>(coords);

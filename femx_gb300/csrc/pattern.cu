@@ -26,6 +26,22 @@ using gbfem::DeviceStatus;
 constexpr int kWarpsPerBlock = 8;
 constexpr int kStageCap      = 512; // candidates staged in shared memory per warp
 
+// Offsets must start at 0 and be non-decreasing; checked before any DOF
+// table is read, so no later kernel can index past the copied tables.
+__global__ void validateOffsets(int ne, const int* __restrict__ ro,
+                                const int* __restrict__ so, DeviceStatus* st)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ne)
+  {
+    return;
+  }
+  if (ro[e + 1] < ro[e] || so[e + 1] < so[e] || (e == 0 && (ro[0] != 0 || so[0] != 0)))
+  {
+    gbfem::devFail(st, gbfem::kDevNegativeLocal, e);
+  }
+}
+
 __global__ void countCandidates(int ne, int num_res, int num_states,
                                 const int* __restrict__ ro,
                                 const int* __restrict__ rd,
@@ -42,12 +58,6 @@ __global__ void countCandidates(int ne, int num_res, int num_states,
   }
   const int r0 = ro[e], r1 = ro[e + 1], s0 = so[e], s1 = so[e + 1];
   const int nr = r1 - r0, nc = s1 - s0;
-  if (nr < 0 || nc < 0 || (e == 0 && (r0 != 0 || s0 != 0)))
-  {
-    gbfem::devFail(st, gbfem::kDevNegativeLocal, e);
-    elem_jac[e] = 0;
-    return;
-  }
   elem_jac[e] = static_cast<long long>(nr) * nc;
   atomicMax(&stats[0], nr);
   atomicMax(&stats[1], nc);
@@ -334,6 +344,13 @@ extern "C" int gbfem_assembly_map_create(int num_res, int num_states,
       cudaCheck(cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s), "memset");
       cudaCheck(cudaMemsetAsync(row_cand, 0, sizeof(int) * (num_res + 1LL), s),
                 "memset");
+      if (num_elems > 0)
+      {
+        validateOffsets<<<blocksFor(num_elems, 256), 256, 0, s>>>(
+            num_elems, m->res_offsets, m->state_offsets, status);
+        cudaCheck(cudaGetLastError(), "AssemblyMap offsets launch");
+      }
+      checkDeviceStatus(status, s);
       if (num_elems > 0)
       {
         countCandidates<<<blocksFor(num_elems, 256), 256, 0, s>>>(

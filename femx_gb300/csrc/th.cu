@@ -113,6 +113,7 @@ __device__ __forceinline__ const ThTablesF& tables(float)
 struct ThArgs
 {
   int            ne;
+  int            num_nodes;
   const int*     dofs;  // [ne][15]
   const int*     conn6; // [ne][6]
   const double2* coords;
@@ -152,7 +153,25 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
   {
     S.st[l] = T(a.state[a.dofs[15 * e + l]]);
   }
+  bool nodes_ok = true;
   if (has && l == 15)
+  {
+    for (int k = 0; k < 6; ++k)
+    {
+      nodes_ok = nodes_ok
+                 && static_cast<unsigned>(a.conn6[6 * e + k])
+                        < static_cast<unsigned>(a.num_nodes);
+    }
+    if (!nodes_ok)
+    {
+      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+    }
+  }
+  if (has && l == 15 && !nodes_ok)
+  {
+    S.ok = 0;
+  }
+  else if (has && l == 15)
   {
     const double2 x0 = a.coords[a.conn6[6 * e + 0]];
     const double2 x1 = a.coords[a.conn6[6 * e + 1]];
@@ -356,7 +375,8 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
       return;
     }
     ThArgs a{};
-    a.ne      = map->num_elems;
+    a.ne        = map->num_elems;
+    a.num_nodes = num_p2_nodes;
     a.dofs    = map->state_dofs;
     a.conn6   = conn6;
     a.coords  = reinterpret_cast<const double2*>(coords);
