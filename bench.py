@@ -1,25 +1,30 @@
 """Benchmark of the femx assembly hot path on GB300.
 
-Workload (default, one GPU): P1 Poisson on a structured 1024x1024 grid split
-into 2,097,152 triangles (1,050,625 nodes, 7,346,177 nonzeros), FP64,
-per-element conductivity kappa = exp(g) with g a seeded Gaussian random field
-(correlation length 0.05, variance 1), Fourier-mode source, homogeneous
-Dirichlet data on the boundary. One step is the reference's forward-solve
-preparation plus a Krylov-like product chain:
-    assemble residual + Jacobian (CSR)   (assembly::assemble)
-    rhs = -res                           (VectorHandler::axpby)
-    prepareForwardSolve                  (BoundaryMap lifting)
-    10 x CSR SpMV, x <- A x / 8          (MatrixHandler::matvec)
-Synthetic seeded inputs stand in for real data (no dataset is involved).
-
-value   elements/s, inputs resident in HBM, CUDA events on the launch stream,
-        L2 flushed (512 MB write) before every step, outside the events.
-e2e     the same steps through the public API with pinned host buffers:
-        kappa, f, u copied in and rhs, x copied out inside the timed region.
---impl reference: the CPU oracle (a serial restatement of femx's own CPU
-        path, which has no threading) on the host cores, same workload.
-Multi-GPU (torchrun): replicas only — each rank runs its own instance, no
-collective on the data path; value = all ranks' elements / max time.
+Headline workload (one GPU): incompressible Navier-Stokes lid-driven cavity,
+Taylor-Hood P2/P1 on a structured 256x256 triangulation (131,072 elements,
+526,338 velocity + 66,049 pressure DOFs, 17,526,281 nonzeros), Re = 1000
+(nu = 1e-3). One step assembles the Newton Jacobian and residual at a
+seeded iterate (stream-function velocity, N(0,1) pressure) and applies the
+Dirichlet rows (lid u = (1,0), no-slip walls, pressure pinned at vertex 0)
+with replaceRes + replaceRows(diag 1), as ConstrainedTimeResidual does.
+  value          elements/s of the FP32-quadrature / FP64-accumulation path
+  fp64_plain     the same step on the plain FP64 path (the drop-in)
+  rel_err        ||J - J_fp64||inf/||J_fp64||inf of the fast path, full size;
+                 and the plain path against the CPU oracle on a 64x64 mesh
+Sub-results in the same line:
+  vjp            P1 Poisson 512x512 (524,288 elements): residual VJP w.r.t.
+                 the state and the per-element control m = log kappa,
+                 grads/s (one gradient = both VJPs once)
+  poisson        P1 Poisson 1024x1024 FP64: assembly + rhs = -res +
+                 prepareForwardSolve + 10 SpMVs, elements/s
+Inputs are seeded synthetic fields with the configured shapes (no dataset).
+Timing: CUDA events on the launch stream, 512 MB L2 flush before each step
+(outside the events), warm-up steps untimed. e2e: same step through the
+public API with the state copied in from pinned host memory and the
+residual copied out inside the timed region.
+--impl reference: the CPU oracle (serial restatement of femx's CPU assembly
+loop, which is single-threaded) on the host, same headline workload.
+Multi-GPU (torchrun): replicas only; value = all ranks' elements / max time.
 """
 from __future__ import annotations
 
@@ -36,17 +41,16 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "NS P2/P1 Jacobian elems/s & VJP grads/s vs plain FP64 GPU path at stated rel err"
-NX = 1024
-NSPMV = 10
-SPMV_SCALE = 0.125
+TH_NX, NU = 256, 1.0e-3
+VJP_NX = 512
+POISSON_NX, NSPMV, SPMV_SCALE = 1024, 10, 0.125
 
 
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as fh:
-            d = json.load(fh)
-        return float(d["hbm_gbs"]), "measured"
+            return float(json.load(fh)["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
 
 
@@ -58,27 +62,50 @@ def traffic_table():
     return {}
 
 
-def make_inputs():
-    from femx_gb300 import meshes
-    coords, conn = meshes.structured_tri(NX)
-    kappa = np.exp(meshes.grf_centroids(coords, conn, seed=2, ell=0.05, var=1.0, grid=1024))
-    f = meshes.fourier_source(coords, 1)
-    u = np.zeros(coords.shape[0])
-    bdofs = meshes.dirichlet_dofs(coords, meshes.boundary_nodes(coords))
-    g = np.zeros(len(bdofs))
-    return coords, conn, kappa, f, u, bdofs, g
+# ------------------------------------------------------------------ inputs
 
+def th_inputs(nx):
+    from femx_gb300 import meshes
+    c3, k3 = meshes.structured_tri(nx)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    state = meshes.cavity_state(cp2, nv, seed=3)
+    bdofs, bvals = meshes.cavity_dirichlet(cp2, cp2.shape[0])
+    return dict(coords=cp2, conn6=conn6, nv=nv, offs=offs, dofs=dofs, nd=nd, state=state,
+                bdofs=bdofs, bvals=bvals)
+
+
+def p1_inputs(nx, seed_kappa=2):
+    from femx_gb300 import meshes
+    coords, conn = meshes.structured_tri(nx)
+    kappa = np.exp(meshes.grf_centroids(coords, conn, seed=seed_kappa, ell=0.05, var=1.0,
+                                        grid=max(512, nx)))
+    f = meshes.fourier_source(coords, 1)
+    bdofs = meshes.dirichlet_dofs(coords, meshes.boundary_nodes(coords))
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    return dict(coords=coords, conn=conn, kappa=kappa, f=f, bdofs=bdofs, offs=offs, dofs=dofs)
+
+
+def th_config():
+    from femx_gb300 import meshes
+    c = meshes.structured_counts(TH_NX)
+    return {"workload": f"ns_taylor_hood_p2p1_cavity_{TH_NX}x{TH_NX}_newton_jacobian_residual",
+            "elements": c["elems"], "velocity_dofs": 2 * (c["nodes"] + c["edges"]),
+            "pressure_dofs": c["nodes"], "nnz": 17526281, "Re": 1000,
+            "precision": "fp32 element quadrature, fp64 accumulation/scatter/vectors",
+            "bcs": "lid u=(1,0), no-slip walls, pressure pin; replaceRes + replaceRows",
+            "l2": "flushed (512 MB write) before each step"}
+
+
+# ------------------------------------------------------------------ clocks
 
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
-
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index):
-        self.index = index
-        self.proc = None
+        self.index, self.proc, self.out = index, None, ""
 
     def __enter__(self):
         try:
@@ -91,7 +118,6 @@ class Clocks:
         return self
 
     def __exit__(self, *exc):
-        self.out = ""
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -121,46 +147,25 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def fp64_peak_tflops(torch, A_lib):
-    """Measured FP64 FMA ceiling (TFLOP/s) of this GPU."""
-    import ctypes as C
-    props = torch.cuda.get_device_properties(0)
-    blocks, threads, iters = props.multi_processor_count * 16, 256, 4096
-    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
-    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    call = A_lib.lib().gbfem_probe_fp64_fma
-    for _ in range(2):
-        A_lib.check(call(blocks, threads, iters, C.c_void_p(out.data_ptr()), s))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record()
-    A_lib.check(call(blocks, threads, iters, C.c_void_p(out.data_ptr()), s))
-    e1.record()
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) * 1e-3
-    return 16.0 * iters * blocks * threads / t / 1e12
+# ------------------------------------------------------------------ reference arm
 
-
-def run_reference(args, rank):
-    """CPU oracle arm: same workload, serial restatement of femx's CPU path."""
+def run_reference(args):
     from oracle import pyoracle as orc
-    from femx_gb300 import meshes
-    coords, conn, kappa, f, u, bdofs, g = make_inputs()
-    n, e = coords.shape[0], conn.shape[0]
-    offs, dofs = meshes.scalar_elem_dofs(conn)
+    d = th_inputs(TH_NX)
+    nd = d["nd"]
     t0 = time.perf_counter()
-    om = orc.AssemblyMap(n, n, offs, dofs, offs, dofs)
-    q = orc.P1Quad(coords, conn)
-    ob = orc.BoundaryMap(bdofs, om.row_ptr, om.col_ind)
+    om = orc.AssemblyMap(nd, nd, d["offs"], d["dofs"], d["offs"], d["dofs"])
+    th = orc.THQuad(d["coords"], d["conn6"])
+    ob = orc.BoundaryMap(d["bdofs"], om.row_ptr, om.col_ind)
     setup_s = time.perf_counter() - t0
-    x0 = np.random.default_rng(5).standard_normal(n)
+    e = d["conn6"].shape[0]
+    res = np.zeros(nd)
+    vals = np.zeros(om.nnz)
 
     def step():
-        res, vals = orc.assemble_p1_kappa(om, q, kappa, f, u)
-        vals, rhs = ob.prepare_forward_solve(vals, -res, g)
-        x = rhs
-        for _ in range(NSPMV):
-            x = orc.matvec(om.row_ptr, om.col_ind, vals, x, alpha=SPMV_SCALE)
-        return x
+        orc.assemble_th_range(om, th, NU, d["state"], 0, -1, res, vals)
+        orc.lib().orc_replace_res(ob.h, d["state"], d["bvals"], res)
+        orc.lib().orc_replace_rows(ob.h, ob.row_ptr, vals, 1.0)
 
     for _ in range(args.warmup):
         step()
@@ -169,31 +174,58 @@ def run_reference(args, rank):
         step()
     dt = (time.perf_counter() - t0) / args.steps
     value = e / dt
-    line = {
+    print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "elements/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": config_block(),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "config": th_config(),
         "cpu_baseline": {"value": value, "unit": "elements/s", "cores": 1, "kind": "port",
-                         "sample": f"full workload, {args.steps} steps after {args.warmup} "
-                                   f"warm-up (setup {setup_s:.1f}s excluded)"},
+                         "sample": f"full 256x256 Taylor-Hood mesh, {args.steps} steps after "
+                                   f"{args.warmup} warm-up; setup {setup_s:.1f}s excluded"},
         "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "notes": "femx's generic CPU assembly and host matvec are single-threaded "
-                 "(no OpenMP on this path); the oracle restates them serially, so one "
-                 "core is what the reference implementation uses",
-    }
-    print(json.dumps(line), flush=True)
+        "notes": "femx's generic CPU assembly loop is single-threaded (no OpenMP on the "
+                 "assemble path); the oracle restates it serially, one core",
+    }), flush=True)
 
 
-def config_block():
-    from femx_gb300 import meshes
-    c = meshes.structured_counts(NX)
-    return {"workload": f"poisson_p1_kappa_{NX}x{NX}_assemble_bc_{NSPMV}spmv",
-            "elements": c["elems"], "nodes": c["nodes"], "nnz": c["nnz_p1"],
-            "kappa": "exp(GRF, ell=0.05, var=1)", "source": "8 Fourier modes",
-            "dirichlet": "all boundary nodes", "l2": "flushed (512 MB write) before each step"}
+# ------------------------------------------------------------------ GPU arm
+
+class Timer:
+    def __init__(self, torch, stream, flush):
+        self.torch, self.stream, self.flush = torch, stream, flush
+
+    def run(self, fn, steps, warmup):
+        torch = self.torch
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        for a, b in evs:
+            self.flush.zero_()
+            a.record(self.stream)
+            fn()
+            b.record(self.stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs) / steps * 1e-3
+
+
+def fp64_peak_tflops(torch, L):
+    import ctypes as C
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    blocks, threads, iters = props.multi_processor_count * 16, 256, 4096
+    out = torch.empty(blocks * threads, dtype=torch.float64, device="cuda")
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    f = L.lib().gbfem_probe_fp64_fma
+    for _ in range(2):
+        L.check(f(blocks, threads, iters, C.c_void_p(out.data_ptr()), s))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    L.check(f(blocks, threads, iters, C.c_void_p(out.data_ptr()), s))
+    e1.record()
+    torch.cuda.synchronize()
+    return 16.0 * iters * blocks * threads / (e0.elapsed_time(e1) * 1e-3) / 1e12
 
 
 def main():
@@ -203,199 +235,264 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only", default="", help="run one workload: th, th64, vjp, poisson")
+    ap.add_argument("--soak", type=float, default=1.0,
+                    help="seconds of untimed headline steps before timing (clock sampling)")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
-
     if args.impl == "reference":
         if rank == 0:
-            run_reference(args, rank)
+            run_reference(args)
         return
+    args.warmup = max(args.warmup, 3)
 
     import torch
     import torch.distributed as dist
     from femx_gb300 import _lib as L
     from femx_gb300 import assembly as A
     from femx_gb300 import build as B
-    from femx_gb300 import meshes
 
     if not os.path.exists(B.LIB):
         B.build()
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
-
-    coords, conn, kappa, f, u, bdofs, g = make_inputs()
-    n, e = coords.shape[0], conn.shape[0]
-    offs, dofs = meshes.scalar_elem_dofs(conn)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    timer = Timer(torch, stream, flush)
+    hbm, peak_kind = peaks()
+    traffic = traffic_table()
 
     def d(a, dtype=None):
         t = torch.from_numpy(np.ascontiguousarray(a))
         return (t if dtype is None else t.to(dtype)).cuda()
 
-    amap = A.makeAssemblyMap(n, n, d(offs), d(dofs), d(offs), d(dofs))
-    pat = amap.pattern()
-    bc = A.makeBoundaryMap(d(bdofs), pat)
-    coords_d, kappa_d, f_d, u_d, g_d = d(coords), d(kappa), d(f), d(u), d(g)
-    res = torch.zeros(n, dtype=torch.float64, device="cuda")
-    rhs = torch.zeros_like(res)
-    xa = torch.zeros_like(res)
-    xb = torch.zeros_like(res)
-    jac = A.CsrMatrix(pat)
-    nnz = pat.nnz
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    stream = torch.cuda.current_stream()
+    def maxrank(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
 
-    def step(ev=None):
-        if ev is not None:
-            ev[0].record(stream)
-        A.assembleP1Kappa(amap, coords_d, kappa_d, f_d, u_d, res, jac)
-        if ev is not None:
-            ev[1].record(stream)
-        A.axpby(-1.0, res, 0.0, rhs)
-        A.prepareForwardSolve(bc, jac, rhs, g_d)
-        if ev is not None:
-            ev[2].record(stream)
-        x, y = rhs, xa
-        for i in range(NSPMV):
-            A.matvec(jac, x, y, alpha=SPMV_SCALE)
-            x, y = y, (xb if y is xa else xa)
-        if ev is not None:
-            ev[3].record(stream)
-        return x
+    only = args.only
+    line = {}
+    launches = 0
 
-    launches_per_step = 1 + 1 + 1 + NSPMV  # assemble, axpby, lifting, SpMVs
+    # ---------------- headline: Taylor-Hood Newton J + R ----------------
+    if only in ("", "th", "th64"):
+        nx = 64 if only == "th64" else TH_NX
+        t = th_inputs(nx)
+        nd, e = t["nd"], t["conn6"].shape[0]
+        amap = A.makeAssemblyMap(nd, nd, d(t["offs"]), d(t["dofs"]), d(t["offs"]), d(t["dofs"]))
+        pat = amap.pattern()
+        bc = A.makeBoundaryMap(d(t["bdofs"]), pat)
+        coords, conn6, state = d(t["coords"]), d(t["conn6"]), d(t["state"])
+        bvals = d(t["bvals"])
+        res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        jac = A.CsrMatrix(pat)
 
-    for _ in range(args.warmup):
-        step()
-    amap.check()
-    torch.cuda.synchronize()
+        def th_step(prec):
+            def fn():
+                A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision=prec)
+                A.replaceRes(bc, state, bvals, res)
+                A.replaceRows(bc, jac, 1.0)
+            return fn
 
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        for s in range(args.steps):
-            flush.zero_()
-            step(evs[s])
-        torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    t_asm = sum(ev[0].elapsed_time(ev[1]) for ev in evs) / args.steps * 1e-3
-    t_bc = sum(ev[1].elapsed_time(ev[2]) for ev in evs) / args.steps * 1e-3
-    t_spmv = sum(ev[2].elapsed_time(ev[3]) for ev in evs) / args.steps * 1e-3
-    t_step = t_asm + t_bc + t_spmv
-    if world > 1:
-        tt = torch.tensor([t_step], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+        # clock soak (~1 s of the headline step) then the timed region
+        with Clocks(local) as clk:
+            t_end = time.perf_counter() + args.soak
+            while time.perf_counter() < t_end:
+                th_step("fp32_quad")()
+                torch.cuda.synchronize()
+            if world > 1:
+                dist.barrier()
+            torch.cuda.synchronize()
+            t_fast = maxrank(timer.run(th_step("fp32_quad"), args.steps, args.warmup))
+            if world > 1:
+                dist.barrier()
+            t_plain = maxrank(timer.run(th_step("fp64"), args.steps, args.warmup))
+        launches += 3 * args.steps
+        amap.check()
+        # kernel-only time of the fast assembly (no BC kernels)
+        t_kern = timer.run(lambda: A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac,
+                                                        precision="fp32_quad"),
+                           args.steps, args.warmup)
+        t_kern64 = timer.run(lambda: A.assembleTaylorHood(amap, coords, conn6, NU, state, res,
+                                                          jac, precision="fp64"),
+                             max(3, args.steps // 4), 2)
+        # accuracy of the fast path against the plain FP64 path at full size
+        A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision="fp64")
+        j64, r64 = jac.vals.clone(), res.clone()
+        A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision="fp32_quad")
+        err_j = float((jac.vals - j64).abs().max() / j64.abs().max())
+        err_r = float((res - r64).abs().max() / r64.abs().max())
 
-    # e2e: public API with pinned host buffers, copies inside the timed region
-    kappa_h = torch.from_numpy(kappa).pin_memory()
-    f_h = torch.from_numpy(f).pin_memory()
-    u_h = torch.from_numpy(u).pin_memory()
-    rhs_h = torch.empty(n, dtype=torch.float64).pin_memory()
-    x_h = torch.empty(n, dtype=torch.float64).pin_memory()
-    h2d = 8 * e + 8 * n + 8 * n
-    d2h = 8 * n + 8 * n
+        # e2e: state in from pinned host memory, residual out, inside the timing
+        state_h = torch.from_numpy(t["state"]).pin_memory()
+        res_h = torch.empty(nd, dtype=torch.float64).pin_memory()
 
-    def e2e_step():
-        kappa_d.copy_(kappa_h, non_blocking=True)
-        f_d.copy_(f_h, non_blocking=True)
-        u_d.copy_(u_h, non_blocking=True)
-        x = step()
-        rhs_h.copy_(rhs, non_blocking=True)
-        x_h.copy_(x, non_blocking=True)
+        def e2e():
+            state.copy_(state_h, non_blocking=True)
+            th_step("fp32_quad")()
+            res_h.copy_(res, non_blocking=True)
+        t_e2e = maxrank(timer.run(e2e, args.steps, args.warmup))
+        launches += 3 * args.steps
 
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_t = 0.0
-    for s in range(args.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        e2e_step()
-        e1.record(stream)
-        e1.synchronize()
-        e2e_t += e0.elapsed_time(e1) * 1e-3
-    e2e_t /= args.steps
-    if world > 1:
-        tt = torch.tensor([e2e_t], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+        nnz = pat.nnz
+        np2 = t["coords"].shape[0]
+        b_th = 8 * nnz + 16 * nd + 60 * e + 24 * e + 16 * np2
+        # FP64 work of the plain kernel per element (instruction count, FMA = 2 FLOP)
+        flop_th = 2 * 6500
+        fp64 = fp64_peak_tflops(torch, L)
+        line.update({
+            "metric": METRIC, "value": world * e / t_fast, "unit": "elements/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_fast * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 quadrature / f64 accumulation",
+            "data": "synthetic (seeded)", "config": th_config() if nx == TH_NX else
+            {"workload": f"ns_taylor_hood_p2p1_cavity_{nx}x{nx}"},
+            "e2e": {"value": world * e / t_e2e, "unit": "elements/s",
+                    "h2d_bytes_per_step": 8 * nd, "d2h_bytes_per_step": 8 * nd,
+                    "ms_per_step": t_e2e * 1e3},
+            "fp64_plain": {"value": world * e / t_plain, "unit": "elements/s",
+                           "ms_per_step": t_plain * 1e3,
+                           "speedup_of_fast_path": t_plain / t_fast},
+            "rel_err_vs_fp64": {"jacobian": err_j, "residual": err_r,
+                                "gate": 1e-6, "norm": "inf, relative"},
+            "roofline": {"bound": "hbm", "achieved": b_th / t_kern / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": b_th / t_kern / 1e9 / hbm,
+                         "traffic": traffic.get("th_fp32"), "kernel": "thKernel<float,true>",
+                         "launch_ms": t_kern * 1e3, "algorithmic_bytes": b_th,
+                         "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"},
+            "roofline_fp64_plain": {"bound": "fp64", "achieved": flop_th * e / t_kern64 / 1e12,
+                                    "peak": fp64, "unit": "TFLOP/s",
+                                    "frac": flop_th * e / t_kern64 / 1e12 / fp64,
+                                    "kernel": "thKernel<double,true>",
+                                    "launch_ms": t_kern64 * 1e3,
+                                    "peak_source": "measured by gbfem_probe_fp64_fma"},
+            "fp64_fma_peak_tflops_measured": fp64,
+            "clocks": clk.summary(),
+        })
+        del amap, bc, jac, res, j64, r64
 
-    hbm, peak_kind = peaks()
-    b_asm = 20 * e + 32 * n + 8 * nnz
-    b_spmv = 12 * nnz + 20 * n
-    t_one_spmv = t_spmv / NSPMV
-    traffic = traffic_table()
-    kern = {
-        "p1_assemble": {"bound": "hbm", "achieved": b_asm / t_asm / 1e9, "peak": hbm,
-                        "unit": "GB/s", "frac": b_asm / t_asm / 1e9 / hbm,
-                        "traffic": traffic.get("p1_assemble"), "launch_ms": t_asm * 1e3,
-                        "algorithmic_bytes": b_asm},
-        "spmv": {"bound": "hbm", "achieved": b_spmv / t_one_spmv / 1e9, "peak": hbm,
-                 "unit": "GB/s", "frac": b_spmv / t_one_spmv / 1e9 / hbm,
-                 "traffic": traffic.get("spmv"), "launch_ms": t_one_spmv * 1e3,
-                 "algorithmic_bytes": b_spmv},
-    }
-    dominant = "p1_assemble" if t_asm >= t_spmv else "spmv"
-    roof = dict(kern[dominant])
-    roof["kernel"] = dominant
-    roof["peak_source"] = f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})"
-    fp64 = fp64_peak_tflops(torch, L)
+    # ---------------- VJP (config 4) ----------------
+    if only in ("", "vjp"):
+        p = p1_inputs(VJP_NX, seed_kappa=4)
+        n, e = p["coords"].shape[0], p["conn"].shape[0]
+        amap = A.makeAssemblyMap(n, n, d(p["offs"]), d(p["dofs"]), d(p["offs"]), d(p["dofs"]))
+        coords, kappa = d(p["coords"]), d(p["kappa"])
+        rng = np.random.default_rng(4)
+        u, lam = d(rng.standard_normal(n)), d(rng.standard_normal(n))
+        g_u = torch.zeros(n, dtype=torch.float64, device="cuda")
+        g_m = torch.zeros(e, dtype=torch.float64, device="cuda")
+        res_v = {}
+        for prec in ("fp32_quad", "fp64"):
+            tt = maxrank(timer.run(lambda: A.vjpP1Kappa(amap, coords, kappa, u, lam, g_u, g_m,
+                                                         precision=prec), args.steps,
+                                   args.warmup))
+            res_v[prec] = (tt, g_u.clone(), g_m.clone())
+        launches += 2 * args.steps
+        t64, gu64, gm64 = res_v["fp64"]
+        t32, gu32, gm32 = res_v["fp32_quad"]
+        b_vjp = 28 * e + 40 * n
+        line["vjp"] = {
+            "workload": f"poisson_p1_{VJP_NX}x{VJP_NX}_vjp_state_and_control",
+            "grads_per_s": world / t32, "grads_per_s_fp64": world / t64,
+            "ms_per_grad": t32 * 1e3, "ms_per_grad_fp64": t64 * 1e3,
+            "elements": e,
+            "rel_err_fp32_vs_fp64": {
+                "g_u": float((gu32 - gu64).abs().max() / gu64.abs().max()),
+                "g_m": float((gm32 - gm64).abs().max() / gm64.abs().max())},
+            "roofline": {"bound": "hbm", "achieved": b_vjp / t32 / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": b_vjp / t32 / 1e9 / hbm,
+                         "algorithmic_bytes": b_vjp},
+        }
+        del amap
 
-    line = {
-        "metric": METRIC, "value": world * e / t_step, "unit": "elements/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded)", "config": config_block(),
-        "e2e": {"value": world * e / e2e_t, "unit": "elements/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_t * 1e3},
-        "roofline": roof,
-        "kernels": kern,
-        "phases_ms": {"assemble": t_asm * 1e3, "rhs_and_lifting": t_bc * 1e3,
-                      "spmv_x10": t_spmv * 1e3},
-        "nnz_per_s": world * nnz / t_asm,
-        "fp64_fma_peak_tflops_measured": fp64,
-        "gpu_launches": launches_per_step * args.steps,
-        "clocks": clk.summary(),
-        "scaling_mode": "replicas" if world > 1 else "single",
-    }
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(coords, conn, kappa, f, u, bdofs, g)
+    # ---------------- Poisson forward + SpMV (config 2) ----------------
+    if only in ("", "poisson"):
+        p = p1_inputs(POISSON_NX)
+        n, e = p["coords"].shape[0], p["conn"].shape[0]
+        amap = A.makeAssemblyMap(n, n, d(p["offs"]), d(p["dofs"]), d(p["offs"]), d(p["dofs"]))
+        pat = amap.pattern()
+        bc = A.makeBoundaryMap(d(p["bdofs"]), pat)
+        coords, kappa, f = d(p["coords"]), d(p["kappa"]), d(p["f"])
+        u = torch.zeros(n, dtype=torch.float64, device="cuda")
+        g = torch.zeros(len(p["bdofs"]), dtype=torch.float64, device="cuda")
+        res = torch.zeros(n, dtype=torch.float64, device="cuda")
+        rhs, xa, xb = torch.zeros_like(res), torch.zeros_like(res), torch.zeros_like(res)
+        jac = A.CsrMatrix(pat)
+
+        def asm():
+            A.assembleP1Kappa(amap, coords, kappa, f, u, res, jac)
+
+        def bcs():
+            A.axpby(-1.0, res, 0.0, rhs)
+            A.prepareForwardSolve(bc, jac, rhs, g)
+
+        def spmvs():
+            x, y = rhs, xa
+            for _ in range(NSPMV):
+                A.matvec(jac, x, y, alpha=SPMV_SCALE)
+                x, y = y, (xb if y is xa else xa)
+
+        def full():
+            asm()
+            bcs()
+            spmvs()
+
+        t_full = maxrank(timer.run(full, args.steps, args.warmup))
+        t_asm = timer.run(asm, args.steps, args.warmup)
+        asm()
+        bcs()
+        t_spmv = timer.run(spmvs, args.steps, args.warmup) / NSPMV
+        launches += (3 + NSPMV) * args.steps
+        nnz = pat.nnz
+        b_asm = 20 * e + 32 * n + 8 * nnz
+        b_spmv = 12 * nnz + 20 * n
+        line["poisson"] = {
+            "workload": f"poisson_p1_kappa_{POISSON_NX}x{POISSON_NX}_assemble_bc_{NSPMV}spmv",
+            "elements_per_s": world * e / t_full, "ms_per_step": t_full * 1e3,
+            "nnz_per_s_assembly": nnz / t_asm,
+            "assembly": {"bound": "hbm", "achieved": b_asm / t_asm / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": b_asm / t_asm / 1e9 / hbm,
+                         "launch_ms": t_asm * 1e3, "traffic": traffic.get("p1_assemble")},
+            "spmv": {"bound": "hbm", "achieved": b_spmv / t_spmv / 1e9, "peak": hbm,
+                     "unit": "GB/s", "frac": b_spmv / t_spmv / 1e9 / hbm,
+                     "launch_ms": t_spmv * 1e3, "traffic": traffic.get("spmv")},
+        }
+        del amap, bc, jac
+
+    line["gpu_launches"] = launches
+    line["scaling_mode"] = "replicas" if world > 1 else "single"
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and only in ("", "th"):
+        line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
 
-def cpu_baseline(coords, conn, kappa, f, u, bdofs, g):
-    """Oracle port on one host core, bounded sample of the same workload."""
+def cpu_baseline():
+    """Oracle port on one host core: bounded sample of the headline workload."""
     from oracle import pyoracle as orc
-    from femx_gb300 import meshes
-    n, e = coords.shape[0], conn.shape[0]
-    offs, dofs = meshes.scalar_elem_dofs(conn)
-    om = orc.AssemblyMap(n, n, offs, dofs, offs, dofs)
-    q = orc.P1Quad(coords, conn)
-    ob = orc.BoundaryMap(bdofs, om.row_ptr, om.col_ind)
-    steps, t_total = 0, 0.0
-    while t_total < 10.0 and steps < 20:
+    t = th_inputs(TH_NX)
+    nd = t["nd"]
+    om = orc.AssemblyMap(nd, nd, t["offs"], t["dofs"], t["offs"], t["dofs"])
+    th = orc.THQuad(t["coords"], t["conn6"])
+    res, vals = np.zeros(nd), np.zeros(om.nnz)
+    e = t["conn6"].shape[0]
+    steps, total = 0, 0.0
+    while total < 8.0 and steps < 10:
         t0 = time.perf_counter()
-        res, vals = orc.assemble_p1_kappa(om, q, kappa, f, u)
-        vals, rhs = ob.prepare_forward_solve(vals, -res, g)
-        x = rhs
-        for _ in range(NSPMV):
-            x = orc.matvec(om.row_ptr, om.col_ind, vals, x, alpha=SPMV_SCALE)
-        t_total += time.perf_counter() - t0
+        orc.assemble_th_range(om, th, NU, t["state"], 0, -1, res, vals)
+        total += time.perf_counter() - t0
         steps += 1
-    return {"value": e * steps / t_total, "unit": "elements/s", "cores": 1, "kind": "port",
-            "sample": f"{steps} full steps of the same 1024x1024 workload (serial oracle)"}
+    return {"value": e * steps / total, "unit": "elements/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} full assemblies of the 256x256 Taylor-Hood mesh (serial oracle)"}
 
 
 if __name__ == "__main__":

@@ -28,6 +28,16 @@ struct gbfem_assembly_map
   int* row_ptr       = nullptr;
   int* col_ind       = nullptr;
 
+  // Compact Jacobian scatter map for uniform layouts: for element e and
+  // local row i, the CSR slot of local column j is
+  //   row_ptr[res_dof(e, i)] + jac_pos[(e * uniform_res + i) * pos_stride + j]
+  // (one byte per entry, rows padded to pos_stride bytes so kernels load a
+  // whole row of positions with one vector load). Null when the layout is
+  // not uniform or a row has more than 256 entries; kernels then fall back
+  // to jac_map.
+  unsigned char* jac_pos    = nullptr;
+  int            pos_stride = 0;
+
   // Status word written by hot-path kernels that meet invalid data
   // (degenerate elements); read by gbfem_assembly_map_check().
   gbfem::DeviceStatus* status = nullptr;

@@ -31,6 +31,8 @@ struct P1Args
   const double*        f;      // nodal source or nullptr
   const double*        u;      // state
   const int*           jac_map;
+  const int*           row_ptr;
+  const unsigned*      jac_pos; // [ne][3] words: in-row positions, or null
   double*              res;
   double*              vals;
   DeviceStatus*        status;
@@ -118,14 +120,32 @@ __global__ void __launch_bounds__(256) p1AssembleKernel(P1Args a)
   gbfem::redAdd(a.res + d2, r2);
   if (kJac)
   {
-    const int* jm = a.jac_map + 9 * e;
     const double v[9] = {double(K.k00), double(K.k01), double(K.k02),
                          double(K.k01), double(K.k11), double(K.k12),
                          double(K.k02), double(K.k12), double(K.k22)};
-#pragma unroll
-    for (int i = 0; i < 9; ++i)
+    if (a.jac_pos != nullptr)
     {
-      gbfem::redAdd(a.vals + jm[i], v[i]);
+      const int d[3] = {d0, d1, d2};
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+      {
+        const int      rs = a.row_ptr[d[i]];
+        const unsigned w  = a.jac_pos[3 * e + i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+        {
+          gbfem::redAdd(a.vals + rs + int((w >> (8 * j)) & 0xffu), v[3 * i + j]);
+        }
+      }
+    }
+    else
+    {
+      const int* jm = a.jac_map + 9 * e;
+#pragma unroll
+      for (int i = 0; i < 9; ++i)
+      {
+        gbfem::redAdd(a.vals + jm[i], v[i]);
+      }
     }
   }
 }
@@ -227,6 +247,9 @@ P1Args makeArgs(const gbfem_assembly_map* map, int num_nodes,
   a.kappa   = kappa;
   a.u       = u;
   a.jac_map = map->jac_map;
+  a.row_ptr = map->row_ptr;
+  a.jac_pos = map->pos_stride == 4 ? reinterpret_cast<const unsigned*>(map->jac_pos)
+                                   : nullptr;
   a.status  = map->status;
   return a;
 }

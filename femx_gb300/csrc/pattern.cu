@@ -219,6 +219,44 @@ __global__ void rankColumns(int num_res, const int* __restrict__ cand_off,
   }
 }
 
+// Largest in-row position of every local entry (decides the compact map).
+__global__ void maxInRowPos(int ne, int nr, int nc, const int* __restrict__ rd,
+                            const int* __restrict__ row_ptr,
+                            const int* __restrict__ jac_map, int* __restrict__ mx)
+{
+  const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<long long>(ne) * nr)
+  {
+    return;
+  }
+  const int rs = row_ptr[rd[t]];
+  int       m  = 0;
+  for (int j = 0; j < nc; ++j)
+  {
+    m = max(m, jac_map[t * nc + j] - rs);
+  }
+  atomicMax(mx, m);
+}
+
+__global__ void fillInRowPos(int ne, int nr, int nc, int stride,
+                             const int* __restrict__ rd,
+                             const int* __restrict__ row_ptr,
+                             const int* __restrict__ jac_map,
+                             unsigned char* __restrict__ pos)
+{
+  const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<long long>(ne) * nr)
+  {
+    return;
+  }
+  const int rs = row_ptr[rd[t]];
+  for (int j = 0; j < stride; ++j)
+  {
+    pos[t * stride + j] =
+        j < nc ? static_cast<unsigned char>(jac_map[t * nc + j] - rs) : 0;
+  }
+}
+
 __global__ void compareTables(long long n, const int* __restrict__ a,
                               const int* __restrict__ b, int* __restrict__ diff)
 {
@@ -263,6 +301,7 @@ gbfem_assembly_map::~gbfem_assembly_map()
     gbfem::deviceFree(p);
   }
   gbfem::deviceFree(status);
+  gbfem::deviceFree(jac_pos);
 }
 
 namespace gbfem
@@ -436,6 +475,31 @@ extern "C" int gbfem_assembly_map_create(int num_res, int num_states,
         cudaCheck(cudaStreamSynchronize(s), "AssemblyMap compare");
         deviceFree(diff);
         m->same_dofs = diff_h == 0;
+      }
+      // Compact in-row position map (uniform layouts, rows up to 256 wide).
+      if (num_elems > 0 && m->uniform_res > 0 && m->uniform_state > 0)
+      {
+        const long long rows_tot = static_cast<long long>(num_elems) * m->uniform_res;
+        int*            mx       = deviceAlloc<int>(1);
+        cudaCheck(cudaMemsetAsync(mx, 0, sizeof(int), s), "memset");
+        maxInRowPos<<<blocksFor(rows_tot, 256), 256, 0, s>>>(
+            num_elems, m->uniform_res, m->uniform_state, m->res_dofs, m->row_ptr,
+            m->jac_map, mx);
+        int mx_h = 0;
+        cudaCheck(cudaMemcpyAsync(&mx_h, mx, sizeof(int), cudaMemcpyDeviceToHost, s),
+                  "AssemblyMap position readback");
+        cudaCheck(cudaStreamSynchronize(s), "AssemblyMap position scan");
+        deviceFree(mx);
+        if (mx_h < 256)
+        {
+          const int stride = m->uniform_state <= 4 ? 4 : ((m->uniform_state + 15) / 16) * 16;
+          m->pos_stride    = stride;
+          m->jac_pos       = deviceAlloc<unsigned char>(rows_tot * stride);
+          fillInRowPos<<<blocksFor(rows_tot, 256), 256, 0, s>>>(
+              num_elems, m->uniform_res, m->uniform_state, stride, m->res_dofs,
+              m->row_ptr, m->jac_map, m->jac_pos);
+          cudaCheck(cudaGetLastError(), "AssemblyMap position launch");
+        }
       }
       cudaCheck(cudaStreamSynchronize(s), "AssemblyMap build");
     }

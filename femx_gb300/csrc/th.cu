@@ -4,14 +4,25 @@
 // MixedFESpace order (MixedFESpace.cpp:57-84), and uses the published
 // 6-point degree-4 triangle rule (Dunavant).
 //
-// Layout: a 16-lane group owns one element, lane l computes local row l
-// (lane 15 helps with the shared stages). Per element, shared memory holds
-// the gathered state, the physical shape gradients at the six quadrature
-// points and the quadrature-point state (u, grad u, p), computed once per
-// element — unlike the reference's row operators, which recompute the
-// quadrature-point state for every row (femx/model/ns/Components.hpp:
-// 492-495). Each row's 15 Jacobian entries and residual are then scatter-
-// added with FP64 reductions at L2.
+// On GB300 the FP64 pipe (~1 TFLOP/s measured) bounds the plain path, so the
+// element is factorised to spend as few FP64 operations as possible while
+// giving exactly the quadrature sums of the row operator (up to rounding):
+//   diffusion  D_ab = sum_kl Gh_kl S^kl_ab,  Gh = nu|det| J^-1 J^-T and
+//              S^kl_ab = sum_q w_q dN^_a,k dN^_b,l (reference constants);
+//   reaction   M^ce_ab = |det| sum_v G_v[c][e] T^v_ab: grad u of a P2 field
+//              is linear, so its quadrature values are the vertex values G_v
+//              interpolated, T^v_ab = sum_q w_q N^_a N^_b lambda_v(q);
+//   pressure   B_(a,c),b = -|det| sum_k Jinv[k][c] C^k_ab,
+//              C^k_ab = sum_q w_q psi^_b dN^_a,k;
+//   convection A_ab = |det| sum_q w_q N^_a (dN^_b . ut_q), ut_q = J^-T-free
+//              transform Jinv u_q, the only term kept at quadrature points.
+// The residual follows from the same blocks: R_(a,c) = sum_b (D+A)_ab
+// u_(b,c) + sum_b B_(a,c),b p_b, R_p(b) = sum_(a,e) B_(a,e),b u_(a,e).
+//
+// Layout: a 16-lane group owns one element; shared stages compute the
+// geometry, the quadrature-point transforms and the vertex gradients once;
+// then lane l produces local row l (15 entries + residual), and scatter-adds
+// them with FP64 reductions at L2 through the compact in-row position map.
 #include <type_traits>
 
 #include "maps.cuh"
@@ -20,244 +31,332 @@ namespace
 {
 using gbfem::DeviceStatus;
 
-constexpr int kLanes          = 16;
-constexpr int kElemsPerBlock  = 8;
-constexpr int kThreads        = kLanes * kElemsPerBlock;
-constexpr int kNq             = 6;
+constexpr int kLanes         = 16;
+constexpr int kElemsPerBlock = 8;
+constexpr int kThreads       = kLanes * kElemsPerBlock;
+constexpr int kNq            = 6;
 
-struct ThTables
+template <class R>
+struct ThRef
 {
-  double N[kNq][6];      // P2 values
-  double P[kNq][3];      // P1 values
-  double dNr[kNq][6][2]; // P2 reference gradients
-  double w[kNq];         // weights (reference area 1/2)
+  R N[kNq][6];       // P2 values at the quadrature points
+  R wN[kNq][6];      // w_q N^_a(q)
+  R dNr[kNq][6][2];  // P2 reference gradients at the quadrature points
+  R S00[6][6], S11[6][6], S01[6][6]; // S^00, S^11, S^01 + S^10
+  R T[3][6][6];      // sum_q w N^_a N^_b lambda_v
+  R C[2][6][3];      // sum_q w psi^_b dN^_a,k
+  R dNv[3][6][2];    // P2 reference gradients at the vertices
+  R w[kNq];
 };
 
-struct ThTablesF
+constexpr void p2Eval(double r, double s, double* N, double* dN)
 {
-  float N[kNq][6];
-  float P[kNq][3];
-  float dNr[kNq][6][2];
-  float w[kNq];
-};
-
-constexpr ThTables makeTables()
-{
-  ThTables   t{};
-  const double a1 = 0.445948490915964886, w1 = 0.223381589678011466 * 0.5;
-  const double a2 = 0.091576213509770743, w2 = 0.109951743655321868 * 0.5;
-  const double q[kNq][3] = {{a1, a1, w1}, {1.0 - 2.0 * a1, a1, w1},
-                            {a1, 1.0 - 2.0 * a1, w1}, {a2, a2, w2},
-                            {1.0 - 2.0 * a2, a2, w2}, {a2, 1.0 - 2.0 * a2, w2}};
-  for (int i = 0; i < kNq; ++i)
+  const double l0 = 1.0 - r - s, l1 = r, l2 = s;
+  const double g0[2] = {-1.0, -1.0}, g1[2] = {1.0, 0.0}, g2[2] = {0.0, 1.0};
+  N[0] = l0 * (2.0 * l0 - 1.0);
+  N[1] = l1 * (2.0 * l1 - 1.0);
+  N[2] = l2 * (2.0 * l2 - 1.0);
+  N[3] = 4.0 * l0 * l1;
+  N[4] = 4.0 * l1 * l2;
+  N[5] = 4.0 * l2 * l0;
+  for (int d = 0; d < 2; ++d)
   {
-    const double r = q[i][0], s = q[i][1];
-    const double l0 = 1.0 - r - s, l1 = r, l2 = s;
-    const double g0[2] = {-1.0, -1.0}, g1[2] = {1.0, 0.0}, g2[2] = {0.0, 1.0};
-    t.N[i][0] = l0 * (2.0 * l0 - 1.0);
-    t.N[i][1] = l1 * (2.0 * l1 - 1.0);
-    t.N[i][2] = l2 * (2.0 * l2 - 1.0);
-    t.N[i][3] = 4.0 * l0 * l1;
-    t.N[i][4] = 4.0 * l1 * l2;
-    t.N[i][5] = 4.0 * l2 * l0;
-    for (int d = 0; d < 2; ++d)
-    {
-      t.dNr[i][0][d] = (4.0 * l0 - 1.0) * g0[d];
-      t.dNr[i][1][d] = (4.0 * l1 - 1.0) * g1[d];
-      t.dNr[i][2][d] = (4.0 * l2 - 1.0) * g2[d];
-      t.dNr[i][3][d] = 4.0 * (l1 * g0[d] + l0 * g1[d]);
-      t.dNr[i][4][d] = 4.0 * (l2 * g1[d] + l1 * g2[d]);
-      t.dNr[i][5][d] = 4.0 * (l0 * g2[d] + l2 * g0[d]);
-    }
-    t.P[i][0] = l0;
-    t.P[i][1] = l1;
-    t.P[i][2] = l2;
-    t.w[i]    = q[i][2];
+    dN[0 * 2 + d] = (4.0 * l0 - 1.0) * g0[d];
+    dN[1 * 2 + d] = (4.0 * l1 - 1.0) * g1[d];
+    dN[2 * 2 + d] = (4.0 * l2 - 1.0) * g2[d];
+    dN[3 * 2 + d] = 4.0 * (l1 * g0[d] + l0 * g1[d]);
+    dN[4 * 2 + d] = 4.0 * (l2 * g1[d] + l1 * g2[d]);
+    dN[5 * 2 + d] = 4.0 * (l0 * g2[d] + l2 * g0[d]);
   }
-  return t;
 }
 
-constexpr ThTablesF makeTablesF()
+constexpr ThRef<double> makeRef()
 {
-  const ThTables d = makeTables();
-  ThTablesF      f{};
+  ThRef<double> t{};
+  const double  a1 = 0.445948490915964886, w1 = 0.223381589678011466 * 0.5;
+  const double  a2 = 0.091576213509770743, w2 = 0.109951743655321868 * 0.5;
+  const double  q[kNq][3] = {{a1, a1, w1}, {1.0 - 2.0 * a1, a1, w1},
+                            {a1, 1.0 - 2.0 * a1, w1}, {a2, a2, w2},
+                            {1.0 - 2.0 * a2, a2, w2}, {a2, 1.0 - 2.0 * a2, w2}};
+  const double  dP[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+  double        lam[kNq][3]{};
   for (int i = 0; i < kNq; ++i)
   {
+    double N[6]{}, dN[12]{};
+    p2Eval(q[i][0], q[i][1], N, dN);
+    lam[i][0] = 1.0 - q[i][0] - q[i][1];
+    lam[i][1] = q[i][0];
+    lam[i][2] = q[i][1];
+    t.w[i]    = q[i][2];
     for (int a = 0; a < 6; ++a)
     {
-      f.N[i][a]      = static_cast<float>(d.N[i][a]);
-      f.dNr[i][a][0] = static_cast<float>(d.dNr[i][a][0]);
-      f.dNr[i][a][1] = static_cast<float>(d.dNr[i][a][1]);
+      t.N[i][a]      = N[a];
+      t.wN[i][a]     = q[i][2] * N[a];
+      t.dNr[i][a][0] = dN[2 * a];
+      t.dNr[i][a][1] = dN[2 * a + 1];
+    }
+  }
+  for (int a = 0; a < 6; ++a)
+  {
+    for (int b = 0; b < 6; ++b)
+    {
+      double s00 = 0.0, s11 = 0.0, s01 = 0.0;
+      double tv[3] = {0.0, 0.0, 0.0};
+      for (int i = 0; i < kNq; ++i)
+      {
+        const double w = t.w[i];
+        s00 += w * t.dNr[i][a][0] * t.dNr[i][b][0];
+        s11 += w * t.dNr[i][a][1] * t.dNr[i][b][1];
+        s01 += w * (t.dNr[i][a][0] * t.dNr[i][b][1] + t.dNr[i][a][1] * t.dNr[i][b][0]);
+        for (int v = 0; v < 3; ++v)
+        {
+          tv[v] += w * t.N[i][a] * t.N[i][b] * lam[i][v];
+        }
+      }
+      t.S00[a][b] = s00;
+      t.S11[a][b] = s11;
+      t.S01[a][b] = s01;
+      for (int v = 0; v < 3; ++v)
+      {
+        t.T[v][a][b] = tv[v];
+      }
     }
     for (int b = 0; b < 3; ++b)
     {
-      f.P[i][b] = static_cast<float>(d.P[i][b]);
+      for (int k = 0; k < 2; ++k)
+      {
+        double c = 0.0;
+        for (int i = 0; i < kNq; ++i)
+        {
+          c += t.w[i] * lam[i][b] * t.dNr[i][a][k];
+        }
+        t.C[k][a][b] = c;
+      }
     }
-    f.w[i] = static_cast<float>(d.w[i]);
   }
-  return f;
+  const double vx[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+  for (int v = 0; v < 3; ++v)
+  {
+    double N[6]{}, dN[12]{};
+    p2Eval(vx[v][0], vx[v][1], N, dN);
+    for (int s = 0; s < 6; ++s)
+    {
+      t.dNv[v][s][0] = dN[2 * s];
+      t.dNv[v][s][1] = dN[2 * s + 1];
+    }
+  }
+  (void)dP;
+  return t;
 }
 
-__constant__ ThTables  kTab  = makeTables();
-__constant__ ThTablesF kTabF = makeTablesF();
-
-__device__ __forceinline__ const ThTables& tables(double)
+template <class R>
+constexpr ThRef<R> castRef()
 {
-  return kTab;
+  const ThRef<double> d = makeRef();
+  ThRef<R>            r{};
+  for (int q = 0; q < kNq; ++q)
+  {
+    r.w[q] = static_cast<R>(d.w[q]);
+    for (int a = 0; a < 6; ++a)
+    {
+      r.N[q][a]      = static_cast<R>(d.N[q][a]);
+      r.wN[q][a]     = static_cast<R>(d.wN[q][a]);
+      r.dNr[q][a][0] = static_cast<R>(d.dNr[q][a][0]);
+      r.dNr[q][a][1] = static_cast<R>(d.dNr[q][a][1]);
+    }
+  }
+  for (int a = 0; a < 6; ++a)
+  {
+    for (int b = 0; b < 6; ++b)
+    {
+      r.S00[a][b] = static_cast<R>(d.S00[a][b]);
+      r.S11[a][b] = static_cast<R>(d.S11[a][b]);
+      r.S01[a][b] = static_cast<R>(d.S01[a][b]);
+      for (int v = 0; v < 3; ++v)
+      {
+        r.T[v][a][b] = static_cast<R>(d.T[v][a][b]);
+      }
+    }
+    for (int b = 0; b < 3; ++b)
+    {
+      r.C[0][a][b] = static_cast<R>(d.C[0][a][b]);
+      r.C[1][a][b] = static_cast<R>(d.C[1][a][b]);
+    }
+  }
+  for (int v = 0; v < 3; ++v)
+  {
+    for (int s2 = 0; s2 < 6; ++s2)
+    {
+      r.dNv[v][s2][0] = static_cast<R>(d.dNv[v][s2][0]);
+      r.dNv[v][s2][1] = static_cast<R>(d.dNv[v][s2][1]);
+    }
+  }
+  return r;
 }
-__device__ __forceinline__ const ThTablesF& tables(float)
+
+__device__ const ThRef<double> kRefD = makeRef();
+__device__ const ThRef<float>  kRefF = castRef<float>();
+
+__device__ __forceinline__ const ThRef<double>* refTables(double)
 {
-  return kTabF;
+  return &kRefD;
+}
+__device__ __forceinline__ const ThRef<float>* refTables(float)
+{
+  return &kRefF;
 }
 
 struct ThArgs
 {
-  int            ne;
-  int            num_nodes;
-  const int*     dofs;  // [ne][15]
-  const int*     conn6; // [ne][6]
-  const double2* coords;
-  double         nu;
-  const double*  state;
-  const int*     jac_map;
-  double*        res;
-  double*        vals;
-  DeviceStatus*  status;
+  int                  ne;
+  int                  num_nodes;
+  const int*           dofs;  // [ne][15]
+  const int*           conn6; // [ne][6]
+  const double2*       coords;
+  double               nu;
+  const double*        state;
+  const int*           row_ptr;
+  const unsigned char* jac_pos; // [ne][15][16] or null
+  const int*           jac_map; // fallback
+  double*              res;
+  double*              vals;
+  DeviceStatus*        status;
 };
 
 template <class T>
 struct ElemShared
 {
   T   st[16];
+  T   aInvJ[4];  // |det| * J^-1
   T   invJ[4];
-  T   W[kNq];
-  T   dN[kNq][6][2];
-  T   u[kNq][2];
-  T   G[kNq][4];
-  T   p[kNq];
+  T   G3[3];     // nu |det| (J^-1 J^-T): 00, 11, 01
+  T   ut[kNq][2];
+  T   vq[kNq][6]; // |det| dN^_b(q) . ut_q
+  T   Gv[3][4];   // |det| grad u at the vertices, [v][c*2+e]
   int ok;
 };
 
 template <class T, bool kJac>
 __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
 {
+  __shared__ ThRef<T>      ref;
   __shared__ ElemShared<T> sh[kElemsPerBlock];
-  const int  l   = threadIdx.x & (kLanes - 1);
-  const int  le  = threadIdx.x / kLanes;
-  const int  e   = blockIdx.x * kElemsPerBlock + le;
-  const bool has = e < a.ne;
+  {
+    const T* src = reinterpret_cast<const T*>(refTables(T()));
+    T*       dst = reinterpret_cast<T*>(&ref);
+    for (int i = threadIdx.x; i < int(sizeof(ThRef<T>) / sizeof(T)); i += kThreads)
+    {
+      dst[i] = src[i];
+    }
+  }
+  const int      l   = threadIdx.x & (kLanes - 1);
+  const int      le  = threadIdx.x / kLanes;
+  const int      e   = blockIdx.x * kElemsPerBlock + le;
+  const bool     has = e < a.ne;
   ElemShared<T>& S   = sh[le];
-  const auto&    tab = tables(T());
 
   if (has && l < 15)
   {
     S.st[l] = T(a.state[a.dofs[15 * e + l]]);
   }
-  bool nodes_ok = true;
   if (has && l == 15)
   {
+    bool nodes_ok = true;
     for (int k = 0; k < 6; ++k)
     {
       nodes_ok = nodes_ok
                  && static_cast<unsigned>(a.conn6[6 * e + k])
                         < static_cast<unsigned>(a.num_nodes);
     }
+    S.ok = 0;
     if (!nodes_ok)
     {
       gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
     }
-  }
-  if (has && l == 15 && !nodes_ok)
-  {
-    S.ok = 0;
-  }
-  else if (has && l == 15)
-  {
-    const double2 x0 = a.coords[a.conn6[6 * e + 0]];
-    const double2 x1 = a.coords[a.conn6[6 * e + 1]];
-    const double2 x2 = a.coords[a.conn6[6 * e + 2]];
-    // J[a][b] = d x_a / d r_b from the vertices (affine element)
-    const double j00 = x1.x - x0.x, j01 = x2.x - x0.x;
-    const double j10 = x1.y - x0.y, j11 = x2.y - x0.y;
-    const double det = j00 * j11 - j01 * j10;
-    const double ad  = fabs(det);
-    S.ok             = ad >= 1.0e-30 ? 1 : 0;
-    if (S.ok)
-    {
-      const double inv = 1.0 / det;
-      S.invJ[0]        = T(j11 * inv);
-      S.invJ[1]        = T(-j01 * inv);
-      S.invJ[2]        = T(-j10 * inv);
-      S.invJ[3]        = T(j00 * inv);
-      for (int q = 0; q < kNq; ++q)
-      {
-        S.W[q] = T(ad * tab.w[q]);
-      }
-    }
     else
     {
-      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+      const double2 x0 = a.coords[a.conn6[6 * e + 0]];
+      const double2 x1 = a.coords[a.conn6[6 * e + 1]];
+      const double2 x2 = a.coords[a.conn6[6 * e + 2]];
+      // J[a][b] = d x_a / d r_b of the affine map (vertex nodes)
+      const double j00 = x1.x - x0.x, j01 = x2.x - x0.x;
+      const double j10 = x1.y - x0.y, j11 = x2.y - x0.y;
+      const double det = j00 * j11 - j01 * j10;
+      const double ad  = fabs(det);
+      if (ad >= 1.0e-30)
+      {
+        S.ok             = 1;
+        const double inv = 1.0 / det;
+        const double i00 = j11 * inv, i01 = -j01 * inv;
+        const double i10 = -j10 * inv, i11 = j00 * inv;
+        S.invJ[0]        = T(i00);
+        S.invJ[1]        = T(i01);
+        S.invJ[2]        = T(i10);
+        S.invJ[3]        = T(i11);
+        S.aInvJ[0]       = T(ad * i00);
+        S.aInvJ[1]       = T(ad * i01);
+        S.aInvJ[2]       = T(ad * i10);
+        S.aInvJ[3]       = T(ad * i11);
+        const double nad = a.nu * ad;
+        S.G3[0]          = T(nad * (i00 * i00 + i01 * i01));
+        S.G3[1]          = T(nad * (i10 * i10 + i11 * i11));
+        S.G3[2]          = T(nad * (i00 * i10 + i01 * i11));
+      }
+      else
+      {
+        gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+      }
     }
   }
   __syncthreads();
   const bool live = has && S.ok;
-  if (live)
+  if (live && l < 12)
   {
-    // physical gradients dN[q][i][d] = sum_b dNr[q][i][b] invJ[b][d]
-    for (int i = l; i < kNq * 12; i += kLanes)
+    // |det| grad u at vertex v: [c][e] = sum_k aInvJ[k][e] sum_s u_(s,c) dNv
+    const int v = l >> 2, c = (l >> 1) & 1, ee = l & 1;
+    T         g0 = 0, g1 = 0;
+#pragma unroll
+    for (int s2 = 0; s2 < 6; ++s2)
     {
-      const int q = i / 12, s = (i % 12) / 2, d = i % 2;
-      S.dN[q][s][d] = T(tab.dNr[q][s][0]) * S.invJ[0 * 2 + d]
-                      + T(tab.dNr[q][s][1]) * S.invJ[1 * 2 + d];
+      const T us = S.st[2 * s2 + c];
+      g0 += us * ref.dNv[v][s2][0];
+      g1 += us * ref.dNv[v][s2][1];
     }
+    S.Gv[v][c * 2 + ee] = g0 * S.aInvJ[0 * 2 + ee] + g1 * S.aInvJ[1 * 2 + ee];
   }
-  __syncthreads();
   if (live && l < kNq)
   {
     const int q  = l;
-    T         u0 = 0, u1 = 0, g00 = 0, g01 = 0, g10 = 0, g11 = 0, p = 0;
+    T         u0 = 0, u1 = 0;
 #pragma unroll
-    for (int s = 0; s < 6; ++s)
+    for (int s2 = 0; s2 < 6; ++s2)
     {
-      const T v0 = S.st[2 * s], v1 = S.st[2 * s + 1];
-      const T n  = T(tab.N[q][s]);
-      u0 += n * v0;
-      u1 += n * v1;
-      g00 += v0 * S.dN[q][s][0];
-      g01 += v0 * S.dN[q][s][1];
-      g10 += v1 * S.dN[q][s][0];
-      g11 += v1 * S.dN[q][s][1];
+      u0 += ref.N[q][s2] * S.st[2 * s2];
+      u1 += ref.N[q][s2] * S.st[2 * s2 + 1];
     }
-#pragma unroll
-    for (int b = 0; b < 3; ++b)
+    // ut_k = sum_d Jinv[k][d] u_d, so that u . dN_b = dN^_b . ut
+    S.ut[q][0] = S.aInvJ[0] * u0 + S.aInvJ[1] * u1;
+    S.ut[q][1] = S.aInvJ[2] * u0 + S.aInvJ[3] * u1;
+  }
+  __syncthreads();
+  if (live)
+  {
+    for (int i = l; i < kNq * 6; i += kLanes)
     {
-      p += T(tab.P[q][b]) * S.st[12 + b];
+      const int q = i / 6, b = i % 6;
+      S.vq[q][b]  = ref.dNr[q][b][0] * S.ut[q][0] + ref.dNr[q][b][1] * S.ut[q][1];
     }
-    S.u[q][0] = u0;
-    S.u[q][1] = u1;
-    S.G[q][0] = g00;
-    S.G[q][1] = g01;
-    S.G[q][2] = g10;
-    S.G[q][3] = g11;
-    S.p[q]    = p;
   }
   __syncthreads();
   if (!live || l >= 15)
   {
     return;
   }
-  const T nu = T(a.nu);
-  // Velocity row (sa, c): jcc[sb] -> column (sb, c), jco[sb] -> (sb, 1-c),
-  // jp[b] -> pressure column b. Pressure row b: jcc[sb] -> (sb, 0),
-  // jco[sb] -> (sb, 1). Compile-time indices keep everything in registers.
-  T jcc[6], jco[6], jp[3];
-#pragma unroll
-  for (int j = 0; j < 6; ++j)
-  {
-    jcc[j] = 0;
-    jco[j] = 0;
-  }
-  jp[0] = jp[1] = jp[2] = 0;
+
+  // Row l: velocity (sa, c) for l < 12, pressure b = l - 12 otherwise.
+  // jcc[b] -> column (b, c), jco[b] -> (b, 1-c), jp[b] -> pressure b;
+  // for pressure rows jcc/jco hold the columns (b, 0) and (b, 1).
+  T   jcc[6], jco[6], jp[3] = {0, 0, 0};
   T   r = 0;
   int c = 0;
   if (l < 12)
@@ -265,72 +364,97 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
     const int sa = l >> 1;
     c            = l & 1;
     const int oc = c ^ 1;
-    for (int q = 0; q < kNq; ++q)
+    const T   Gcc[3] = {S.Gv[0][c * 2 + c], S.Gv[1][c * 2 + c], S.Gv[2][c * 2 + c]};
+    const T   Gco[3] = {S.Gv[0][c * 2 + oc], S.Gv[1][c * 2 + oc], S.Gv[2][c * 2 + oc]};
+#pragma unroll
+    for (int b = 0; b < 6; ++b)
     {
-      const T W   = S.W[q];
-      const T Na  = T(tab.N[q][sa]);
-      const T dx  = S.dN[q][sa][0], dy = S.dN[q][sa][1];
-      const T ux  = S.u[q][0], uy = S.u[q][1];
-      const T gcx = S.G[q][2 * c], gcy = S.G[q][2 * c + 1];
-      const T gcc = S.G[q][2 * c + c], gco = S.G[q][2 * c + oc];
-      const T WNa = W * Na;
-      const T dc  = c == 0 ? dx : dy;
-      r += W * (nu * (gcx * dx + gcy * dy) - S.p[q] * dc)
-           + WNa * (ux * gcx + uy * gcy);
-      if (kJac)
+      T da = S.G3[0] * ref.S00[sa][b] + S.G3[1] * ref.S11[sa][b] + S.G3[2] * ref.S01[sa][b];
+#pragma unroll
+      for (int q = 0; q < kNq; ++q)
       {
-        const T Wnu = W * nu;
-#pragma unroll
-        for (int sb = 0; sb < 6; ++sb)
-        {
-          const T bx   = S.dN[q][sb][0], by = S.dN[q][sb][1];
-          const T diff = bx * dx + by * dy;
-          const T adv  = ux * bx + uy * by;
-          const T tNb  = WNa * T(tab.N[q][sb]);
-          jcc[sb] += Wnu * diff + WNa * adv + tNb * gcc;
-          jco[sb] += tNb * gco;
-        }
-        const T wd = W * dc;
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-        {
-          jp[b] -= wd * T(tab.P[q][b]);
-        }
+        da += ref.wN[q][sa] * S.vq[q][b];
       }
+      const T mcc = ref.T[0][sa][b] * Gcc[0] + ref.T[1][sa][b] * Gcc[1]
+                    + ref.T[2][sa][b] * Gcc[2];
+      const T mco = ref.T[0][sa][b] * Gco[0] + ref.T[1][sa][b] * Gco[1]
+                    + ref.T[2][sa][b] * Gco[2];
+      jcc[b] = da + mcc;
+      jco[b] = mco;
+      r += da * S.st[2 * b + c];
+    }
+    const T ic0 = S.aInvJ[0 * 2 + c], ic1 = S.aInvJ[1 * 2 + c];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+    {
+      jp[b] = -(ic0 * ref.C[0][sa][b] + ic1 * ref.C[1][sa][b]);
+      r += jp[b] * S.st[12 + b];
     }
   }
   else
   {
     const int b = l - 12;
-    for (int q = 0; q < kNq; ++q)
-    {
-      const T wp = S.W[q] * T(tab.P[q][b]);
-      r -= wp * (S.G[q][0] + S.G[q][3]);
-      if (kJac)
-      {
 #pragma unroll
-        for (int sa = 0; sa < 6; ++sa)
-        {
-          jcc[sa] -= wp * S.dN[q][sa][0];
-          jco[sa] -= wp * S.dN[q][sa][1];
-        }
-      }
+    for (int sa = 0; sa < 6; ++sa)
+    {
+      const T c0 = ref.C[0][sa][b], c1 = ref.C[1][sa][b];
+      jcc[sa]    = -(S.aInvJ[0] * c0 + S.aInvJ[2] * c1);
+      jco[sa]    = -(S.aInvJ[1] * c0 + S.aInvJ[3] * c1);
+      r += jcc[sa] * S.st[2 * sa] + jco[sa] * S.st[2 * sa + 1];
     }
   }
-  gbfem::redAdd(a.res + a.dofs[15 * e + l], double(r));
+  const int row_dof = a.dofs[15 * e + l];
+  gbfem::redAdd(a.res + row_dof, double(r));
   if (kJac)
   {
-    const int* jm = a.jac_map + 225 * e + 15 * l;
-#pragma unroll
-    for (int sb = 0; sb < 6; ++sb)
+    double*   out = a.vals;
+    const int rs  = a.row_ptr[row_dof];
+    int       col[15];
+    if (a.jac_pos != nullptr)
     {
-      gbfem::redAdd(a.vals + jm[2 * sb + c], double(jcc[sb]));
-      gbfem::redAdd(a.vals + jm[2 * sb + (c ^ 1)], double(jco[sb]));
+      const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
+      const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        col[j] = rs + int((wd[j >> 2] >> (8 * (j & 3))) & 0xffu);
+      }
     }
-#pragma unroll
-    for (int b = 0; b < 3; ++b)
+    else
     {
-      gbfem::redAdd(a.vals + jm[12 + b], double(jp[b]));
+      const int* jm = a.jac_map + 225LL * e + 15 * l;
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        col[j] = jm[j];
+      }
+    }
+    if (l < 12)
+    {
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
+      {
+        // velocity columns (b, c) and (b, 1-c) of local order 2b + comp
+        const int k0 = c == 0 ? col[2 * b] : col[2 * b + 1];
+        const int k1 = c == 0 ? col[2 * b + 1] : col[2 * b];
+        gbfem::redAdd(out + k0, double(jcc[b]));
+        gbfem::redAdd(out + k1, double(jco[b]));
+      }
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+      {
+        gbfem::redAdd(out + col[12 + b], double(jp[b]));
+      }
+    }
+    else
+    {
+#pragma unroll
+      for (int sa = 0; sa < 6; ++sa)
+      {
+        gbfem::redAdd(out + col[2 * sa], double(jcc[sa]));
+        gbfem::redAdd(out + col[2 * sa + 1], double(jco[sa]));
+      }
+      // the pressure-pressure block is structurally present and zero
     }
   }
 }
@@ -383,6 +507,8 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     a.nu      = nu;
     a.state   = state;
     a.jac_map = map->jac_map;
+    a.row_ptr = map->row_ptr;
+    a.jac_pos = map->pos_stride == 16 ? map->jac_pos : nullptr;
     a.res     = res;
     a.vals    = vals;
     a.status  = map->status;

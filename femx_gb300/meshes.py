@@ -216,3 +216,35 @@ def stream_velocity(coords: np.ndarray, seed: int, nmodes: int = 16) -> np.ndarr
         u[:, 0] += c[k] * np.sin(a * x) * b * np.cos(b * y)
         u[:, 1] -= c[k] * a * np.cos(a * x) * np.sin(b * y)
     return u
+
+
+def cavity_dirichlet(coords_p2: np.ndarray, num_p2_nodes: int, tol: float = 1e-12):
+    """Lid-driven cavity constraints on the Taylor-Hood layout.
+
+    Issued the way a femx user would with DirichletBC (DirichletBC.cpp:127-146,
+    ascending nodes per call): lid u_x = 1, lid u_y = 0, walls u_x = 0,
+    walls u_y = 0 (lid = nodes with y = 1, corners included), then the
+    pressure pin at vertex 0 (gaugeDofs, femx/model/ns/Helper.cpp:61-82).
+    Returns (dofs int32, values float64).
+    """
+    bnd = boundary_nodes(coords_p2, tol)
+    lid = np.abs(coords_p2[:, 1] - 1.0) < tol
+    wall = bnd & ~lid
+    parts = [
+        (dirichlet_dofs(coords_p2, lid, comps=2, comp=0), 1.0),
+        (dirichlet_dofs(coords_p2, lid, comps=2, comp=1), 0.0),
+        (dirichlet_dofs(coords_p2, wall, comps=2, comp=0), 0.0),
+        (dirichlet_dofs(coords_p2, wall, comps=2, comp=1), 0.0),
+        (np.array([2 * num_p2_nodes], dtype=np.int32), 0.0),
+    ]
+    dofs = np.concatenate([p[0] for p in parts]).astype(np.int32)
+    vals = np.concatenate([np.full(len(p[0]), p[1]) for p in parts])
+    return dofs, vals
+
+
+def cavity_state(coords_p2: np.ndarray, num_vertices: int, seed: int):
+    """Seeded Newton iterate: stream-function velocity at the P2 nodes, N(0,1)
+    pressure at the vertices; flattened in the Taylor-Hood DOF order."""
+    vel = stream_velocity(coords_p2, seed)
+    p = np.random.default_rng(seed).standard_normal(num_vertices)
+    return np.concatenate([vel.reshape(-1), p])

@@ -561,6 +561,12 @@ struct TaylorHoodNS
   void evalRow(int e, int row, const double* st, double& res,
                double* jac) const
   {
+    evalRowNu(nu, e, row, st, res, jac);
+  }
+
+  void evalRowNu(double nu, int e, int row, const double* st, double& res,
+                 double* jac) const
+  {
     res = 0.0;
     for (int c = 0; c < 15; ++c)
     {
@@ -644,12 +650,17 @@ struct TaylorHoodNS
 // residual rows through res_dofs and Jacobian entries through jac_map.
 template <class Op>
 void assembleLoop(const Map& m, const Op& op, const double* state,
-                  double* res, double* vals)
+                  double* res, double* vals, int e0 = 0, int e1 = -1)
 {
+  if (e1 < 0 || e1 > m.num_elems)
+  {
+    e1 = m.num_elems;
+  }
+  require(e0 >= 0 && e0 <= e1, "element range is invalid");
   std::fill(res, res + m.num_res, 0.0);
   std::fill(vals, vals + m.row_ptr[m.num_res], 0.0);
   std::vector<double> st(m.max_state), re(m.max_res), jac(m.max_jac);
-  for (int e = 0; e < m.num_elems; ++e)
+  for (int e = e0; e < e1; ++e)
   {
     const int nr = m.nrow(e), nc = m.ncol(e);
     for (int c = 0; c < nc; ++c)
@@ -935,6 +946,53 @@ int orc_vjp_p1_kappa(const void* mh, const void* qh, const int* conn,
   });
 }
 
+void* orc_th_quad_create(int num_p2_nodes, const double* coords,
+                         int num_elems, const int* conn6)
+{
+  TaylorHoodNS* out = nullptr;
+  guarded([&] {
+    auto* t = new TaylorHoodNS;
+    try
+    {
+      t->build(num_p2_nodes, coords, num_elems, conn6);
+    }
+    catch (...)
+    {
+      delete t;
+      throw;
+    }
+    out = t;
+  });
+  return out;
+}
+
+void orc_th_quad_free(void* h)
+{
+  delete static_cast<TaylorHoodNS*>(h);
+}
+
+int orc_assemble_th_range(const void* mh, const void* th, double nu,
+                          const double* state, double* res, double* vals,
+                          int e0, int e1)
+{
+  return guarded([&] {
+    const Map& m = *static_cast<const Map*>(mh);
+    require(m.max_res <= 15 && m.max_state <= 15,
+            "Taylor-Hood element expects 15 DOFs per element");
+    // Borrow the prebuilt tables; only the viscosity is per call.
+    struct Op
+    {
+      const TaylorHoodNS* t;
+      double              nu;
+      void evalRow(int e, int row, const double* st, double& res, double* jac) const
+      {
+        t->evalRowNu(nu, e, row, st, res, jac);
+      }
+    } op{static_cast<const TaylorHoodNS*>(th), nu};
+    assembleLoop(m, op, state, res, vals, e0, e1);
+  });
+}
+
 int orc_assemble_th_ns(const void* mh, int num_p2_nodes, const double* coords,
                        const int* conn6, double nu, const double* state,
                        double* res, double* vals)
@@ -947,6 +1005,21 @@ int orc_assemble_th_ns(const void* mh, int num_p2_nodes, const double* coords,
     op.nu = nu;
     op.build(num_p2_nodes, coords, m.num_elems, conn6);
     assembleLoop(m, op, state, res, vals);
+  });
+}
+
+int orc_assemble_p1_range(const void* mh, const void* qh, const int* conn,
+                          const double* kappa, const double* f_nodal,
+                          const double* u, double* res, double* vals, int e0,
+                          int e1)
+{
+  return guarded([&] {
+    const Map&    m = *static_cast<const Map*>(mh);
+    const P1Quad& q = *static_cast<const P1Quad*>(qh);
+    require(q.ne == m.num_elems,
+            "Geometry and AssemblyMap have different element counts");
+    const KappaPoissonP1 op{&q, conn, kappa, f_nodal};
+    assembleLoop(m, op, u, res, vals, e0, e1);
   });
 }
 

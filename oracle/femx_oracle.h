@@ -104,10 +104,27 @@ int orc_vjp_p1_kappa(const void* map, const void* quad, const int* conn,
  *   R_p(b)   = -int psi_b div u
  * and its exact Jacobian are accumulated through the generic element loop
  * with one evalRow per local row (femx/assembly/Assembly.hpp:153-226), using
- * the 6-point degree-4 triangle rule. state/res/vals in global DOF order. */
+ * the 6-point degree-4 triangle rule. state/res/vals in global DOF order.
+ * orc_th_quad_create builds the per-element tables once (the analogue of
+ * ElementQuadratureData, ElementQuadratureData.cpp:14-59). */
+void* orc_th_quad_create(int num_p2_nodes, const double* coords,
+                         int num_elems, const int* conn6);
+void  orc_th_quad_free(void* th);
+/* Assembles elements [elem_begin, elem_end) (the whole mesh when
+ * elem_end < 0); outputs are zeroed first. */
+int orc_assemble_th_range(const void* map, const void* th, double nu,
+                          const double* state, double* res, double* vals,
+                          int elem_begin, int elem_end);
+/* Whole-mesh convenience: builds the tables and assembles every element. */
 int orc_assemble_th_ns(const void* map, int num_p2_nodes,
                        const double* coords, const int* conn6, double nu,
                        const double* state, double* res, double* vals);
+
+/* Elements [elem_begin, elem_end) of the P1 assembly (bounded CPU samples). */
+int orc_assemble_p1_range(const void* map, const void* quad, const int* conn,
+                          const double* kappa, const double* f_nodal,
+                          const double* u, double* res, double* vals,
+                          int elem_begin, int elem_end);
 
 #ifdef __cplusplus
 }

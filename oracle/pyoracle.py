@@ -63,6 +63,11 @@ def lib():
         L.orc_assemble_p1_kappa.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, C.c_void_p, _f64p, _f64p, _f64p]
         L.orc_vjp_p1_kappa.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, _f64p, _f64p, C.c_void_p, C.c_void_p]
         L.orc_assemble_th_ns.argtypes = [C.c_void_p, C.c_int, _f64p, _i32p, C.c_double, _f64p, _f64p, _f64p]
+        L.orc_th_quad_create.restype = C.c_void_p
+        L.orc_th_quad_create.argtypes = [C.c_int, _f64p, C.c_int, _i32p]
+        L.orc_th_quad_free.argtypes = [C.c_void_p]
+        L.orc_assemble_th_range.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int, C.c_int]
+        L.orc_assemble_p1_range.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, C.c_void_p, _f64p, _f64p, _f64p, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -228,4 +233,41 @@ def assemble_th_ns(amap: AssemblyMap, coords_p2, conn6, nu, state):
     c = _f64(coords_p2)
     _check(lib().orc_assemble_th_ns(amap.h, c.shape[0], c, _i32(conn6), float(nu), _f64(state),
                                     res, vals))
+    return res, vals
+
+
+class THQuad:
+    """Per-element Taylor-Hood tables (ElementQuadratureData analogue)."""
+
+    def __init__(self, coords_p2, conn6):
+        self.coords = _f64(coords_p2)
+        self.conn6 = _i32(conn6)
+        h = lib().orc_th_quad_create(self.coords.shape[0], self.coords, self.conn6.shape[0],
+                                     self.conn6)
+        if not h:
+            raise OracleError(lib().orc_last_error().decode())
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_th_quad_free(self.h)
+            self.h = None
+
+
+def assemble_th_range(amap: AssemblyMap, th: THQuad, nu, state, elem_begin=0, elem_end=-1,
+                      res=None, vals=None):
+    res = np.zeros(amap.num_res) if res is None else res
+    vals = np.zeros(amap.nnz) if vals is None else vals
+    _check(lib().orc_assemble_th_range(amap.h, th.h, float(nu), _f64(state), res, vals,
+                                       int(elem_begin), int(elem_end)))
+    return res, vals
+
+
+def assemble_p1_range(amap: AssemblyMap, quad: P1Quad, kappa, f_nodal, u, elem_begin=0,
+                      elem_end=-1, res=None, vals=None):
+    res = np.zeros(amap.num_res) if res is None else res
+    vals = np.zeros(amap.nnz) if vals is None else vals
+    f = None if f_nodal is None else _f64(f_nodal)
+    _check(lib().orc_assemble_p1_range(amap.h, quad.h, quad.conn, _f64(kappa), _ptr(f), _f64(u),
+                                       res, vals, int(elem_begin), int(elem_end)))
     return res, vals
