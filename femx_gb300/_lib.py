@@ -21,6 +21,7 @@ GBFEM_ENOMEM = 4
 
 PREC_FP64 = 0
 PREC_FP32_QUAD = 1
+PREC_MIXED = 2
 
 
 class GbfemError(RuntimeError):
@@ -80,6 +81,7 @@ SIGNATURES = {
     "gbfem_vjp_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
     "gbfem_probe_fp64_fma": (_i, [_i, _i, _i, _vp, _vp]),
+    "gbfem_probe_convert": (_i, [_i, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

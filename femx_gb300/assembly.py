@@ -35,7 +35,8 @@ __all__ = [
     "axpby", "PRECISIONS",
 ]
 
-PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32_quad": _lib.PREC_FP32_QUAD}
+PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32_quad": _lib.PREC_FP32_QUAD,
+              "mixed": _lib.PREC_MIXED}
 
 
 def _stream():

@@ -145,6 +145,78 @@ long long exclusiveScan(const int* in, int* out, long long n, cudaStream_t s);
 long long exclusiveScan64to32(const long long* in, int* out, long long n,
                               cudaStream_t s);
 
+// Exact float -> double conversion from the IEEE-754 fields, on the integer
+// pipe. On GB300 the hardware conversion issues on the FP64 pipe (the scarce
+// one), so kernels whose element math runs in FP32 convert with this.
+// Normal numbers and zeros take the integer path; subnormal, infinite and NaN
+// inputs (absent from FE data) fall back to the hardware conversion.
+__device__ __forceinline__ double f32ToF64(float f)
+{
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if ((u & 0x7fffffffu) == 0u)
+  {
+    return __longlong_as_double(static_cast<long long>(u & 0x80000000u) << 32);
+  }
+  if (e - 1u >= 0xfeu)
+  {
+    return static_cast<double>(f);
+  }
+  const unsigned long long bits =
+      (static_cast<unsigned long long>(u & 0x80000000u) << 32)
+      | (static_cast<unsigned long long>(e + 896u) << 52)
+      | (static_cast<unsigned long long>(u & 0x7fffffu) << 29);
+  return __longlong_as_double(static_cast<long long>(bits));
+}
+
+// double -> float with round-to-nearest-even, from the IEEE-754 fields on
+// the integer pipe (same reason as above). Values whose float result is
+// normal take the integer path; zeros are exact; anything that would be
+// subnormal, infinite or NaN uses the hardware conversion.
+__device__ __forceinline__ float f64ToF32(double d)
+{
+  const unsigned long long b  = static_cast<unsigned long long>(__double_as_longlong(d));
+  const unsigned           hi = static_cast<unsigned>(b >> 32);
+  const unsigned           lo = static_cast<unsigned>(b);
+  const unsigned           s  = hi & 0x80000000u;
+  const int                fe = static_cast<int>((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if ((b << 1) == 0ull)
+  {
+    return __uint_as_float(s);
+  }
+  if (fe <= 0 || fe >= 255)
+  {
+    return __double2float_rn(d);
+  }
+  const unsigned m    = ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rem  = lo & 0x1fffffffu;
+  const unsigned half = 0x10000000u;
+  unsigned       r    = s | (static_cast<unsigned>(fe) << 23) | m;
+  r += (rem > half || (rem == half && (m & 1u))) ? 1u : 0u; // carry may round up to inf
+  return __uint_as_float(r);
+}
+
+template <class T>
+__device__ __forceinline__ T fromF64(double d);
+template <>
+__device__ __forceinline__ double fromF64<double>(double d)
+{
+  return d;
+}
+template <>
+__device__ __forceinline__ float fromF64<float>(double d)
+{
+  return f64ToF32(d);
+}
+__device__ __forceinline__ double toF64(double d)
+{
+  return d;
+}
+__device__ __forceinline__ double toF64(float f)
+{
+  return f32ToF64(f);
+}
+
 // FP64 reduction-add at L2 without a return value.
 __device__ __forceinline__ void redAdd(double* addr, double v)
 {

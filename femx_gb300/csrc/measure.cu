@@ -30,7 +30,31 @@ __global__ void fp64FmaProbe(int iters, double* out)
   }
   out[t] = s;
 }
+__global__ void convertProbe(int n, const double* in, float* out_f, double* out_d)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    const float f = gbfem::f64ToF32(in[i]);
+    out_f[i]      = f;
+    out_d[i]      = gbfem::f32ToF64(f);
+  }
+}
 } // namespace
+
+extern "C" int gbfem_probe_convert(int n, const double* in, float* out_f,
+                                   double* out_d, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(n >= 0 && (n == 0 || (in && out_f && out_d)), "probe arguments are invalid");
+    if (n > 0)
+    {
+      convertProbe<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, in, out_f, out_d);
+      cudaCheck(cudaGetLastError(), "convert probe launch");
+    }
+  });
+}
 
 extern "C" int gbfem_probe_fp64_fma(int blocks, int threads, int iters,
                                     double* out, void* stream)

@@ -51,8 +51,8 @@ template <class T>
 __device__ __forceinline__ bool elementK(double2 x0, double2 x1, double2 x2,
                                          double kappa, ElemK<T>& K)
 {
-  const T ax = T(x1.x - x0.x), ay = T(x1.y - x0.y);
-  const T bx = T(x2.x - x0.x), by = T(x2.y - x0.y);
+  const T ax = gbfem::fromF64<T>(x1.x - x0.x), ay = gbfem::fromF64<T>(x1.y - x0.y);
+  const T bx = gbfem::fromF64<T>(x2.x - x0.x), by = gbfem::fromF64<T>(x2.y - x0.y);
   const T det  = ax * by - bx * ay;
   const T adet = det < T(0) ? -det : det;
   if (!(adet >= T(1.0e-30)))
@@ -61,7 +61,7 @@ __device__ __forceinline__ bool elementK(double2 x0, double2 x1, double2 x2,
   }
   // h1 = (by, -bx), h2 = (-ay, ax), h0 = -(h1 + h2) = (ay - by, bx - ax)
   const T h0x = ay - by, h0y = bx - ax;
-  const T s   = T(kappa) * T(0.5) / adet;
+  const T s   = gbfem::fromF64<T>(kappa) * T(0.5) / adet;
   K.k01       = s * (h0x * by - h0y * bx);
   K.k02       = s * (-h0x * ay + h0y * ax);
   K.k12       = s * (-by * ay - bx * ax);
@@ -72,7 +72,7 @@ __device__ __forceinline__ bool elementK(double2 x0, double2 x1, double2 x2,
   return true;
 }
 
-template <bool kF32, bool kSepConn, bool kLoad, bool kJac>
+template <bool kF32, bool kSepConn, bool kLoad, bool kJac, bool kRes = true>
 __global__ void __launch_bounds__(256) p1AssembleKernel(P1Args a)
 {
   using T     = typename std::conditional<kF32, float, double>::type;
@@ -102,27 +102,34 @@ __global__ void __launch_bounds__(256) p1AssembleKernel(P1Args a)
     gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
     return;
   }
-  const double u0 = a.u[d0], u1 = a.u[d1], u2 = a.u[d2];
-  double r0 = double(K.k00) * u0 + double(K.k01) * u1 + double(K.k02) * u2;
-  double r1 = double(K.k01) * u0 + double(K.k11) * u1 + double(K.k12) * u2;
-  double r2 = double(K.k02) * u0 + double(K.k12) * u1 + double(K.k22) * u2;
+  // Element residual in T (FP64 on the plain path); accumulation in FP64.
+  const T u0 = gbfem::fromF64<T>(a.u[d0]), u1 = gbfem::fromF64<T>(a.u[d1]);
+  const T u2 = gbfem::fromF64<T>(a.u[d2]);
+  T r0 = K.k00 * u0 + K.k01 * u1 + K.k02 * u2;
+  T r1 = K.k01 * u0 + K.k11 * u1 + K.k12 * u2;
+  T r2 = K.k02 * u0 + K.k12 * u1 + K.k22 * u2;
   if (kLoad)
   {
-    const double f0 = a.f[n0], f1 = a.f[n1], f2 = a.f[n2];
-    const double fs = f0 + f1 + f2;
-    const double c  = double(K.adet) * (1.0 / 24.0);
+    const T f0 = gbfem::fromF64<T>(a.f[n0]), f1 = gbfem::fromF64<T>(a.f[n1]);
+    const T f2 = gbfem::fromF64<T>(a.f[n2]);
+    const T fs = f0 + f1 + f2;
+    const T c  = K.adet * T(1.0 / 24.0);
     r0 -= c * (f0 + fs);
     r1 -= c * (f1 + fs);
     r2 -= c * (f2 + fs);
   }
-  gbfem::redAdd(a.res + d0, r0);
-  gbfem::redAdd(a.res + d1, r1);
-  gbfem::redAdd(a.res + d2, r2);
+  if (kRes)
+  {
+    gbfem::redAdd(a.res + d0, gbfem::toF64(r0));
+    gbfem::redAdd(a.res + d1, gbfem::toF64(r1));
+    gbfem::redAdd(a.res + d2, gbfem::toF64(r2));
+  }
   if (kJac)
   {
-    const double v[9] = {double(K.k00), double(K.k01), double(K.k02),
-                         double(K.k01), double(K.k11), double(K.k12),
-                         double(K.k02), double(K.k12), double(K.k22)};
+    const double k00 = gbfem::toF64(K.k00), k01 = gbfem::toF64(K.k01);
+    const double k02 = gbfem::toF64(K.k02), k11 = gbfem::toF64(K.k11);
+    const double k12 = gbfem::toF64(K.k12), k22 = gbfem::toF64(K.k22);
+    const double v[9] = {k00, k01, k02, k01, k11, k12, k02, k12, k22};
     if (a.jac_pos != nullptr)
     {
       const int d[3] = {d0, d1, d2};
@@ -182,21 +189,24 @@ __global__ void __launch_bounds__(256)
     gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
     return;
   }
-  const double l0 = lam[d0], l1 = lam[d1], l2 = lam[d2];
+  const T l0 = gbfem::fromF64<T>(lam[d0]), l1 = gbfem::fromF64<T>(lam[d1]);
+  const T l2 = gbfem::fromF64<T>(lam[d2]);
   // K is symmetric: K^T lam = K lam.
-  const double v0 = double(K.k00) * l0 + double(K.k01) * l1 + double(K.k02) * l2;
-  const double v1 = double(K.k01) * l0 + double(K.k11) * l1 + double(K.k12) * l2;
-  const double v2 = double(K.k02) * l0 + double(K.k12) * l1 + double(K.k22) * l2;
+  const T v0 = K.k00 * l0 + K.k01 * l1 + K.k02 * l2;
+  const T v1 = K.k01 * l0 + K.k11 * l1 + K.k12 * l2;
+  const T v2 = K.k02 * l0 + K.k12 * l1 + K.k22 * l2;
   if (g_u != nullptr)
   {
-    gbfem::redAdd(g_u + d0, v0);
-    gbfem::redAdd(g_u + d1, v1);
-    gbfem::redAdd(g_u + d2, v2);
+    gbfem::redAdd(g_u + d0, gbfem::toF64(v0));
+    gbfem::redAdd(g_u + d1, gbfem::toF64(v1));
+    gbfem::redAdd(g_u + d2, gbfem::toF64(v2));
   }
   if (g_m != nullptr)
   {
     // lam^T K u = (K lam) . u
-    g_m[e] = v0 * a.u[d0] + v1 * a.u[d1] + v2 * a.u[d2];
+    const T u0 = gbfem::fromF64<T>(a.u[d0]), u1 = gbfem::fromF64<T>(a.u[d1]);
+    const T u2 = gbfem::fromF64<T>(a.u[d2]);
+    g_m[e]     = gbfem::toF64(v0 * u0 + v1 * u1 + v2 * u2);
   }
 }
 
@@ -269,7 +279,7 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     require(res != nullptr, "Assembly residual output is null");
     require(res != u && vals != u && (vals == nullptr || res != vals),
             "Assembly state, residual, and matrix values must not alias");
-    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
             "unknown precision mode");
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
@@ -290,15 +300,30 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     }
     const bool load = f_nodal != nullptr, jac = vals != nullptr;
     const bool sep  = conn != nullptr;
-    if (precision == GBFEM_PREC_FP64)
+    if (precision == GBFEM_PREC_FP64 || (precision == GBFEM_PREC_MIXED && !jac))
     {
       sep ? launchAssemble<false, true>(a, load, jac, s)
           : launchAssemble<false, false>(a, load, jac, s);
     }
-    else
+    else if (precision == GBFEM_PREC_FP32_QUAD)
     {
       sep ? launchAssemble<true, true>(a, load, jac, s)
           : launchAssemble<true, false>(a, load, jac, s);
+    }
+    else
+    {
+      // Jacobian from FP32 quadrature, residual from FP64 element math
+      const unsigned blocks = blocksFor(a.ne, 256);
+      if (sep)
+      {
+        p1AssembleKernel<true, true, false, true, false><<<blocks, 256, 0, s>>>(a);
+      }
+      else
+      {
+        p1AssembleKernel<true, false, false, true, false><<<blocks, 256, 0, s>>>(a);
+      }
+      sep ? launchAssemble<false, true>(a, load, false, s)
+          : launchAssemble<false, false>(a, load, false, s);
     }
     cudaCheck(cudaGetLastError(), "P1 assembly launch");
   });
@@ -316,7 +341,7 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     require(lam != nullptr, "VJP adjoint input is null");
     require(g_u != lam && g_u != u && g_m != lam && g_m != u,
             "VJP outputs must not alias inputs");
-    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
             "unknown precision mode");
     cudaStream_t s = asStream(stream);
     if (g_u != nullptr)
@@ -330,7 +355,7 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     }
     const unsigned blocks = blocksFor(a.ne, 256);
     const bool     sep    = conn != nullptr;
-    if (precision == GBFEM_PREC_FP64)
+    if (precision != GBFEM_PREC_FP32_QUAD)
     {
       sep ? p1VjpKernel<false, true><<<blocks, 256, 0, s>>>(a, lam, g_u, g_m)
           : p1VjpKernel<false, false><<<blocks, 256, 0, s>>>(a, lam, g_u, g_m);

@@ -236,11 +236,16 @@ struct ElemShared
   int ok;
 };
 
-template <class T, bool kJac>
+template <class T, bool kJac, bool kRes>
 __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
 {
   __shared__ ThRef<T>      ref;
   __shared__ ElemShared<T> sh[kElemsPerBlock];
+  // Row-major staging of each element's 15x15 block (values and CSR slots)
+  // so that the scatter issues one row per half-warp instruction: lanes then
+  // hit the same row segment and the L2 reductions coalesce.
+  __shared__ double outv[kElemsPerBlock][15][16];
+  __shared__ int    outk[kElemsPerBlock][15][16];
   {
     const T* src = reinterpret_cast<const T*>(refTables(T()));
     T*       dst = reinterpret_cast<T*>(&ref);
@@ -257,7 +262,7 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
 
   if (has && l < 15)
   {
-    S.st[l] = T(a.state[a.dofs[15 * e + l]]);
+    S.st[l] = gbfem::fromF64<T>(a.state[a.dofs[15 * e + l]]);
   }
   if (has && l == 15)
   {
@@ -278,29 +283,30 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
       const double2 x0 = a.coords[a.conn6[6 * e + 0]];
       const double2 x1 = a.coords[a.conn6[6 * e + 1]];
       const double2 x2 = a.coords[a.conn6[6 * e + 2]];
-      // J[a][b] = d x_a / d r_b of the affine map (vertex nodes)
-      const double j00 = x1.x - x0.x, j01 = x2.x - x0.x;
-      const double j10 = x1.y - x0.y, j11 = x2.y - x0.y;
-      const double det = j00 * j11 - j01 * j10;
-      const double ad  = fabs(det);
-      if (ad >= 1.0e-30)
+      // J[a][b] = d x_a / d r_b of the affine map (vertex nodes); the edge
+      // vectors carry the mesh scale and are formed in FP64, the rest in T.
+      const T j00 = gbfem::fromF64<T>(x1.x - x0.x), j01 = gbfem::fromF64<T>(x2.x - x0.x);
+      const T j10 = gbfem::fromF64<T>(x1.y - x0.y), j11 = gbfem::fromF64<T>(x2.y - x0.y);
+      const T det = j00 * j11 - j01 * j10;
+      const T ad  = det < T(0) ? -det : det;
+      if (ad >= T(1.0e-30))
       {
-        S.ok             = 1;
-        const double inv = 1.0 / det;
-        const double i00 = j11 * inv, i01 = -j01 * inv;
-        const double i10 = -j10 * inv, i11 = j00 * inv;
-        S.invJ[0]        = T(i00);
-        S.invJ[1]        = T(i01);
-        S.invJ[2]        = T(i10);
-        S.invJ[3]        = T(i11);
-        S.aInvJ[0]       = T(ad * i00);
-        S.aInvJ[1]       = T(ad * i01);
-        S.aInvJ[2]       = T(ad * i10);
-        S.aInvJ[3]       = T(ad * i11);
-        const double nad = a.nu * ad;
-        S.G3[0]          = T(nad * (i00 * i00 + i01 * i01));
-        S.G3[1]          = T(nad * (i10 * i10 + i11 * i11));
-        S.G3[2]          = T(nad * (i00 * i10 + i01 * i11));
+        S.ok        = 1;
+        const T inv = T(1) / det;
+        const T i00 = j11 * inv, i01 = -j01 * inv;
+        const T i10 = -j10 * inv, i11 = j00 * inv;
+        S.invJ[0]   = i00;
+        S.invJ[1]   = i01;
+        S.invJ[2]   = i10;
+        S.invJ[3]   = i11;
+        S.aInvJ[0]  = ad * i00;
+        S.aInvJ[1]  = ad * i01;
+        S.aInvJ[2]  = ad * i10;
+        S.aInvJ[3]  = ad * i11;
+        const T nad = T(a.nu) * ad;
+        S.G3[0]     = nad * (i00 * i00 + i01 * i01);
+        S.G3[1]     = nad * (i10 * i10 + i11 * i11);
+        S.G3[2]     = nad * (i00 * i10 + i01 * i11);
       }
       else
       {
@@ -348,10 +354,7 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
     }
   }
   __syncthreads();
-  if (!live || l >= 15)
-  {
-    return;
-  }
+  const bool row_lane = live && l < 15;
 
   // Row l: velocity (sa, c) for l < 12, pressure b = l - 12 otherwise.
   // jcc[b] -> column (b, c), jco[b] -> (b, 1-c), jp[b] -> pressure b;
@@ -359,7 +362,7 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
   T   jcc[6], jco[6], jp[3] = {0, 0, 0};
   T   r = 0;
   int c = 0;
-  if (l < 12)
+  if (row_lane && l < 12)
   {
     const int sa = l >> 1;
     c            = l & 1;
@@ -391,7 +394,7 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
       r += jp[b] * S.st[12 + b];
     }
   }
-  else
+  else if (row_lane)
   {
     const int b = l - 12;
 #pragma unroll
@@ -403,58 +406,86 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
       r += jcc[sa] * S.st[2 * sa] + jco[sa] * S.st[2 * sa + 1];
     }
   }
-  const int row_dof = a.dofs[15 * e + l];
-  gbfem::redAdd(a.res + row_dof, double(r));
+  if (row_lane)
+  {
+    const int row_dof = a.dofs[15 * e + l];
+    if (kRes)
+    {
+      gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
+    }
+    if (kJac)
+    {
+      const int rs = a.row_ptr[row_dof];
+      int       col[15];
+      if (a.jac_pos != nullptr)
+      {
+        const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
+        const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int j = 0; j < 15; ++j)
+        {
+          col[j] = rs + int((wd[j >> 2] >> (8 * (j & 3))) & 0xffu);
+        }
+      }
+      else
+      {
+        const int* jm = a.jac_map + 225LL * e + 15 * l;
+#pragma unroll
+        for (int j = 0; j < 15; ++j)
+        {
+          col[j] = jm[j];
+        }
+      }
+      double* ov = outv[le][l];
+      int*    ok = outk[le][l];
+      if (l < 12)
+      {
+#pragma unroll
+        for (int b = 0; b < 6; ++b)
+        {
+          // local columns 2b (component 0) and 2b + 1 (component 1)
+          ov[2 * b + c]       = gbfem::toF64(jcc[b]);
+          ov[2 * b + (c ^ 1)] = gbfem::toF64(jco[b]);
+        }
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+        {
+          ov[12 + b] = gbfem::toF64(jp[b]);
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int sa = 0; sa < 6; ++sa)
+        {
+          ov[2 * sa]     = gbfem::toF64(jcc[sa]);
+          ov[2 * sa + 1] = gbfem::toF64(jco[sa]);
+        }
+        // the pressure-pressure block is structurally present and zero
+        ov[12] = ov[13] = ov[14] = 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        ok[j] = col[j];
+      }
+    }
+  }
   if (kJac)
   {
-    double*   out = a.vals;
-    const int rs  = a.row_ptr[row_dof];
-    int       col[15];
-    if (a.jac_pos != nullptr)
+    __syncwarp();
+    if (live && l < 15)
     {
-      const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
-      const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-      for (int j = 0; j < 15; ++j)
+      // lane l now owns local column l of every row of its element
+#pragma unroll 5
+      for (int row = 0; row < 15; ++row)
       {
-        col[j] = rs + int((wd[j >> 2] >> (8 * (j & 3))) & 0xffu);
+        const double v = outv[le][row][l];
+        if (row < 12 || l < 12)
+        {
+          gbfem::redAdd(a.vals + outk[le][row][l], v);
+        }
       }
-    }
-    else
-    {
-      const int* jm = a.jac_map + 225LL * e + 15 * l;
-#pragma unroll
-      for (int j = 0; j < 15; ++j)
-      {
-        col[j] = jm[j];
-      }
-    }
-    if (l < 12)
-    {
-#pragma unroll
-      for (int b = 0; b < 6; ++b)
-      {
-        // velocity columns (b, c) and (b, 1-c) of local order 2b + comp
-        const int k0 = c == 0 ? col[2 * b] : col[2 * b + 1];
-        const int k1 = c == 0 ? col[2 * b + 1] : col[2 * b];
-        gbfem::redAdd(out + k0, double(jcc[b]));
-        gbfem::redAdd(out + k1, double(jco[b]));
-      }
-#pragma unroll
-      for (int b = 0; b < 3; ++b)
-      {
-        gbfem::redAdd(out + col[12 + b], double(jp[b]));
-      }
-    }
-    else
-    {
-#pragma unroll
-      for (int sa = 0; sa < 6; ++sa)
-      {
-        gbfem::redAdd(out + col[2 * sa], double(jcc[sa]));
-        gbfem::redAdd(out + col[2 * sa + 1], double(jco[sa]));
-      }
-      // the pressure-pressure block is structurally present and zero
     }
   }
 }
@@ -482,7 +513,7 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     require(res != nullptr, "Assembly residual output is null");
     require(res != state && vals != state && (vals == nullptr || res != vals),
             "Assembly state, residual, and matrix values must not alias");
-    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
             "unknown precision mode");
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
@@ -514,15 +545,21 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     a.status  = map->status;
     const unsigned blocks = blocksFor(a.ne, kElemsPerBlock);
     const bool     jac    = vals != nullptr;
-    if (precision == GBFEM_PREC_FP64)
+    if (precision == GBFEM_PREC_FP64 || (precision == GBFEM_PREC_MIXED && !jac))
     {
-      jac ? thKernel<double, true><<<blocks, kThreads, 0, s>>>(a)
-          : thKernel<double, false><<<blocks, kThreads, 0, s>>>(a);
+      jac ? thKernel<double, true, true><<<blocks, kThreads, 0, s>>>(a)
+          : thKernel<double, false, true><<<blocks, kThreads, 0, s>>>(a);
+    }
+    else if (precision == GBFEM_PREC_FP32_QUAD)
+    {
+      jac ? thKernel<float, true, true><<<blocks, kThreads, 0, s>>>(a)
+          : thKernel<float, false, true><<<blocks, kThreads, 0, s>>>(a);
     }
     else
     {
-      jac ? thKernel<float, true><<<blocks, kThreads, 0, s>>>(a)
-          : thKernel<float, false><<<blocks, kThreads, 0, s>>>(a);
+      // Jacobian from FP32 quadrature, residual from FP64 element math
+      thKernel<float, true, false><<<blocks, kThreads, 0, s>>>(a);
+      thKernel<double, false, true><<<blocks, kThreads, 0, s>>>(a);
     }
     cudaCheck(cudaGetLastError(), "Taylor-Hood assembly launch");
   });

@@ -35,10 +35,13 @@ extern "C" {
 #define GBFEM_ENOMEM 4 /* device allocation failed */
 
 /* Arithmetic of the element kernels. FP64: plain double everywhere (the
- * drop-in). FP32_QUAD: element quadrature in float, accumulation, scatter and
- * all global vectors in double. */
+ * drop-in). FP32_QUAD: element quadrature in float (Jacobian and residual
+ * contributions); accumulation, scatter and all global vectors in double.
+ * MIXED: the Newton scheme — Jacobian from FP32 quadrature, residual from
+ * FP64 element math; accumulation in double. */
 #define GBFEM_PREC_FP64 0
 #define GBFEM_PREC_FP32_QUAD 1
+#define GBFEM_PREC_MIXED 2
 
 GBFEM_API const char* gbfem_last_error(void);
 GBFEM_API int         gbfem_version(void);

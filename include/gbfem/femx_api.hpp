@@ -238,6 +238,7 @@ enum class Precision : int
 {
   FP64     = GBFEM_PREC_FP64,
   FP32Quad = GBFEM_PREC_FP32_QUAD,
+  Mixed    = GBFEM_PREC_MIXED,
 };
 
 /** Element operator tag: kappa-weighted P1 Poisson with nodal load. */

@@ -19,6 +19,13 @@ extern "C" {
 GBFEM_API int gbfem_probe_fp64_fma(int blocks, int threads, int iters,
                                    double* out, void* stream);
 
+/* Test hook for the integer-pipe conversions the FP32 element paths use:
+ * out_f[i] = double->float (round to nearest even) of in[i] and
+ * out_d[i] = float->double of out_f[i], computed the way the kernels do.
+ * The tests compare them with the hardware conversions. */
+GBFEM_API int gbfem_probe_convert(int n, const double* in, float* out_f,
+                                  double* out_d, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

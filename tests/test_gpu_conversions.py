@@ -1,0 +1,58 @@
+"""The FP32 element paths convert between double and float with integer bit
+operations (the hardware conversion issues on GB300's FP64 pipe). These must
+agree bit for bit with IEEE-754 round-to-nearest-even conversion."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from femx_gb300 import build
+    build.build()
+
+
+def run_probe(values: np.ndarray):
+    from femx_gb300 import _lib
+    x = torch.from_numpy(np.ascontiguousarray(values, dtype=np.float64)).cuda()
+    f = torch.empty(x.numel(), dtype=torch.float32, device="cuda")
+    d = torch.empty(x.numel(), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().gbfem_probe_convert(
+        x.numel(), C.c_void_p(x.data_ptr()), C.c_void_p(f.data_ptr()), C.c_void_p(d.data_ptr()),
+        C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    return x, f, d
+
+
+def test_conversions_match_ieee_round_to_nearest_even():
+    rng = np.random.default_rng(0)
+    parts = [
+        rng.standard_normal(1 << 20),
+        rng.standard_normal(1 << 18) * 10.0 ** rng.integers(-40, 40, size=1 << 18),
+        np.array([0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 3.4028235677973366e38,
+                  1.1754943508222875e-38, 1.401298464324817e-45, 5e-324, np.inf, -np.inf,
+                  1e300, -1e-300]),
+    ]
+    # halfway cases: doubles exactly between two floats (ties to even), and
+    # values one ulp either side of the tie
+    base = rng.standard_normal(1 << 16).astype(np.float32).astype(np.float64)
+    ulp = np.spacing(base.astype(np.float32)).astype(np.float64)
+    tie = base + 0.5 * ulp
+    parts += [tie, np.nextafter(tie, np.inf), np.nextafter(tie, -np.inf)]
+    vals = np.concatenate(parts)
+    x, f, d = run_probe(vals)
+    ref_f = x.to(torch.float32)
+    assert torch.equal(f.view(torch.int32), ref_f.view(torch.int32))
+    assert torch.equal(d, ref_f.to(torch.float64))
+
+
+def test_nan_stays_nan():
+    _, f, d = run_probe(np.array([np.nan, -np.nan]))
+    assert torch.isnan(f).all() and torch.isnan(d).all()
