@@ -74,6 +74,7 @@ SIGNATURES = {
     "gbfem_replace_res": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "gbfem_zero_boundary": (_i, [_vp, _vp, _vp]),
     "gbfem_prepare_forward_solve": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "gbfem_prepare_forward_solve_noalloc": (_i, [_i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbfem_spmv": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp]),
     "gbfem_spmv_t": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp]),
     "gbfem_axpby": (_i, [_i, _d, _vp, _d, _vp, _vp]),

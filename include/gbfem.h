@@ -124,6 +124,27 @@ GBFEM_API int gbfem_prepare_forward_solve(const gbfem_boundary_map* bc, double* 
                                 double* rhs, const double* bc_vals,
                                 void* stream);
 
+/* Same result as gbfem_boundary_map_create + gbfem_prepare_forward_solve,
+ * for callers that cannot call cudaMalloc (e.g. code running while another
+ * allocator owns the device memory, such as a PyTorch process whose caching
+ * allocator has reserved it, or a real-time solver loop that must not pay for
+ * allocation). It has no counterpart in the reference. It allocates nothing:
+ * its scratch is a fixed library-owned device array of 8 MiB + 256 B, held by
+ * every GPU that loads the library until the process exits, so `rows` may be
+ * at most GBFEM_NOALLOC_MAX_ROWS; larger calls are rejected with
+ * GBFEM_EINVAL. The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress), so make it before any stream capture. It
+ * synchronizes `stream` to report invalid input (out-of-range or repeated
+ * DOFs, a missing diagonal, a malformed pattern) before touching vals/rhs.
+ * All calls share the array and leave it cleared; calls whose GPU work
+ * overlaps (unordered streams) race on it. */
+#define GBFEM_NOALLOC_MAX_ROWS 2097152
+GBFEM_API int gbfem_prepare_forward_solve_noalloc(int num_bcs, const int* dofs,
+                                                  int rows, const int* row_ptr,
+                                                  const int* col_ind, double* vals,
+                                                  double* rhs, const double* bc_vals,
+                                                  void* stream);
+
 /* ---------------------------------------------------------------------------
  * CSR SpMV — replaces MatrixHandler<CudaCsrBackend>::matvec / matvecT
  * (femx/linalg/handler/MatrixHandler.hpp:270-317, MatrixHandler.cu:335-398,
