@@ -1,0 +1,153 @@
+"""Residual VJPs as the adjoint drivers use them.
+
+* torch.autograd.Function backward == explicit VJP kernels;
+* directional derivatives of the residual against central finite
+  differences (h = 1e-6) over 32 seeded directions in the control m and the
+  state u — the accuracy gate is 1e-6 relative;
+* the reduced gradient of J(m) = 0.5 |u(m) - d|^2 against femx's own
+  ReducedFunctional (femx/inverse/ReducedFunctional.hpp:94-117) run on the
+  reference library with DenseLinearSolver (tests/golden/inverse_12.npz).
+  Linear solves here use scipy on the host: they are test infrastructure,
+  the assembly, Dirichlet rows and VJPs run on the GPU.
+"""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+from conftest import load_golden, rel_inf  # noqa: E402
+from femx_gb300 import assembly as A  # noqa: E402
+from femx_gb300 import meshes  # noqa: E402
+from femx_gb300.autograd import p1_kappa_residual  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from femx_gb300 import build
+    build.build()
+
+
+def dev(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    return (t if dtype is None else t.to(dtype)).cuda()
+
+
+def setup(nx, seed, jitter=True):
+    coords, conn = meshes.jittered_tri(nx, seed=seed) if jitter else meshes.structured_tri(nx)
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    n, e = coords.shape[0], conn.shape[0]
+    amap = A.makeAssemblyMap(n, n, dev(offs), dev(dofs), dev(offs), dev(dofs))
+    bdofs = meshes.dirichlet_dofs(coords, meshes.boundary_nodes(coords))
+    bc = A.makeBoundaryMap(dev(bdofs), amap.pattern())
+    return coords, conn, amap, bc, bdofs
+
+
+def residual_np(amap, coords_d, m, u, f_d, bc, g):
+    return p1_kappa_residual(u, m, amap, coords_d, f_d, bc, g).detach()
+
+
+def test_autograd_backward_equals_vjp_kernels():
+    coords, conn, amap, bc, bdofs = setup(20, 1)
+    rng = np.random.default_rng(1)
+    n, e = coords.shape[0], conn.shape[0]
+    u = dev(rng.standard_normal(n)).requires_grad_()
+    m = dev(0.5 * rng.standard_normal(e)).requires_grad_()
+    lam = dev(rng.standard_normal(n))
+    g = dev(rng.standard_normal(len(bdofs)))
+    r = p1_kappa_residual(u, m, amap, dev(coords), dev(meshes.fourier_source(coords, 2)), bc, g)
+    (r * lam).sum().backward()
+    lam_t = lam.clone()
+    lam_t[dev(bdofs).long()] = 0.0
+    gu = torch.zeros(n, dtype=torch.float64, device="cuda")
+    gm = torch.zeros(e, dtype=torch.float64, device="cuda")
+    A.vjpP1Kappa(amap, dev(coords), torch.exp(m.detach()), u.detach(), lam_t, gu, gm)
+    gu[dev(bdofs).long()] += lam[dev(bdofs).long()]
+    assert torch.equal(u.grad, gu)
+    assert torch.equal(m.grad, gm)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-6), ("fp32_quad", 1e-4)])
+def test_vjp_matches_central_differences_32_directions(precision, tol):
+    coords, conn, amap, bc, bdofs = setup(64, 4)
+    rng = np.random.default_rng(4)
+    n, e = coords.shape[0], conn.shape[0]
+    coords_d = dev(coords)
+    f_d = dev(meshes.fourier_source(coords, 1))
+    m0 = dev(meshes.grf_centroids(coords, conn, seed=4, ell=0.05, grid=128))
+    u0 = dev(rng.standard_normal(n))
+    g = dev(np.zeros(len(bdofs)))
+    lam = dev(rng.standard_normal(n))
+    u = u0.clone().requires_grad_()
+    m = m0.clone().requires_grad_()
+    r = p1_kappa_residual(u, m, amap, coords_d, f_d, bc, g, precision=precision)
+    (r * lam).sum().backward()
+    h = 1e-6
+    errs = []
+    for k in range(32):
+        dm = dev(rng.standard_normal(e))
+        dm /= dm.norm()
+        rp = residual_np(amap, coords_d, m0 + h * dm, u0, f_d, bc, g)
+        rm = residual_np(amap, coords_d, m0 - h * dm, u0, f_d, bc, g)
+        fd = float(((rp - rm) * lam).sum()) / (2 * h)
+        an = float((m.grad * dm).sum())
+        errs.append(abs(fd - an) / max(abs(fd), 1e-30))
+        du = dev(rng.standard_normal(n))
+        du /= du.norm()
+        rp = residual_np(amap, coords_d, m0, u0 + h * du, f_d, bc, g)
+        rm = residual_np(amap, coords_d, m0, u0 - h * du, f_d, bc, g)
+        fd = float(((rp - rm) * lam).sum()) / (2 * h)
+        an = float((u.grad * du).sum())
+        errs.append(abs(fd - an) / max(abs(fd), 1e-30))
+    assert max(errs) <= tol, max(errs)
+
+
+def test_gradcheck_small():
+    coords, conn, amap, bc, bdofs = setup(5, 2)
+    rng = np.random.default_rng(2)
+    n, e = coords.shape[0], conn.shape[0]
+    u = dev(rng.standard_normal(n)).requires_grad_()
+    m = dev(0.3 * rng.standard_normal(e)).requires_grad_()
+    coords_d, f_d = dev(coords), dev(meshes.fourier_source(coords, 3))
+    g = dev(rng.standard_normal(len(bdofs)))
+    assert torch.autograd.gradcheck(
+        lambda uu, mm: p1_kappa_residual(uu, mm, amap, coords_d, f_d, bc, g), (u, m),
+        eps=1e-6, atol=1e-8, rtol=1e-6)
+
+
+def test_reduced_gradient_matches_femx_reduced_functional():
+    import scipy.sparse.linalg as spla
+    gd = load_golden("inverse_12")
+    coords, conn = gd["coords"], gd["conn"]
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    n, e = coords.shape[0], conn.shape[0]
+    amap = A.makeAssemblyMap(n, n, dev(offs), dev(dofs), dev(offs), dev(dofs))
+    bdofs = meshes.dirichlet_dofs(coords, meshes.boundary_nodes(coords))
+    bc = A.makeBoundaryMap(dev(bdofs), amap.pattern())
+    coords_d, f_d = dev(coords), dev(gd["f"])
+    m = dev(gd["m"])
+    g = dev(np.zeros(len(bdofs)))
+    zero = torch.zeros(n, dtype=torch.float64, device="cuda")
+    # LinearStateSolver (femx/state/StateSolver.hpp:90-108): rhs = -R(0),
+    # J = dR/du with constrained rows replaced, solve.
+    r0 = p1_kappa_residual(zero, m, amap, coords_d, f_d, bc, g).detach()
+    jac = A.CsrMatrix(amap.pattern())
+    res = torch.empty(n, dtype=torch.float64, device="cuda")
+    A.assembleP1Kappa(amap, coords_d, torch.exp(m), f_d, zero, res, jac)
+    A.replaceRows(bc, jac, 1.0)
+    J = jac.to_scipy()
+    u = spla.spsolve(J.tocsc(), -r0.cpu().numpy())
+    assert rel_inf(u, gd["u"]) <= 1e-10
+    value = 0.5 * float(np.sum((u - gd["d"]) ** 2))
+    assert abs(value - float(gd["value"][0])) <= 1e-10 * abs(float(gd["value"][0]))
+    # adjoint: J^T lam = dJ/du; grad = dJ/dm - (dR/dm)^T lam
+    lam = spla.spsolve(J.T.tocsc(), u - gd["d"])
+    u_t = dev(u).requires_grad_()
+    m_t = m.clone().requires_grad_()
+    r = p1_kappa_residual(u_t, m_t, amap, coords_d, f_d, bc, g)
+    (r * dev(lam)).sum().backward()
+    grad = -m_t.grad.cpu().numpy()
+    assert rel_inf(grad, gd["grad"]) <= 1e-9
