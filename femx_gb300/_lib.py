@@ -54,6 +54,19 @@ class BoundaryMapView(C.Structure):
     ]
 
 
+class BatchInstance(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("map", C.c_void_p), ("num_nodes", C.c_int),
+        ("coords", C.c_void_p), ("conn", C.c_void_p), ("kappa", C.c_void_p),
+        ("f_nodal", C.c_void_p), ("nu", C.c_double), ("state", C.c_void_p),
+        ("lam", C.c_void_p), ("res", C.c_void_p), ("vals", C.c_void_p),
+        ("g_state", C.c_void_p), ("g_control", C.c_void_p),
+    ]
+
+
+BATCH_P1_KAPPA = 1
+BATCH_TH_NS = 2
+
 _vp = C.c_void_p
 _i = C.c_int
 _d = C.c_double
@@ -82,6 +95,11 @@ SIGNATURES = {
     "gbfem_vjp_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
     "gbfem_probe_fp64_fma": (_i, [_i, _i, _i, _vp, _vp]),
+    "gbfem_batch_create": (_i, [_i, C.POINTER(BatchInstance), _vp, C.POINTER(_vp)]),
+    "gbfem_batch_run": (_i, [_vp, _i, _i, _i, _i, _vp]),
+    "gbfem_batch_check": (_i, [_vp, _vp]),
+    "gbfem_batch_num_elems": (C.c_longlong, [_vp]),
+    "gbfem_batch_destroy": (None, [_vp]),
     "gbfem_probe_convert": (_i, [_i, _vp, _vp, _vp, _vp]),
 }
 

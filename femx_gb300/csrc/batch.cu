@@ -1,0 +1,434 @@
+// batch.cu — many assembly instances of uneven size in one persistent launch.
+//
+// Each instance is one femx-style assemble (+ residual VJP) call: a
+// kappa-weighted P1 Poisson or a Taylor-Hood P2/P1 Navier-Stokes Newton
+// assembly on its own mesh and AssemblyMap. gbfem_batch_run enqueues exactly
+// two kernels, so the whole batch can be captured once in a CUDA graph and
+// replayed:
+//   1. zeroSegments — zeroes every instance's residual, matrix values and
+//      state-gradient (the outputs accumulated by FP64 reductions) and
+//      resets the work ticket;
+//   2. batchKernel  — a persistent grid (blocks_per_sm x SM count blocks of
+//      128 threads). Blocks draw work items from one atomic ticket counter
+//      (no block ever waits on another); an item is a chunk of consecutive
+//      elements of one instance. P1 items run one element per thread, with
+//      residual, Jacobian scatter and VJP (K lam, lam^T K u) fused on one
+//      evaluation of the element stiffness; Taylor-Hood items run 16-lane
+//      element groups with the row-coalesced scatter and the fused state VJP
+//      J^T lam (a reduction over the element's rows).
+// The item decode (instance prefix of chunk counts) is built by every block
+// in shared memory from the descriptor table at kernel start.
+#include <vector>
+
+#include "p1_elem.cuh"
+#include "th_elem.cuh"
+
+namespace
+{
+
+constexpr int kBatchThreads = 128;
+constexpr int kMaxInstances = 1024;
+constexpr int kZeroTile     = 8192; // doubles zeroed per block
+
+static_assert(kBatchThreads == kThreads, "Taylor-Hood block shape");
+
+struct BatchDesc
+{
+  int    kind;
+  int    num_elems;
+  P1Args p1;
+  ThArgs th;
+};
+
+struct ZeroSeg
+{
+  double*   ptr;
+  long long n;
+};
+
+__global__ void zeroSegments(const ZeroSeg* __restrict__ segs,
+                             const long long* __restrict__ block_prefix, int nseg,
+                             int* __restrict__ ticket)
+{
+  __shared__ int seg;
+  if (threadIdx.x == 0)
+  {
+    if (blockIdx.x == 0)
+    {
+      *ticket = 0;
+    }
+    int lo = 0, hi = nseg;
+    while (hi - lo > 1)
+    {
+      const int mid = (lo + hi) >> 1;
+      if (block_prefix[mid] <= blockIdx.x)
+      {
+        lo = mid;
+      }
+      else
+      {
+        hi = mid;
+      }
+    }
+    seg = lo;
+  }
+  __syncthreads();
+  const ZeroSeg   s    = segs[seg];
+  const long long base = (static_cast<long long>(blockIdx.x) - block_prefix[seg]) * kZeroTile;
+  const long long end  = base + kZeroTile < s.n ? base + kZeroTile : s.n;
+  for (long long i = base + threadIdx.x; i < end; i += blockDim.x)
+  {
+    s.ptr[i] = 0.0;
+  }
+}
+
+__device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th_chunk)
+{
+  const int c = d.kind == GBFEM_BATCH_P1_KAPPA ? p1_chunk : th_chunk;
+  return (d.num_elems + c - 1) / c;
+}
+
+template <class T, bool kSep, bool kLoad, bool kVjp>
+__device__ __forceinline__ void p1Chunk(const P1Args& a, int e0, int e1)
+{
+  for (int e = e0 + static_cast<int>(threadIdx.x); e < e1; e += kBatchThreads)
+  {
+    p1Element<std::is_same<T, float>::value, kSep, kLoad, true, true, kVjp>(a, e);
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(kBatchThreads)
+    batchKernel(const BatchDesc* __restrict__ descs, int ni, int p1_chunk, int th_chunk,
+                int* __restrict__ ticket)
+{
+  __shared__ ThSmem<T> sm;
+  __shared__ int       prefix[kMaxInstances + 1];
+  __shared__ int       item;
+  thStageRef(sm);
+  if (threadIdx.x == 0)
+  {
+    int acc = 0;
+    for (int i = 0; i < ni; ++i)
+    {
+      prefix[i] = acc;
+      acc += chunksOf(descs[i], p1_chunk, th_chunk);
+    }
+    prefix[ni] = acc;
+  }
+  __syncthreads();
+  const int total = prefix[ni];
+  for (;;)
+  {
+    if (threadIdx.x == 0)
+    {
+      item = atomicAdd(ticket, 1);
+    }
+    __syncthreads();
+    const int it = item;
+    if (it >= total)
+    {
+      break;
+    }
+    int lo = 0, hi = ni;
+    while (hi - lo > 1)
+    {
+      const int mid = (lo + hi) >> 1;
+      if (prefix[mid] <= it)
+      {
+        lo = mid;
+      }
+      else
+      {
+        hi = mid;
+      }
+    }
+    const BatchDesc& d = descs[lo];
+    const int        c = it - prefix[lo];
+    if (d.kind == GBFEM_BATCH_P1_KAPPA)
+    {
+      const int e0 = c * p1_chunk;
+      const int e1 = min(d.num_elems, e0 + p1_chunk);
+      const bool sep = d.p1.conn != nullptr, load = d.p1.f != nullptr;
+      const bool vjp = d.p1.lam != nullptr;
+      if (sep)
+      {
+        if (load)
+        {
+          vjp ? p1Chunk<T, true, true, true>(d.p1, e0, e1)
+              : p1Chunk<T, true, true, false>(d.p1, e0, e1);
+        }
+        else
+        {
+          vjp ? p1Chunk<T, true, false, true>(d.p1, e0, e1)
+              : p1Chunk<T, true, false, false>(d.p1, e0, e1);
+        }
+      }
+      else
+      {
+        if (load)
+        {
+          vjp ? p1Chunk<T, false, true, true>(d.p1, e0, e1)
+              : p1Chunk<T, false, true, false>(d.p1, e0, e1);
+        }
+        else
+        {
+          vjp ? p1Chunk<T, false, false, true>(d.p1, e0, e1)
+              : p1Chunk<T, false, false, false>(d.p1, e0, e1);
+        }
+      }
+    }
+    else
+    {
+      const int e0 = c * th_chunk;
+      const int e1 = min(d.num_elems, e0 + th_chunk);
+      for (int eb = e0; eb < e1; eb += kElemsPerBlock)
+      {
+        if (d.th.lam != nullptr)
+        {
+          thBlock<T, true, true, true>(d.th, eb, sm);
+        }
+        else
+        {
+          thBlock<T, true, true, false>(d.th, eb, sm);
+        }
+      }
+    }
+    __syncthreads(); // everyone has read `item` before it is overwritten
+  }
+}
+
+} // namespace
+
+struct gbfem_batch
+{
+  int                  num_instances = 0;
+  int                  sm_count      = 0;
+  BatchDesc*           d_descs       = nullptr;
+  ZeroSeg*             d_segs        = nullptr;
+  long long*           d_block_prefix = nullptr;
+  int                  nseg          = 0;
+  long long            zero_blocks   = 0;
+  int*                 d_ticket      = nullptr;
+  gbfem::DeviceStatus* d_status      = nullptr;
+  long long            total_elems   = 0;
+
+  ~gbfem_batch()
+  {
+    gbfem::deviceFree(d_descs);
+    gbfem::deviceFree(d_segs);
+    gbfem::deviceFree(d_block_prefix);
+    gbfem::deviceFree(d_ticket);
+    gbfem::deviceFree(d_status);
+  }
+};
+
+extern "C" int gbfem_batch_create(int n, const gbfem_batch_instance* inst, void* stream,
+                                  gbfem_batch** out)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(out != nullptr, "batch output handle is null");
+    *out = nullptr;
+    require(n > 0 && n <= kMaxInstances && inst != nullptr,
+            "batch instance count must be in 1..1024");
+    cudaStream_t s = asStream(stream);
+    auto*        b = new gbfem_batch;
+    try
+    {
+      int dev = 0;
+      cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+      cudaCheck(cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev),
+                "SM count");
+      b->num_instances = n;
+      b->d_status      = deviceAlloc<DeviceStatus>(1);
+      b->d_ticket      = deviceAlloc<int>(1);
+      cudaCheck(cudaMemsetAsync(b->d_status, 0, sizeof(DeviceStatus), s), "memset");
+      std::vector<BatchDesc> descs(n);
+      std::vector<ZeroSeg>   segs;
+      for (int i = 0; i < n; ++i)
+      {
+        const gbfem_batch_instance& x = inst[i];
+        const gbfem_assembly_map*   m = x.map;
+        require(m != nullptr && x.coords != nullptr && x.state != nullptr && x.res != nullptr,
+                "batch instance inputs must not be null");
+        require((reinterpret_cast<uintptr_t>(x.coords) & 15) == 0,
+                "Geometry coordinates must be 16-byte aligned");
+        require(m->num_res == m->num_states && m->same_dofs,
+                "batch instances need identical residual and state DOF tables");
+        BatchDesc& d = descs[i];
+        d            = BatchDesc{};
+        d.kind       = x.kind;
+        d.num_elems  = m->num_elems;
+        b->total_elems += m->num_elems;
+        if (x.kind == GBFEM_BATCH_P1_KAPPA)
+        {
+          require(m->num_elems == 0 || (m->uniform_res == 3 && m->uniform_state == 3),
+                  "KappaPoissonP1 expects three DOFs per element");
+          require(x.kappa != nullptr, "batch P1 instance needs kappa");
+          require(x.conn != nullptr || x.num_nodes == m->num_states,
+                  "Geometry and AssemblyMap have different node counts");
+          P1Args& a   = d.p1;
+          a.ne        = m->num_elems;
+          a.num_nodes = x.num_nodes;
+          a.dofs      = m->state_dofs;
+          a.conn      = x.conn;
+          a.coords    = reinterpret_cast<const double2*>(x.coords);
+          a.kappa     = x.kappa;
+          a.f         = x.f_nodal;
+          a.u         = x.state;
+          a.jac_map   = m->jac_map;
+          a.row_ptr   = m->row_ptr;
+          a.jac_pos   = m->pos_stride == 4 ? reinterpret_cast<const unsigned*>(m->jac_pos)
+                                           : nullptr;
+          a.res       = x.res;
+          a.vals      = x.vals;
+          a.lam       = x.lam;
+          a.g_u       = x.lam != nullptr ? x.g_state : nullptr;
+          a.g_m       = x.lam != nullptr ? x.g_control : nullptr;
+          a.status    = b->d_status;
+          require(x.vals != nullptr, "batch instance needs matrix values");
+        }
+        else if (x.kind == GBFEM_BATCH_TH_NS)
+        {
+          require(m->num_elems == 0 || (m->uniform_res == 15 && m->uniform_state == 15),
+                  "Taylor-Hood element expects 15 DOFs per element");
+          require(x.conn != nullptr && x.vals != nullptr,
+                  "batch Taylor-Hood instance needs conn6 and matrix values");
+          require(x.lam == nullptr || x.g_state != nullptr,
+                  "batch Taylor-Hood VJP needs a state-gradient output");
+          ThArgs& a   = d.th;
+          a.ne        = m->num_elems;
+          a.num_nodes = x.num_nodes;
+          a.dofs      = m->state_dofs;
+          a.conn6     = x.conn;
+          a.coords    = reinterpret_cast<const double2*>(x.coords);
+          a.nu        = x.nu;
+          a.state     = x.state;
+          a.row_ptr   = m->row_ptr;
+          a.jac_pos   = m->pos_stride == 16 ? m->jac_pos : nullptr;
+          a.jac_map   = m->jac_map;
+          a.res       = x.res;
+          a.vals      = x.vals;
+          a.lam       = x.lam;
+          a.g_state   = x.g_state;
+          a.status    = b->d_status;
+        }
+        else
+        {
+          throw Error(GBFEM_EINVAL, "unknown batch instance kind");
+        }
+        segs.push_back({x.res, m->num_res});
+        segs.push_back({x.vals, m->nnz});
+        if (x.lam != nullptr && x.g_state != nullptr)
+        {
+          segs.push_back({x.g_state, m->num_states});
+        }
+      }
+      std::vector<ZeroSeg>   nonempty;
+      std::vector<long long> prefix;
+      long long              acc = 0;
+      for (const auto& z : segs)
+      {
+        if (z.n > 0)
+        {
+          nonempty.push_back(z);
+          prefix.push_back(acc);
+          acc += (z.n + kZeroTile - 1) / kZeroTile;
+        }
+      }
+      b->nseg        = static_cast<int>(nonempty.size());
+      b->zero_blocks = acc;
+      b->d_descs     = deviceAlloc<BatchDesc>(n);
+      b->d_segs      = deviceAlloc<ZeroSeg>(b->nseg);
+      b->d_block_prefix = deviceAlloc<long long>(b->nseg);
+      cudaCheck(cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(BatchDesc) * n,
+                                cudaMemcpyHostToDevice, s),
+                "batch descriptor upload");
+      if (b->nseg > 0)
+      {
+        cudaCheck(cudaMemcpyAsync(b->d_segs, nonempty.data(), sizeof(ZeroSeg) * b->nseg,
+                                  cudaMemcpyHostToDevice, s),
+                  "batch segment upload");
+        cudaCheck(cudaMemcpyAsync(b->d_block_prefix, prefix.data(),
+                                  sizeof(long long) * b->nseg, cudaMemcpyHostToDevice, s),
+                  "batch segment upload");
+      }
+      cudaCheck(cudaStreamSynchronize(s), "batch setup");
+    }
+    catch (...)
+    {
+      delete b;
+      throw;
+    }
+    *out = b;
+  });
+}
+
+extern "C" int gbfem_batch_run(gbfem_batch* b, int precision, int p1_chunk, int th_chunk,
+                               int blocks_per_sm, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(b != nullptr, "batch handle is null");
+    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD,
+            "batch precision must be FP64 or FP32_QUAD");
+    require(p1_chunk >= kBatchThreads && p1_chunk % kBatchThreads == 0,
+            "p1_chunk must be a positive multiple of 128");
+    require(th_chunk >= kElemsPerBlock && th_chunk % kElemsPerBlock == 0,
+            "th_chunk must be a positive multiple of 8");
+    require(blocks_per_sm >= 1 && blocks_per_sm <= 32, "blocks_per_sm must be in 1..32");
+    cudaStream_t s = asStream(stream);
+    if (b->zero_blocks > 0)
+    {
+      zeroSegments<<<static_cast<unsigned>(b->zero_blocks), 256, 0, s>>>(
+          b->d_segs, b->d_block_prefix, b->nseg, b->d_ticket);
+    }
+    else
+    {
+      cudaCheck(cudaMemsetAsync(b->d_ticket, 0, sizeof(int), s), "ticket reset");
+    }
+    cudaCheck(cudaGetLastError(), "batch zero launch");
+    const unsigned grid = static_cast<unsigned>(b->sm_count * blocks_per_sm);
+    if (precision == GBFEM_PREC_FP64)
+    {
+      batchKernel<double><<<grid, kBatchThreads, 0, s>>>(b->d_descs, b->num_instances,
+                                                         p1_chunk, th_chunk, b->d_ticket);
+    }
+    else
+    {
+      batchKernel<float><<<grid, kBatchThreads, 0, s>>>(b->d_descs, b->num_instances,
+                                                        p1_chunk, th_chunk, b->d_ticket);
+    }
+    cudaCheck(cudaGetLastError(), "batch launch");
+  });
+}
+
+extern "C" int gbfem_batch_check(const gbfem_batch* b, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(b != nullptr, "batch handle is null");
+    cudaStream_t s = asStream(stream);
+    try
+    {
+      checkDeviceStatus(b->d_status, s);
+    }
+    catch (...)
+    {
+      cudaMemsetAsync(b->d_status, 0, sizeof(DeviceStatus), s);
+      cudaStreamSynchronize(s);
+      throw;
+    }
+  });
+}
+
+extern "C" long long gbfem_batch_num_elems(const gbfem_batch* b)
+{
+  return b != nullptr ? b->total_elems : 0;
+}
+
+extern "C" void gbfem_batch_destroy(gbfem_batch* b)
+{
+  delete b;
+}

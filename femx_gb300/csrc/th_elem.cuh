@@ -1,0 +1,514 @@
+// th_elem.cuh — device code of the Taylor-Hood P2/P1 element, shared by the
+// standalone assembly kernel (th.cu) and the batched persistent kernel
+// (batch.cu). See th.cu for the formulation.
+#pragma once
+
+#include <type_traits>
+
+#include "maps.cuh"
+
+namespace
+{
+using gbfem::DeviceStatus;
+
+constexpr int kLanes         = 16;
+constexpr int kElemsPerBlock = 8;
+constexpr int kThreads       = kLanes * kElemsPerBlock;
+constexpr int kNq            = 6;
+
+template <class R>
+struct ThRef
+{
+  R N[kNq][6];       // P2 values at the quadrature points
+  R wN[kNq][6];      // w_q N^_a(q)
+  R dNr[kNq][6][2];  // P2 reference gradients at the quadrature points
+  R S00[6][6], S11[6][6], S01[6][6]; // S^00, S^11, S^01 + S^10
+  R T[3][6][6];      // sum_q w N^_a N^_b lambda_v
+  R C[2][6][3];      // sum_q w psi^_b dN^_a,k
+  R dNv[3][6][2];    // P2 reference gradients at the vertices
+  R w[kNq];
+};
+
+constexpr void p2Eval(double r, double s, double* N, double* dN)
+{
+  const double l0 = 1.0 - r - s, l1 = r, l2 = s;
+  const double g0[2] = {-1.0, -1.0}, g1[2] = {1.0, 0.0}, g2[2] = {0.0, 1.0};
+  N[0] = l0 * (2.0 * l0 - 1.0);
+  N[1] = l1 * (2.0 * l1 - 1.0);
+  N[2] = l2 * (2.0 * l2 - 1.0);
+  N[3] = 4.0 * l0 * l1;
+  N[4] = 4.0 * l1 * l2;
+  N[5] = 4.0 * l2 * l0;
+  for (int d = 0; d < 2; ++d)
+  {
+    dN[0 * 2 + d] = (4.0 * l0 - 1.0) * g0[d];
+    dN[1 * 2 + d] = (4.0 * l1 - 1.0) * g1[d];
+    dN[2 * 2 + d] = (4.0 * l2 - 1.0) * g2[d];
+    dN[3 * 2 + d] = 4.0 * (l1 * g0[d] + l0 * g1[d]);
+    dN[4 * 2 + d] = 4.0 * (l2 * g1[d] + l1 * g2[d]);
+    dN[5 * 2 + d] = 4.0 * (l0 * g2[d] + l2 * g0[d]);
+  }
+}
+
+constexpr ThRef<double> makeRef()
+{
+  ThRef<double> t{};
+  const double  a1 = 0.445948490915964886, w1 = 0.223381589678011466 * 0.5;
+  const double  a2 = 0.091576213509770743, w2 = 0.109951743655321868 * 0.5;
+  const double  q[kNq][3] = {{a1, a1, w1}, {1.0 - 2.0 * a1, a1, w1},
+                            {a1, 1.0 - 2.0 * a1, w1}, {a2, a2, w2},
+                            {1.0 - 2.0 * a2, a2, w2}, {a2, 1.0 - 2.0 * a2, w2}};
+  const double  dP[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
+  double        lam[kNq][3]{};
+  for (int i = 0; i < kNq; ++i)
+  {
+    double N[6]{}, dN[12]{};
+    p2Eval(q[i][0], q[i][1], N, dN);
+    lam[i][0] = 1.0 - q[i][0] - q[i][1];
+    lam[i][1] = q[i][0];
+    lam[i][2] = q[i][1];
+    t.w[i]    = q[i][2];
+    for (int a = 0; a < 6; ++a)
+    {
+      t.N[i][a]      = N[a];
+      t.wN[i][a]     = q[i][2] * N[a];
+      t.dNr[i][a][0] = dN[2 * a];
+      t.dNr[i][a][1] = dN[2 * a + 1];
+    }
+  }
+  for (int a = 0; a < 6; ++a)
+  {
+    for (int b = 0; b < 6; ++b)
+    {
+      double s00 = 0.0, s11 = 0.0, s01 = 0.0;
+      double tv[3] = {0.0, 0.0, 0.0};
+      for (int i = 0; i < kNq; ++i)
+      {
+        const double w = t.w[i];
+        s00 += w * t.dNr[i][a][0] * t.dNr[i][b][0];
+        s11 += w * t.dNr[i][a][1] * t.dNr[i][b][1];
+        s01 += w * (t.dNr[i][a][0] * t.dNr[i][b][1] + t.dNr[i][a][1] * t.dNr[i][b][0]);
+        for (int v = 0; v < 3; ++v)
+        {
+          tv[v] += w * t.N[i][a] * t.N[i][b] * lam[i][v];
+        }
+      }
+      t.S00[a][b] = s00;
+      t.S11[a][b] = s11;
+      t.S01[a][b] = s01;
+      for (int v = 0; v < 3; ++v)
+      {
+        t.T[v][a][b] = tv[v];
+      }
+    }
+    for (int b = 0; b < 3; ++b)
+    {
+      for (int k = 0; k < 2; ++k)
+      {
+        double c = 0.0;
+        for (int i = 0; i < kNq; ++i)
+        {
+          c += t.w[i] * lam[i][b] * t.dNr[i][a][k];
+        }
+        t.C[k][a][b] = c;
+      }
+    }
+  }
+  const double vx[3][2] = {{0.0, 0.0}, {1.0, 0.0}, {0.0, 1.0}};
+  for (int v = 0; v < 3; ++v)
+  {
+    double N[6]{}, dN[12]{};
+    p2Eval(vx[v][0], vx[v][1], N, dN);
+    for (int s = 0; s < 6; ++s)
+    {
+      t.dNv[v][s][0] = dN[2 * s];
+      t.dNv[v][s][1] = dN[2 * s + 1];
+    }
+  }
+  (void)dP;
+  return t;
+}
+
+template <class R>
+constexpr ThRef<R> castRef()
+{
+  const ThRef<double> d = makeRef();
+  ThRef<R>            r{};
+  for (int q = 0; q < kNq; ++q)
+  {
+    r.w[q] = static_cast<R>(d.w[q]);
+    for (int a = 0; a < 6; ++a)
+    {
+      r.N[q][a]      = static_cast<R>(d.N[q][a]);
+      r.wN[q][a]     = static_cast<R>(d.wN[q][a]);
+      r.dNr[q][a][0] = static_cast<R>(d.dNr[q][a][0]);
+      r.dNr[q][a][1] = static_cast<R>(d.dNr[q][a][1]);
+    }
+  }
+  for (int a = 0; a < 6; ++a)
+  {
+    for (int b = 0; b < 6; ++b)
+    {
+      r.S00[a][b] = static_cast<R>(d.S00[a][b]);
+      r.S11[a][b] = static_cast<R>(d.S11[a][b]);
+      r.S01[a][b] = static_cast<R>(d.S01[a][b]);
+      for (int v = 0; v < 3; ++v)
+      {
+        r.T[v][a][b] = static_cast<R>(d.T[v][a][b]);
+      }
+    }
+    for (int b = 0; b < 3; ++b)
+    {
+      r.C[0][a][b] = static_cast<R>(d.C[0][a][b]);
+      r.C[1][a][b] = static_cast<R>(d.C[1][a][b]);
+    }
+  }
+  for (int v = 0; v < 3; ++v)
+  {
+    for (int s2 = 0; s2 < 6; ++s2)
+    {
+      r.dNv[v][s2][0] = static_cast<R>(d.dNv[v][s2][0]);
+      r.dNv[v][s2][1] = static_cast<R>(d.dNv[v][s2][1]);
+    }
+  }
+  return r;
+}
+
+__device__ const ThRef<double> kRefD = makeRef();
+__device__ const ThRef<float>  kRefF = castRef<float>();
+
+__device__ __forceinline__ const ThRef<double>* refTables(double)
+{
+  return &kRefD;
+}
+__device__ __forceinline__ const ThRef<float>* refTables(float)
+{
+  return &kRefF;
+}
+
+struct ThArgs
+{
+  int                  ne;
+  int                  num_nodes;
+  const int*           dofs;  // [ne][15]
+  const int*           conn6; // [ne][6]
+  const double2*       coords;
+  double               nu;
+  const double*        state;
+  const int*           row_ptr;
+  const unsigned char* jac_pos; // [ne][15][16] or null
+  const int*           jac_map; // fallback
+  double*              res;
+  double*              vals;
+  const double*        lam;     // adjoint for the fused state VJP, or null
+  double*              g_state; // J^T lam accumulated here when lam != null
+  DeviceStatus*        status;
+};
+
+template <class T>
+struct ElemShared
+{
+  T   st[16];
+  T   aInvJ[4];  // |det| * J^-1
+  T   invJ[4];
+  T   G3[3];     // nu |det| (J^-1 J^-T): 00, 11, 01
+  T   ut[kNq][2];
+  T   vq[kNq][6]; // |det| dN^_b(q) . ut_q
+  T   Gv[3][4];   // |det| grad u at the vertices, [v][c*2+e]
+  int ok;
+};
+
+// Shared memory of one 128-thread block working on up to 8 elements.
+template <class T>
+struct ThSmem
+{
+  ThRef<T>      ref;
+  ElemShared<T> sh[kElemsPerBlock];
+  // Row-major staging of each element's 15x15 block (values and CSR slots)
+  // so that the scatter issues one row per half-warp instruction: lanes then
+  // hit the same row segment and the L2 reductions coalesce.
+  T   outv[kElemsPerBlock][15][16];
+  int outk[kElemsPerBlock][15][16];
+  T   lam[kElemsPerBlock][16];
+};
+
+template <class T>
+__device__ __forceinline__ void thStageRef(ThSmem<T>& sm)
+{
+  const T* src = reinterpret_cast<const T*>(refTables(T()));
+  T*       dst = reinterpret_cast<T*>(&sm.ref);
+  for (int i = threadIdx.x; i < int(sizeof(ThRef<T>) / sizeof(T)); i += kThreads)
+  {
+    dst[i] = src[i];
+  }
+}
+
+// The whole block works on elements [e_base, e_base + 8). Call from every
+// thread of a kThreads-wide block after thStageRef + __syncthreads.
+template <class T, bool kJac, bool kRes, bool kVjp>
+__device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& sm)
+{
+  const ThRef<T>& ref = sm.ref;
+  const int       l   = threadIdx.x & (kLanes - 1);
+  const int       le  = threadIdx.x / kLanes;
+  const int       e   = e_base + le;
+  const bool      has = e < a.ne;
+  ElemShared<T>&  S   = sm.sh[le];
+
+  if (has && l < 15)
+  {
+    S.st[l] = gbfem::fromF64<T>(a.state[a.dofs[15 * e + l]]);
+    if (kVjp)
+    {
+      sm.lam[le][l] = gbfem::fromF64<T>(a.lam[a.dofs[15 * e + l]]);
+    }
+  }
+  if (has && l == 15)
+  {
+    bool nodes_ok = true;
+    for (int k = 0; k < 6; ++k)
+    {
+      nodes_ok = nodes_ok
+                 && static_cast<unsigned>(a.conn6[6 * e + k])
+                        < static_cast<unsigned>(a.num_nodes);
+    }
+    S.ok = 0;
+    if (!nodes_ok)
+    {
+      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+    }
+    else
+    {
+      const double2 x0 = a.coords[a.conn6[6 * e + 0]];
+      const double2 x1 = a.coords[a.conn6[6 * e + 1]];
+      const double2 x2 = a.coords[a.conn6[6 * e + 2]];
+      // J[a][b] = d x_a / d r_b of the affine map (vertex nodes); the edge
+      // vectors carry the mesh scale and are formed in FP64, the rest in T.
+      const T j00 = gbfem::fromF64<T>(x1.x - x0.x), j01 = gbfem::fromF64<T>(x2.x - x0.x);
+      const T j10 = gbfem::fromF64<T>(x1.y - x0.y), j11 = gbfem::fromF64<T>(x2.y - x0.y);
+      const T det = j00 * j11 - j01 * j10;
+      const T ad  = det < T(0) ? -det : det;
+      if (ad >= T(1.0e-30))
+      {
+        S.ok        = 1;
+        const T inv = T(1) / det;
+        const T i00 = j11 * inv, i01 = -j01 * inv;
+        const T i10 = -j10 * inv, i11 = j00 * inv;
+        S.invJ[0]   = i00;
+        S.invJ[1]   = i01;
+        S.invJ[2]   = i10;
+        S.invJ[3]   = i11;
+        S.aInvJ[0]  = ad * i00;
+        S.aInvJ[1]  = ad * i01;
+        S.aInvJ[2]  = ad * i10;
+        S.aInvJ[3]  = ad * i11;
+        const T nad = T(a.nu) * ad;
+        S.G3[0]     = nad * (i00 * i00 + i01 * i01);
+        S.G3[1]     = nad * (i10 * i10 + i11 * i11);
+        S.G3[2]     = nad * (i00 * i10 + i01 * i11);
+      }
+      else
+      {
+        gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+      }
+    }
+  }
+  __syncthreads();
+  const bool live = has && S.ok;
+  if (live && l < 12)
+  {
+    // |det| grad u at vertex v: [c][e] = sum_k aInvJ[k][e] sum_s u_(s,c) dNv
+    const int v = l >> 2, c = (l >> 1) & 1, ee = l & 1;
+    T         g0 = 0, g1 = 0;
+#pragma unroll
+    for (int s2 = 0; s2 < 6; ++s2)
+    {
+      const T us = S.st[2 * s2 + c];
+      g0 += us * ref.dNv[v][s2][0];
+      g1 += us * ref.dNv[v][s2][1];
+    }
+    S.Gv[v][c * 2 + ee] = g0 * S.aInvJ[0 * 2 + ee] + g1 * S.aInvJ[1 * 2 + ee];
+  }
+  if (live && l < kNq)
+  {
+    const int q  = l;
+    T         u0 = 0, u1 = 0;
+#pragma unroll
+    for (int s2 = 0; s2 < 6; ++s2)
+    {
+      u0 += ref.N[q][s2] * S.st[2 * s2];
+      u1 += ref.N[q][s2] * S.st[2 * s2 + 1];
+    }
+    // ut_k = sum_d Jinv[k][d] u_d, so that u . dN_b = dN^_b . ut
+    S.ut[q][0] = S.aInvJ[0] * u0 + S.aInvJ[1] * u1;
+    S.ut[q][1] = S.aInvJ[2] * u0 + S.aInvJ[3] * u1;
+  }
+  __syncthreads();
+  if (live)
+  {
+    for (int i = l; i < kNq * 6; i += kLanes)
+    {
+      const int q = i / 6, b = i % 6;
+      S.vq[q][b]  = ref.dNr[q][b][0] * S.ut[q][0] + ref.dNr[q][b][1] * S.ut[q][1];
+    }
+  }
+  __syncthreads();
+  const bool row_lane = live && l < 15;
+
+  // Row l: velocity (sa, c) for l < 12, pressure b = l - 12 otherwise.
+  // jcc[b] -> column (b, c), jco[b] -> (b, 1-c), jp[b] -> pressure b;
+  // for pressure rows jcc/jco hold the columns (b, 0) and (b, 1).
+  T   jcc[6], jco[6], jp[3] = {0, 0, 0};
+  T   r = 0;
+  int c = 0;
+  if (row_lane && l < 12)
+  {
+    const int sa = l >> 1;
+    c            = l & 1;
+    const int oc = c ^ 1;
+    const T   Gcc[3] = {S.Gv[0][c * 2 + c], S.Gv[1][c * 2 + c], S.Gv[2][c * 2 + c]};
+    const T   Gco[3] = {S.Gv[0][c * 2 + oc], S.Gv[1][c * 2 + oc], S.Gv[2][c * 2 + oc]};
+#pragma unroll
+    for (int b = 0; b < 6; ++b)
+    {
+      T da = S.G3[0] * ref.S00[sa][b] + S.G3[1] * ref.S11[sa][b] + S.G3[2] * ref.S01[sa][b];
+#pragma unroll
+      for (int q = 0; q < kNq; ++q)
+      {
+        da += ref.wN[q][sa] * S.vq[q][b];
+      }
+      const T mcc = ref.T[0][sa][b] * Gcc[0] + ref.T[1][sa][b] * Gcc[1]
+                    + ref.T[2][sa][b] * Gcc[2];
+      const T mco = ref.T[0][sa][b] * Gco[0] + ref.T[1][sa][b] * Gco[1]
+                    + ref.T[2][sa][b] * Gco[2];
+      jcc[b] = da + mcc;
+      jco[b] = mco;
+      r += da * S.st[2 * b + c];
+    }
+    const T ic0 = S.aInvJ[0 * 2 + c], ic1 = S.aInvJ[1 * 2 + c];
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+    {
+      jp[b] = -(ic0 * ref.C[0][sa][b] + ic1 * ref.C[1][sa][b]);
+      r += jp[b] * S.st[12 + b];
+    }
+  }
+  else if (row_lane)
+  {
+    const int b = l - 12;
+#pragma unroll
+    for (int sa = 0; sa < 6; ++sa)
+    {
+      const T c0 = ref.C[0][sa][b], c1 = ref.C[1][sa][b];
+      jcc[sa]    = -(S.aInvJ[0] * c0 + S.aInvJ[2] * c1);
+      jco[sa]    = -(S.aInvJ[1] * c0 + S.aInvJ[3] * c1);
+      r += jcc[sa] * S.st[2 * sa] + jco[sa] * S.st[2 * sa + 1];
+    }
+  }
+  if (row_lane)
+  {
+    const int row_dof = a.dofs[15 * e + l];
+    if (kRes)
+    {
+      gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
+    }
+    if (kJac)
+    {
+      const int rs = a.row_ptr[row_dof];
+      int       col[15];
+      if (a.jac_pos != nullptr)
+      {
+        const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
+        const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int j = 0; j < 15; ++j)
+        {
+          col[j] = rs + int((wd[j >> 2] >> (8 * (j & 3))) & 0xffu);
+        }
+      }
+      else
+      {
+        const int* jm = a.jac_map + 225LL * e + 15 * l;
+#pragma unroll
+        for (int j = 0; j < 15; ++j)
+        {
+          col[j] = jm[j];
+        }
+      }
+      T*   ov = sm.outv[le][l];
+      int* ok = sm.outk[le][l];
+      if (l < 12)
+      {
+#pragma unroll
+        for (int b = 0; b < 6; ++b)
+        {
+          // local columns 2b (component 0) and 2b + 1 (component 1)
+          ov[2 * b + c]       = jcc[b];
+          ov[2 * b + (c ^ 1)] = jco[b];
+        }
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+        {
+          ov[12 + b] = jp[b];
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int sa = 0; sa < 6; ++sa)
+        {
+          ov[2 * sa]     = jcc[sa];
+          ov[2 * sa + 1] = jco[sa];
+        }
+        // the pressure-pressure block is structurally present and zero
+        ov[12] = ov[13] = ov[14] = T(0);
+      }
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        ok[j] = col[j];
+      }
+    }
+  }
+  if (kJac)
+  {
+    __syncwarp();
+    if (live && l < 15)
+    {
+      // lane l now owns local column l of every row of its element
+#pragma unroll 5
+      for (int row = 0; row < 15; ++row)
+      {
+        const double v = gbfem::toF64(sm.outv[le][row][l]);
+        if (row < 12 || l < 12)
+        {
+          gbfem::redAdd(a.vals + sm.outk[le][row][l], v);
+        }
+      }
+      if (kVjp)
+      {
+        // fused state VJP: (J_e^T lam_e)_l, a reduction over the rows
+        T acc = 0;
+#pragma unroll
+        for (int row = 0; row < 15; ++row)
+        {
+          acc += sm.outv[le][row][l] * sm.lam[le][row];
+        }
+        gbfem::redAdd(a.g_state + a.dofs[15 * e + l], gbfem::toF64(acc));
+      }
+    }
+  }
+  __syncthreads(); // the block's shared staging is reused by the next call
+}
+
+template <class T, bool kJac, bool kRes>
+__global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
+{
+  __shared__ ThSmem<T> sm;
+  thStageRef(sm);
+  __syncthreads();
+  thBlock<T, kJac, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+} // namespace
+

@@ -204,6 +204,55 @@ GBFEM_API int gbfem_assemble_th_ns(const gbfem_assembly_map* map, int num_p2_nod
                          const double* state, double* res, double* vals,
                          int precision, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched assembly: many independent instances (meshes of uneven size, P1
+ * Poisson and Taylor-Hood NS mixed) assembled by one persistent launch.
+ * Each instance is the work of one gbfem_assemble_p1_kappa /
+ * gbfem_assemble_th_ns call (femx's assembly::assemble per instance,
+ * CudaAssembly.hpp:319-364) plus, when `lam` is given, the residual VJPs:
+ * P1: g_state = K^T lam, g_control[e] = lam_e^T K_e u_e (gbfem_vjp_p1_kappa);
+ * Taylor-Hood: g_state = J^T lam of the assembled Jacobian. femx has no
+ * batched entry; this replaces a loop of per-instance calls.
+ * gbfem_batch_run enqueues two kernels (zero outputs, persistent assembly),
+ * allocates nothing and does not synchronize.
+ * ------------------------------------------------------------------------ */
+#define GBFEM_BATCH_P1_KAPPA 1
+#define GBFEM_BATCH_TH_NS 2
+
+typedef struct
+{
+  int                       kind; /* GBFEM_BATCH_P1_KAPPA or GBFEM_BATCH_TH_NS */
+  const gbfem_assembly_map* map;
+  int                       num_nodes;
+  const double*             coords;  /* [num_nodes][2], 16-byte aligned */
+  const int*                conn;    /* P1: [E][3] or NULL; Taylor-Hood: conn6 */
+  const double*             kappa;   /* P1 */
+  const double*             f_nodal; /* P1, may be NULL */
+  double                    nu;      /* Taylor-Hood */
+  const double*             state;
+  const double*             lam;       /* adjoint; NULL skips the VJP */
+  double*                   res;       /* [num_res] */
+  double*                   vals;      /* [nnz] */
+  double*                   g_state;   /* [num_states] */
+  double*                   g_control; /* P1: [num_elems] */
+} gbfem_batch_instance;
+
+typedef struct gbfem_batch gbfem_batch;
+
+GBFEM_API int       gbfem_batch_create(int num_instances,
+                                       const gbfem_batch_instance* instances,
+                                       void* stream, gbfem_batch** out);
+/* precision: GBFEM_PREC_FP64 or GBFEM_PREC_FP32_QUAD. Work items are
+ * p1_chunk P1 elements (multiple of 128) or th_chunk Taylor-Hood elements
+ * (multiple of 8); the grid is blocks_per_sm x SM count. */
+GBFEM_API int       gbfem_batch_run(gbfem_batch* batch, int precision, int p1_chunk,
+                                    int th_chunk, int blocks_per_sm, void* stream);
+/* Reads and clears the batch's device status word (degenerate elements,
+ * out-of-range connectivity). Synchronizes `stream`. */
+GBFEM_API int       gbfem_batch_check(const gbfem_batch* batch, void* stream);
+GBFEM_API long long gbfem_batch_num_elems(const gbfem_batch* batch);
+GBFEM_API void      gbfem_batch_destroy(gbfem_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

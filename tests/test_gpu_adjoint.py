@@ -66,11 +66,15 @@ def test_autograd_backward_equals_vjp_kernels():
     gm = torch.zeros(e, dtype=torch.float64, device="cuda")
     A.vjpP1Kappa(amap, dev(coords), torch.exp(m.detach()), u.detach(), lam_t, gu, gm)
     gu[dev(bdofs).long()] += lam[dev(bdofs).long()]
-    assert torch.equal(u.grad, gu)
-    assert torch.equal(m.grad, gm)
+    # FP64 reductions at L2 sum in a run-dependent order: equal to rounding
+    assert rel_inf(u.grad.cpu().numpy(), gu.cpu().numpy()) <= 1e-14
+    assert rel_inf(m.grad.cpu().numpy(), gm.cpu().numpy()) <= 1e-14
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-6), ("fp32_quad", 1e-4)])
+# MIXED keeps the gradient in FP64 (the VJP kernels run FP64 element math);
+# FP32_QUAD carries ~1e-7 per element, which cancellation in a directional
+# derivative over many elements amplifies, hence its looser gate.
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-6), ("mixed", 1e-6), ("fp32_quad", 1e-4)])
 def test_vjp_matches_central_differences_32_directions(precision, tol):
     coords, conn, amap, bc, bdofs = setup(64, 4)
     rng = np.random.default_rng(4)
@@ -115,7 +119,7 @@ def test_gradcheck_small():
     g = dev(rng.standard_normal(len(bdofs)))
     assert torch.autograd.gradcheck(
         lambda uu, mm: p1_kappa_residual(uu, mm, amap, coords_d, f_d, bc, g), (u, m),
-        eps=1e-6, atol=1e-8, rtol=1e-6)
+        eps=1e-6, atol=1e-8, rtol=1e-6, nondet_tol=1e-12)
 
 
 def test_reduced_gradient_matches_femx_reduced_functional():
