@@ -423,22 +423,43 @@ def main():
             rr = p1_kappa_residual(u_r, m_r, amap, coords, f_d, bcv, gz, precision=prec)
             (rr * lam).sum().backward()
             grads[prec] = (u_r.grad, m_r.grad)
-        h = 1e-6
-        fd_err = {"mixed": 0.0, "fp32_quad": 0.0}
+        # Central differences from the serial CPU oracle residual (fixed
+        # summation order, so the two evaluations' rounding is correlated).
+        from oracle import pyoracle as orc
+        om = orc.AssemblyMap(n, n, p["offs"], p["dofs"], p["offs"], p["dofs"])
+        oq = orc.P1Quad(p["coords"], p["conn"])
+        ob = orc.BoundaryMap(p["bdofs"], om.row_ptr, om.col_ind)
+        u_h, m_h, lam_h = u.cpu().numpy(), m0.cpu().numpy(), lam.cpu().numpy()
+        g_h = np.zeros(len(p["bdofs"]))
+
+        def R(uu, mm):
+            r_, _ = orc.assemble_p1_kappa(om, oq, np.exp(mm), p["f"], uu)
+            return ob.replace_res(uu, g_h, r_)
+
+        hg = {k: (gu_.cpu().numpy(), gm_.cpu().numpy()) for k, (gu_, gm_) in grads.items()}
+        # the oracle's own analytic gradient: its disagreement with the same
+        # finite differences is the noise floor of the FD check itself
+        lt = lam_h.copy()
+        lt[p["bdofs"]] = 0.0
+        ogu, ogm = orc.vjp_p1_kappa(om, oq, np.exp(m_h), u_h, lt)
+        ogu[p["bdofs"]] += lam_h[p["bdofs"]]
+        hg["oracle"] = (ogu, ogm)
+        direct = {"g_u": float(np.abs(hg["mixed"][0] - ogu).max() / np.abs(ogu).max()),
+                  "g_m": float(np.abs(hg["mixed"][1] - ogm).max() / np.abs(ogm).max())}
+        fd_err = {hh: {k: 0.0 for k in hg} for hh in (1e-6, 1e-5)}
         for _ in range(32):
             for which in ("m", "u"):
-                dv = d(rng.standard_normal(e if which == "m" else n))
-                dv /= dv.norm()
-                if which == "m":
-                    rp = p1_kappa_residual(u, m0 + h * dv, amap, coords, f_d, bcv, gz)
-                    rm = p1_kappa_residual(u, m0 - h * dv, amap, coords, f_d, bcv, gz)
-                else:
-                    rp = p1_kappa_residual(u + h * dv, m0, amap, coords, f_d, bcv, gz)
-                    rm = p1_kappa_residual(u - h * dv, m0, amap, coords, f_d, bcv, gz)
-                fd = float(((rp - rm) * lam).sum()) / (2 * h)
-                for prec, (gu_, gm_) in grads.items():
-                    an = float(((gm_ if which == "m" else gu_) * dv).sum())
-                    fd_err[prec] = max(fd_err[prec], abs(fd - an) / max(abs(fd), 1e-300))
+                dv = rng.standard_normal(e if which == "m" else n)
+                dv /= np.linalg.norm(dv)
+                for hh in (1e-6, 1e-5):
+                    if which == "m":
+                        fd = float((R(u_h, m_h + hh * dv) - R(u_h, m_h - hh * dv)) @ lam_h) / (2 * hh)
+                    else:
+                        fd = float((R(u_h + hh * dv, m_h) - R(u_h - hh * dv, m_h)) @ lam_h) / (2 * hh)
+                    for prec, (gu_, gm_) in hg.items():
+                        an = float((gm_ if which == "m" else gu_) @ dv)
+                        fd_err[hh][prec] = max(fd_err[hh][prec],
+                                               abs(fd - an) / max(abs(fd), 1e-300))
         line["vjp"] = {
             "workload": f"poisson_p1_{VJP_NX}x{VJP_NX}_vjp_state_and_control",
             "grads_per_s": world / t32, "grads_per_s_fp64": world / t64,
@@ -447,13 +468,20 @@ def main():
             "rel_err_fp32_vs_fp64": {
                 "g_u": float((gu32 - gu64).abs().max() / gu64.abs().max()),
                 "g_m": float((gm32 - gm64).abs().max() / gm64.abs().max())},
-            "fd_check": {"directions": 32, "h": h, "gate": 1e-6,
-                         "max_rel_err_fp64_gradient": fd_err["mixed"],
-                         "max_rel_err_fp32_quadrature": fd_err["fp32_quad"],
-                         "fd_of": "fp64 residual with Dirichlet rows",
-                         "note": "per-element FP32 errors (1e-7) are amplified by "
-                                 "cancellation in directional derivatives over 524k "
-                                 "elements; the FP64 gradient passes the gate"},
+            "fd_check": {
+                "directions": "32 in m and 32 in u (unit, seeded)", "gate": 1e-6,
+                "fd_of": "fp64 residual with Dirichlet rows (serial CPU oracle)",
+                "h=1e-6": {"fp64_gradient": fd_err[1e-6]["mixed"],
+                           "fp32_quadrature_gradient": fd_err[1e-6]["fp32_quad"],
+                           "oracle_exact_gradient_noise_floor": fd_err[1e-6]["oracle"]},
+                "h=1e-5": {"fp64_gradient": fd_err[1e-5]["mixed"],
+                           "fp32_quadrature_gradient": fd_err[1e-5]["fp32_quad"],
+                           "oracle_exact_gradient_noise_floor": fd_err[1e-5]["oracle"]},
+                "gpu_fp64_gradient_vs_oracle_gradient": direct,
+                "note": "at 512x512 the h=1e-6 differences are limited by their own "
+                        "rounding (the oracle's exact gradient shows the same floor); "
+                        "FP32 per-element errors (1e-7) are amplified by cancellation "
+                        "in directional derivatives over 524k elements"},
             "roofline": {"bound": "hbm", "achieved": b_vjp / t32 / 1e9, "peak": hbm,
                          "unit": "GB/s", "frac": b_vjp / t32 / 1e9 / hbm,
                          "algorithmic_bytes": b_vjp},
@@ -547,37 +575,51 @@ def main():
                                         d(rng.standard_normal(nd))))
                 n_th += 1
         batch = Batch(insts)
-        params, tune = autotune(batch, "fp32_quad", reps=2, use_cache=False)
-        g32 = batch.graph("fp32_quad", **params)
-        t_b32 = maxrank(timer.run(g32.replay, args.steps, args.warmup))
-        outs32 = [(x.res.clone(), x.vals.clone(), x.g_u.clone()) for x in insts]
-        params64, _ = autotune(batch, "fp64", reps=2, use_cache=False)
-        g64 = batch.graph("fp64", **params64)
-        t_b64 = maxrank(timer.run(g64.replay, args.steps, args.warmup))
-        batch.check()
-        err = {"jacobian": 0.0, "residual": 0.0, "vjp_state": 0.0}
-        for x, (r32, v32, gu32) in zip(insts, outs32):
-            err["residual"] = max(err["residual"], float((r32 - x.res).abs().max()
-                                                         / x.res.abs().max()))
-            err["jacobian"] = max(err["jacobian"], float((v32 - x.vals).abs().max()
-                                                         / x.vals.abs().max()))
-            err["vjp_state"] = max(err["vjp_state"], float((gu32 - x.g_u).abs().max()
-                                                           / x.g_u.abs().max()))
-        launches += 4 * args.steps
+        runs, tuned = {}, {}
+        for prec in ("fp64", "mixed", "fp32_quad"):
+            params, tune = autotune(batch, prec, reps=2, use_cache=False)
+            gr = batch.graph(prec, **params)
+            runs[prec] = maxrank(timer.run(gr.replay, args.steps, args.warmup))
+            tuned[prec] = params
+            if prec == "fp64":
+                ref = [(x.res.clone(), x.vals.clone(), x.g_u.clone(),
+                        None if getattr(x, "g_m", None) is None else x.g_m.clone())
+                       for x in insts]
+            else:
+                err = {"jacobian": 0.0, "residual": 0.0, "vjp_state": 0.0, "vjp_control": 0.0}
+                for x, (r64, v64, gu64, gm64) in zip(insts, ref):
+                    def rel(a, b):
+                        return float((a - b).abs().max() / b.abs().max())
+                    err["residual"] = max(err["residual"], rel(x.res, r64))
+                    err["jacobian"] = max(err["jacobian"], rel(x.vals, v64))
+                    err["vjp_state"] = max(err["vjp_state"], rel(x.g_u, gu64))
+                    if gm64 is not None:
+                        err["vjp_control"] = max(err["vjp_control"], rel(x.g_m, gm64))
+                tuned[prec + "_err"] = err
+            del gr
+            batch.check()
+        t_b32, t_b64, t_bmx = runs["fp32_quad"], runs["fp64"], runs["mixed"]
+        launches += 6 * args.steps
         line["batch"] = {
             "workload": "256 uneven instances (P1 Poisson jittered/permuted nx in 32..512, "
                         "Taylor-Hood cavity nx in 32..128, Re in 100..1000), residual + "
                         "Jacobian + VJP, one persistent launch replayed from a CUDA graph",
             "instances": {"p1": n_p1, "taylor_hood": n_th}, "elements": batch.num_elems,
-            "elements_per_s": world * batch.num_elems / t_b32,
+            "elements_per_s_fp32_quad": world * batch.num_elems / t_b32,
+            "elements_per_s_mixed": world * batch.num_elems / t_bmx,
             "elements_per_s_fp64": world * batch.num_elems / t_b64,
-            "ms_per_step": t_b32 * 1e3, "ms_per_step_fp64": t_b64 * 1e3,
-            "speedup_vs_plain_fp64": t_b64 / t_b32,
-            "max_rel_err_fp32_vs_fp64": err, "gate": 1e-6,
-            "autotuned": {"fp32_quad": params, "fp64": params64,
-                          "configs_timed": len(tune) if isinstance(tune, dict) else None},
+            "ms_per_step": {"fp32_quad": t_b32 * 1e3, "mixed": t_bmx * 1e3,
+                            "fp64": t_b64 * 1e3},
+            "speedup_vs_plain_fp64": {"fp32_quad": t_b64 / t_b32, "mixed": t_b64 / t_bmx},
+            "max_rel_err_vs_fp64": {"fp32_quad": tuned.pop("fp32_quad_err"),
+                                    "mixed": tuned.pop("mixed_err")},
+            "gate": 1e-6,
+            "precision_modes": {"fp32_quad": "all element quadrature fp32, fp64 accumulation",
+                                "mixed": "Jacobian fp32 quadrature; residual and P1 "
+                                         "gradients fp64; Taylor-Hood J^T lam from the fp32 J"},
+            "autotuned": tuned,
         }
-        del insts, batch, g32, g64
+        del insts, batch
 
     line["gpu_launches"] = launches
     line["scaling_mode"] = "replicas" if world > 1 else "single"

@@ -88,24 +88,76 @@ __device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th
   return (d.num_elems + c - 1) / c;
 }
 
-template <class T, bool kSep, bool kLoad, bool kVjp>
+// kMode: 0 = FP64, 1 = FP32 quadrature, 2 = MIXED (Jacobian from FP32
+// quadrature; residual and the P1 gradients from FP64 element math; the
+// Taylor-Hood state VJP J^T lam uses the FP32 Jacobian it transposes).
+constexpr int kModeFp64  = 0;
+constexpr int kModeFp32  = 1;
+constexpr int kModeMixed = 2;
+
+template <int kMode, bool kSep, bool kLoad, bool kVjp>
 __device__ __forceinline__ void p1Chunk(const P1Args& a, int e0, int e1)
 {
   for (int e = e0 + static_cast<int>(threadIdx.x); e < e1; e += kBatchThreads)
   {
-    p1Element<std::is_same<T, float>::value, kSep, kLoad, true, true, kVjp>(a, e);
+    if (kMode == kModeFp64)
+    {
+      p1Element<false, kSep, kLoad, true, true, kVjp>(a, e);
+    }
+    else if (kMode == kModeFp32)
+    {
+      p1Element<true, kSep, kLoad, true, true, kVjp>(a, e);
+    }
+    else
+    {
+      p1Element<true, kSep, false, true, false, false>(a, e);
+      p1Element<false, kSep, kLoad, false, true, kVjp>(a, e);
+    }
   }
 }
 
+template <int kMode, bool kSep>
+__device__ __forceinline__ void p1Dispatch(const P1Args& a, int e0, int e1)
+{
+  const bool load = a.f != nullptr, vjp = a.lam != nullptr;
+  if (load)
+  {
+    vjp ? p1Chunk<kMode, kSep, true, true>(a, e0, e1)
+        : p1Chunk<kMode, kSep, true, false>(a, e0, e1);
+  }
+  else
+  {
+    vjp ? p1Chunk<kMode, kSep, false, true>(a, e0, e1)
+        : p1Chunk<kMode, kSep, false, false>(a, e0, e1);
+  }
+}
+
+// Shared memory is one buffer, viewed as the FP32 or the FP64 element staging;
+// `staged` records which reference tables it currently holds (uniform).
 template <class T>
+__device__ __forceinline__ ThSmem<T>& ensureRef(unsigned char* raw, int& staged)
+{
+  auto&     sm   = *reinterpret_cast<ThSmem<T>*>(raw);
+  const int want = std::is_same<T, double>::value ? 1 : 0;
+  if (staged != want)
+  {
+    __syncthreads(); // previous users of the buffer are done
+    thStageRef(sm);
+    __syncthreads();
+    staged = want;
+  }
+  return sm;
+}
+
+template <int kMode>
 __global__ void __launch_bounds__(kBatchThreads)
     batchKernel(const BatchDesc* __restrict__ descs, int ni, int p1_chunk, int th_chunk,
                 int* __restrict__ ticket)
 {
-  __shared__ ThSmem<T> sm;
-  __shared__ int       prefix[kMaxInstances + 1];
-  __shared__ int       item;
-  thStageRef(sm);
+  __shared__ __align__(16) unsigned char smraw[sizeof(ThSmem<double>)];
+  __shared__ int prefix[kMaxInstances + 1];
+  __shared__ int item;
+  int            staged = -1;
   if (threadIdx.x == 0)
   {
     int acc = 0;
@@ -149,48 +201,46 @@ __global__ void __launch_bounds__(kBatchThreads)
     {
       const int e0 = c * p1_chunk;
       const int e1 = min(d.num_elems, e0 + p1_chunk);
-      const bool sep = d.p1.conn != nullptr, load = d.p1.f != nullptr;
-      const bool vjp = d.p1.lam != nullptr;
-      if (sep)
+      d.p1.conn != nullptr ? p1Dispatch<kMode, true>(d.p1, e0, e1)
+                           : p1Dispatch<kMode, false>(d.p1, e0, e1);
+    }
+    else
+    {
+      const int  e0  = c * th_chunk;
+      const int  e1  = min(d.num_elems, e0 + th_chunk);
+      const bool vjp = d.th.lam != nullptr;
+      if (kMode == kModeFp64)
       {
-        if (load)
+        auto& sm = ensureRef<double>(smraw, staged);
+        for (int eb = e0; eb < e1; eb += kElemsPerBlock)
         {
-          vjp ? p1Chunk<T, true, true, true>(d.p1, e0, e1)
-              : p1Chunk<T, true, true, false>(d.p1, e0, e1);
-        }
-        else
-        {
-          vjp ? p1Chunk<T, true, false, true>(d.p1, e0, e1)
-              : p1Chunk<T, true, false, false>(d.p1, e0, e1);
+          vjp ? thBlock<double, true, true, true>(d.th, eb, sm)
+              : thBlock<double, true, true, false>(d.th, eb, sm);
         }
       }
       else
       {
-        if (load)
+        auto& smf = ensureRef<float>(smraw, staged);
+        for (int eb = e0; eb < e1; eb += kElemsPerBlock)
         {
-          vjp ? p1Chunk<T, false, true, true>(d.p1, e0, e1)
-              : p1Chunk<T, false, true, false>(d.p1, e0, e1);
+          if (kMode == kModeFp32)
+          {
+            vjp ? thBlock<float, true, true, true>(d.th, eb, smf)
+                : thBlock<float, true, true, false>(d.th, eb, smf);
+          }
+          else
+          {
+            vjp ? thBlock<float, true, false, true>(d.th, eb, smf)
+                : thBlock<float, true, false, false>(d.th, eb, smf);
+          }
         }
-        else
+        if (kMode == kModeMixed)
         {
-          vjp ? p1Chunk<T, false, false, true>(d.p1, e0, e1)
-              : p1Chunk<T, false, false, false>(d.p1, e0, e1);
-        }
-      }
-    }
-    else
-    {
-      const int e0 = c * th_chunk;
-      const int e1 = min(d.num_elems, e0 + th_chunk);
-      for (int eb = e0; eb < e1; eb += kElemsPerBlock)
-      {
-        if (d.th.lam != nullptr)
-        {
-          thBlock<T, true, true, true>(d.th, eb, sm);
-        }
-        else
-        {
-          thBlock<T, true, true, false>(d.th, eb, sm);
+          auto& smd = ensureRef<double>(smraw, staged);
+          for (int eb = e0; eb < e1; eb += kElemsPerBlock)
+          {
+            thBlock<double, false, true, false>(d.th, eb, smd);
+          }
         }
       }
     }
@@ -371,8 +421,8 @@ extern "C" int gbfem_batch_run(gbfem_batch* b, int precision, int p1_chunk, int 
   using namespace gbfem;
   return guarded([&] {
     require(b != nullptr, "batch handle is null");
-    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD,
-            "batch precision must be FP64 or FP32_QUAD");
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
+            "unknown precision mode");
     require(p1_chunk >= kBatchThreads && p1_chunk % kBatchThreads == 0,
             "p1_chunk must be a positive multiple of 128");
     require(th_chunk >= kElemsPerBlock && th_chunk % kElemsPerBlock == 0,
@@ -392,13 +442,18 @@ extern "C" int gbfem_batch_run(gbfem_batch* b, int precision, int p1_chunk, int 
     const unsigned grid = static_cast<unsigned>(b->sm_count * blocks_per_sm);
     if (precision == GBFEM_PREC_FP64)
     {
-      batchKernel<double><<<grid, kBatchThreads, 0, s>>>(b->d_descs, b->num_instances,
-                                                         p1_chunk, th_chunk, b->d_ticket);
+      batchKernel<kModeFp64><<<grid, kBatchThreads, 0, s>>>(
+          b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
+    }
+    else if (precision == GBFEM_PREC_FP32_QUAD)
+    {
+      batchKernel<kModeFp32><<<grid, kBatchThreads, 0, s>>>(
+          b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
     }
     else
     {
-      batchKernel<float><<<grid, kBatchThreads, 0, s>>>(b->d_descs, b->num_instances,
-                                                        p1_chunk, th_chunk, b->d_ticket);
+      batchKernel<kModeMixed><<<grid, kBatchThreads, 0, s>>>(
+          b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
     }
     cudaCheck(cudaGetLastError(), "batch launch");
   });

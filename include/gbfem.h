@@ -242,7 +242,9 @@ typedef struct gbfem_batch gbfem_batch;
 GBFEM_API int       gbfem_batch_create(int num_instances,
                                        const gbfem_batch_instance* instances,
                                        void* stream, gbfem_batch** out);
-/* precision: GBFEM_PREC_FP64 or GBFEM_PREC_FP32_QUAD. Work items are
+/* precision: GBFEM_PREC_FP64, GBFEM_PREC_FP32_QUAD or GBFEM_PREC_MIXED
+ * (Jacobian from FP32 quadrature; residual and P1 gradients in FP64; the
+ * Taylor-Hood J^T lam uses the FP32 Jacobian). Work items are
  * p1_chunk P1 elements (multiple of 128) or th_chunk Taylor-Hood elements
  * (multiple of 8); the grid is blocks_per_sm x SM count. */
 GBFEM_API int       gbfem_batch_run(gbfem_batch* batch, int precision, int p1_chunk,
