@@ -154,7 +154,9 @@ __global__ void __launch_bounds__(kBatchThreads)
     batchKernel(const BatchDesc* __restrict__ descs, int ni, int p1_chunk, int th_chunk,
                 int* __restrict__ ticket)
 {
-  __shared__ __align__(16) unsigned char smraw[sizeof(ThSmem<double>)];
+  __shared__ __align__(16) unsigned char
+      smraw[sizeof(ThSmem<double>) > sizeof(ThSmem<float>) ? sizeof(ThSmem<double>)
+                                                            : sizeof(ThSmem<float>)];
   __shared__ int prefix[kMaxInstances + 1];
   __shared__ int item;
   int            staged = -1;
@@ -230,16 +232,8 @@ __global__ void __launch_bounds__(kBatchThreads)
           }
           else
           {
-            vjp ? thBlock<float, true, false, true>(d.th, eb, smf)
-                : thBlock<float, true, false, false>(d.th, eb, smf);
-          }
-        }
-        if (kMode == kModeMixed)
-        {
-          auto& smd = ensureRef<double>(smraw, staged);
-          for (int eb = e0; eb < e1; eb += kElemsPerBlock)
-          {
-            thBlock<double, false, true, false>(d.th, eb, smd);
+            vjp ? thBlock<float, true, false, true, true>(d.th, eb, smf)
+                : thBlock<float, true, false, false, true>(d.th, eb, smf);
           }
         }
       }

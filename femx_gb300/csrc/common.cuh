@@ -145,6 +145,18 @@ long long exclusiveScan(const int* in, int* out, long long n, cudaStream_t s);
 long long exclusiveScan64to32(const long long* in, int* out, long long n,
                               cudaStream_t s);
 
+// Rare-path hardware conversions, kept out of line so the compiler branches
+// around them instead of predicating them into every conversion (they issue
+// on the FP64 pipe).
+static __device__ __noinline__ double f32ToF64Slow(float f)
+{
+  return static_cast<double>(f);
+}
+static __device__ __noinline__ float f64ToF32Slow(double d)
+{
+  return __double2float_rn(d);
+}
+
 // Exact float -> double conversion from the IEEE-754 fields, on the integer
 // pipe. On GB300 the hardware conversion issues on the FP64 pipe (the scarce
 // one), so kernels whose element math runs in FP32 convert with this.
@@ -160,7 +172,7 @@ __device__ __forceinline__ double f32ToF64(float f)
   }
   if (e - 1u >= 0xfeu)
   {
-    return static_cast<double>(f);
+    return f32ToF64Slow(f);
   }
   const unsigned long long bits =
       (static_cast<unsigned long long>(u & 0x80000000u) << 32)
@@ -186,7 +198,7 @@ __device__ __forceinline__ float f64ToF32(double d)
   }
   if (fe <= 0 || fe >= 255)
   {
-    return __double2float_rn(d);
+    return f64ToF32Slow(d);
   }
   const unsigned m    = ((hi & 0xfffffu) << 3) | (lo >> 29);
   const unsigned rem  = lo & 0x1fffffffu;

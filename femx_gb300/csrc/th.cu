@@ -90,9 +90,9 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     }
     else
     {
-      // Jacobian from FP32 quadrature, residual from FP64 element math
-      thKernel<float, true, false><<<blocks, kThreads, 0, s>>>(a);
-      thKernel<double, false, true><<<blocks, kThreads, 0, s>>>(a);
+      // one launch: Jacobian from FP32 quadrature, residual from FP64
+      // direct quadrature in the same blocks
+      thKernelMixed<<<blocks, kThreads, 0, s>>>(a);
     }
     cudaCheck(cudaGetLastError(), "Taylor-Hood assembly launch");
   });

@@ -26,6 +26,7 @@ struct ThRef
   R T[3][6][6];      // sum_q w N^_a N^_b lambda_v
   R C[2][6][3];      // sum_q w psi^_b dN^_a,k
   R dNv[3][6][2];    // P2 reference gradients at the vertices
+  R P[kNq][3];       // P1 (pressure) values at the quadrature points
   R w[kNq];
 };
 
@@ -67,6 +68,9 @@ constexpr ThRef<double> makeRef()
     lam[i][0] = 1.0 - q[i][0] - q[i][1];
     lam[i][1] = q[i][0];
     lam[i][2] = q[i][1];
+    t.P[i][0] = lam[i][0];
+    t.P[i][1] = lam[i][1];
+    t.P[i][2] = lam[i][2];
     t.w[i]    = q[i][2];
     for (int a = 0; a < 6; ++a)
     {
@@ -137,6 +141,10 @@ constexpr ThRef<R> castRef()
   for (int q = 0; q < kNq; ++q)
   {
     r.w[q] = static_cast<R>(d.w[q]);
+    for (int b = 0; b < 3; ++b)
+    {
+      r.P[q][b] = static_cast<R>(d.P[q][b]);
+    }
     for (int a = 0; a < 6; ++a)
     {
       r.N[q][a]      = static_cast<R>(d.N[q][a]);
@@ -230,6 +238,18 @@ struct ThSmem
   T   outv[kElemsPerBlock][15][16];
   int outk[kElemsPerBlock][15][16];
   T   lam[kElemsPerBlock][16];
+  // FP64 residual by direct quadrature (MIXED mode): state, geometry and the
+  // per-quadrature-point reference-coordinate fluxes Ft[q][c][k], sources
+  // s[q][c] and weighted divergence dq[q].
+  struct Res64
+  {
+    double st[16];
+    double invJ[4];
+    double ad;
+    double Ft[kNq][2][2];
+    double src[kNq][2];
+    double dq[kNq];
+  } r64[kElemsPerBlock];
 };
 
 template <class T>
@@ -245,9 +265,15 @@ __device__ __forceinline__ void thStageRef(ThSmem<T>& sm)
 
 // The whole block works on elements [e_base, e_base + 8). Call from every
 // thread of a kThreads-wide block after thStageRef + __syncthreads.
-template <class T, bool kJac, bool kRes, bool kVjp>
+// kRes64 (with kRes = false): the residual is evaluated in FP64 by direct
+// quadrature alongside the T-precision Jacobian (the MIXED Newton scheme):
+//   R_(a,c) = sum_q [ Ft_c(q) . dN^_a(q) + src_c(q) N^_a(q) ],
+//   Ft_c = J^-1 W (nu grad u_c - p e_c),  src_c = W u . grad u_c,
+//   R_p(b)  = -sum_q psi^_b(q) W div u(q).
+template <class T, bool kJac, bool kRes, bool kVjp, bool kRes64 = false>
 __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& sm)
 {
+  static_assert(!(kRes && kRes64), "one residual precision at a time");
   const ThRef<T>& ref = sm.ref;
   const int       l   = threadIdx.x & (kLanes - 1);
   const int       le  = threadIdx.x / kLanes;
@@ -255,9 +281,15 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   const bool      has = e < a.ne;
   ElemShared<T>&  S   = sm.sh[le];
 
+  auto& R64 = sm.r64[le];
   if (has && l < 15)
   {
-    S.st[l] = gbfem::fromF64<T>(a.state[a.dofs[15 * e + l]]);
+    const double sv = a.state[a.dofs[15 * e + l]];
+    S.st[l]         = gbfem::fromF64<T>(sv);
+    if (kRes64)
+    {
+      R64.st[l] = sv;
+    }
     if (kVjp)
     {
       sm.lam[le][l] = gbfem::fromF64<T>(a.lam[a.dofs[15 * e + l]]);
@@ -284,8 +316,20 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       const double2 x2 = a.coords[a.conn6[6 * e + 2]];
       // J[a][b] = d x_a / d r_b of the affine map (vertex nodes); the edge
       // vectors carry the mesh scale and are formed in FP64, the rest in T.
-      const T j00 = gbfem::fromF64<T>(x1.x - x0.x), j01 = gbfem::fromF64<T>(x2.x - x0.x);
-      const T j10 = gbfem::fromF64<T>(x1.y - x0.y), j11 = gbfem::fromF64<T>(x2.y - x0.y);
+      const double dj00 = x1.x - x0.x, dj01 = x2.x - x0.x;
+      const double dj10 = x1.y - x0.y, dj11 = x2.y - x0.y;
+      if (kRes64)
+      {
+        const double ddet = dj00 * dj11 - dj01 * dj10;
+        const double dinv = 1.0 / ddet;
+        R64.invJ[0]       = dj11 * dinv;
+        R64.invJ[1]       = -dj01 * dinv;
+        R64.invJ[2]       = -dj10 * dinv;
+        R64.invJ[3]       = dj00 * dinv;
+        R64.ad            = fabs(ddet);
+      }
+      const T j00 = gbfem::fromF64<T>(dj00), j01 = gbfem::fromF64<T>(dj01);
+      const T j10 = gbfem::fromF64<T>(dj10), j11 = gbfem::fromF64<T>(dj11);
       const T det = j00 * j11 - j01 * j10;
       const T ad  = det < T(0) ? -det : det;
       if (ad >= T(1.0e-30))
@@ -302,7 +346,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
         S.aInvJ[1]  = ad * i01;
         S.aInvJ[2]  = ad * i10;
         S.aInvJ[3]  = ad * i11;
-        const T nad = T(a.nu) * ad;
+        const T nad = gbfem::fromF64<T>(a.nu) * ad;
         S.G3[0]     = nad * (i00 * i00 + i01 * i01);
         S.G3[1]     = nad * (i10 * i10 + i11 * i11);
         S.G3[2]     = nad * (i00 * i10 + i01 * i11);
@@ -342,6 +386,48 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     // ut_k = sum_d Jinv[k][d] u_d, so that u . dN_b = dN^_b . ut
     S.ut[q][0] = S.aInvJ[0] * u0 + S.aInvJ[1] * u1;
     S.ut[q][1] = S.aInvJ[2] * u0 + S.aInvJ[3] * u1;
+  }
+  if (kRes64 && live && l >= 6 && l < 6 + kNq)
+  {
+    // FP64 quadrature-point state and fluxes, reference tables from global
+    const ThRef<double>& rd = kRefD;
+    const int            q  = l - 6;
+    double               u0 = 0, u1 = 0, r00 = 0, r01 = 0, r10 = 0, r11 = 0;
+#pragma unroll
+    for (int s2 = 0; s2 < 6; ++s2)
+    {
+      const double v0 = R64.st[2 * s2], v1 = R64.st[2 * s2 + 1];
+      const double n = rd.N[q][s2], g0 = rd.dNr[q][s2][0], g1 = rd.dNr[q][s2][1];
+      u0 += n * v0;
+      u1 += n * v1;
+      r00 += v0 * g0; // sum_s u_(s,c) dN^_s,k  as [c][k]
+      r01 += v0 * g1;
+      r10 += v1 * g0;
+      r11 += v1 * g1;
+    }
+    const double* iJ = R64.invJ;
+    // grad u_c [e] = sum_k r_ck invJ[k][e]
+    const double G00 = r00 * iJ[0] + r01 * iJ[2], G01 = r00 * iJ[1] + r01 * iJ[3];
+    const double G10 = r10 * iJ[0] + r11 * iJ[2], G11 = r10 * iJ[1] + r11 * iJ[3];
+    double       pq  = 0;
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+    {
+      pq += rd.P[q][b] * R64.st[12 + b];
+    }
+    const double W   = rd.w[q] * R64.ad;
+    const double nu  = a.nu;
+    // physical fluxes W (nu grad u_c - p e_c), mapped by J^-1: Ft_c[k] =
+    // sum_e invJ[k][e] F_c[e], so that F_c . dN_a = Ft_c . dN^_a
+    const double F00 = W * (nu * G00 - pq), F01 = W * nu * G01;
+    const double F10 = W * nu * G10, F11 = W * (nu * G11 - pq);
+    R64.Ft[q][0][0] = iJ[0] * F00 + iJ[1] * F01;
+    R64.Ft[q][0][1] = iJ[2] * F00 + iJ[3] * F01;
+    R64.Ft[q][1][0] = iJ[0] * F10 + iJ[1] * F11;
+    R64.Ft[q][1][1] = iJ[2] * F10 + iJ[3] * F11;
+    R64.src[q][0]   = W * (u0 * G00 + u1 * G01);
+    R64.src[q][1]   = W * (u0 * G10 + u1 * G11);
+    R64.dq[q]       = W * (G00 + G11);
   }
   __syncthreads();
   if (live)
@@ -411,6 +497,30 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     if (kRes)
     {
       gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
+    }
+    if (kRes64)
+    {
+      const ThRef<double>& rd = kRefD;
+      double               r6 = 0;
+      if (l < 12)
+      {
+        const int sa = l >> 1, cc = l & 1;
+#pragma unroll
+        for (int q = 0; q < kNq; ++q)
+        {
+          r6 += R64.Ft[q][cc][0] * rd.dNr[q][sa][0] + R64.Ft[q][cc][1] * rd.dNr[q][sa][1]
+                + R64.src[q][cc] * rd.N[q][sa];
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int q = 0; q < kNq; ++q)
+        {
+          r6 -= rd.P[q][l - 12] * R64.dq[q];
+        }
+      }
+      gbfem::redAdd(a.res + row_dof, r6);
     }
     if (kJac)
     {
@@ -508,6 +618,15 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
   thStageRef(sm);
   __syncthreads();
   thBlock<T, kJac, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+// MIXED: FP32-quadrature Jacobian and FP64 residual in one pass.
+__global__ void __launch_bounds__(kThreads) thKernelMixed(ThArgs a)
+{
+  __shared__ ThSmem<float> sm;
+  thStageRef(sm);
+  __syncthreads();
+  thBlock<float, true, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
 
 } // namespace
