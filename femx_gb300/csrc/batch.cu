@@ -132,34 +132,34 @@ __device__ __forceinline__ void p1Dispatch(const P1Args& a, int e0, int e1)
   }
 }
 
-// Shared memory is one buffer, viewed as the FP32 or the FP64 element staging;
-// `staged` records which reference tables it currently holds (uniform).
-template <class T>
-__device__ __forceinline__ ThSmem<T>& ensureRef(unsigned char* raw, int& staged)
+// Taylor-Hood staging of each precision mode.
+template <int kMode>
+struct BatchSmem;
+template <>
+struct BatchSmem<kModeFp64>
 {
-  auto&     sm   = *reinterpret_cast<ThSmem<T>*>(raw);
-  const int want = std::is_same<T, double>::value ? 1 : 0;
-  if (staged != want)
-  {
-    __syncthreads(); // previous users of the buffer are done
-    thStageRef(sm);
-    __syncthreads();
-    staged = want;
-  }
-  return sm;
-}
+  using type = ThSmem<double>;
+};
+template <>
+struct BatchSmem<kModeFp32>
+{
+  using type = ThSmem<float>;
+};
+template <>
+struct BatchSmem<kModeMixed>
+{
+  using type = ThSmemMixed<float>;
+};
 
 template <int kMode>
 __global__ void __launch_bounds__(kBatchThreads)
     batchKernel(const BatchDesc* __restrict__ descs, int ni, int p1_chunk, int th_chunk,
                 int* __restrict__ ticket)
 {
-  __shared__ __align__(16) unsigned char
-      smraw[sizeof(ThSmem<double>) > sizeof(ThSmem<float>) ? sizeof(ThSmem<double>)
-                                                            : sizeof(ThSmem<float>)];
-  __shared__ int prefix[kMaxInstances + 1];
-  __shared__ int item;
-  int            staged = -1;
+  __shared__ typename BatchSmem<kMode>::type sm;
+  __shared__ int                             prefix[kMaxInstances + 1];
+  __shared__ int                             item;
+  thStageRef(sm);
   if (threadIdx.x == 0)
   {
     int acc = 0;
@@ -211,30 +211,22 @@ __global__ void __launch_bounds__(kBatchThreads)
       const int  e0  = c * th_chunk;
       const int  e1  = min(d.num_elems, e0 + th_chunk);
       const bool vjp = d.th.lam != nullptr;
-      if (kMode == kModeFp64)
+      for (int eb = e0; eb < e1; eb += kElemsPerBlock)
       {
-        auto& sm = ensureRef<double>(smraw, staged);
-        for (int eb = e0; eb < e1; eb += kElemsPerBlock)
+        if constexpr (kMode == kModeFp64)
         {
           vjp ? thBlock<double, true, true, true>(d.th, eb, sm)
               : thBlock<double, true, true, false>(d.th, eb, sm);
         }
-      }
-      else
-      {
-        auto& smf = ensureRef<float>(smraw, staged);
-        for (int eb = e0; eb < e1; eb += kElemsPerBlock)
+        else if constexpr (kMode == kModeFp32)
         {
-          if (kMode == kModeFp32)
-          {
-            vjp ? thBlock<float, true, true, true>(d.th, eb, smf)
-                : thBlock<float, true, true, false>(d.th, eb, smf);
-          }
-          else
-          {
-            vjp ? thBlock<float, true, false, true, true>(d.th, eb, smf)
-                : thBlock<float, true, false, false, true>(d.th, eb, smf);
-          }
+          vjp ? thBlock<float, true, true, true>(d.th, eb, sm)
+              : thBlock<float, true, true, false>(d.th, eb, sm);
+        }
+        else
+        {
+          vjp ? thBlock<float, true, false, true, true>(d.th, eb, sm)
+              : thBlock<float, true, false, false, true>(d.th, eb, sm);
         }
       }
     }

@@ -28,13 +28,15 @@ struct gbfem_assembly_map
   int* row_ptr       = nullptr;
   int* col_ind       = nullptr;
 
-  // Compact Jacobian scatter map for uniform layouts: for element e and
-  // local row i, the CSR slot of local column j is
-  //   row_ptr[res_dof(e, i)] + jac_pos[(e * uniform_res + i) * pos_stride + j]
-  // (one byte per entry, rows padded to pos_stride bytes so kernels load a
-  // whole row of positions with one vector load). Null when the layout is
-  // not uniform or a row has more than 256 entries; kernels then fall back
-  // to jac_map.
+  // Compact Jacobian scatter map for uniform layouts: one byte per local
+  // entry (i, j) giving its in-row position, CSR slot = row_ptr[res_dof(e,
+  // i)] + position. Blocks up to 4 columns (P1) are row-major,
+  //   jac_pos[(e * uniform_res + i) * 4 + j],
+  // wider blocks (up to 16 rows, e.g. Taylor-Hood's 15) column-major,
+  //   jac_pos[(e * uniform_state + j) * pos_stride + i],
+  // records padded to pos_stride bytes so a kernel loads one record with one
+  // vector load. Null when the layout is not uniform or a row has more than
+  // 256 entries; kernels then fall back to jac_map.
   unsigned char* jac_pos    = nullptr;
   int            pos_stride = 0;
 

@@ -238,7 +238,11 @@ __global__ void maxInRowPos(int ne, int nr, int nc, const int* __restrict__ rd,
   atomicMax(mx, m);
 }
 
-__global__ void fillInRowPos(int ne, int nr, int nc, int stride,
+// Row-major (stride 4): byte j of record (e, i) is entry (i, j).
+// Column-major (stride >= 16): byte i of record (e, j) is entry (i, j), so
+// the lane that scatters local column j loads all its rows' positions with
+// one 16-byte load. Padding bytes are zeroed by the caller.
+__global__ void fillInRowPos(int ne, int nr, int nc, int stride, bool col_major,
                              const int* __restrict__ rd,
                              const int* __restrict__ row_ptr,
                              const int* __restrict__ jac_map,
@@ -250,6 +254,16 @@ __global__ void fillInRowPos(int ne, int nr, int nc, int stride,
     return;
   }
   const int rs = row_ptr[rd[t]];
+  if (col_major)
+  {
+    const long long e = t / nr;
+    const int       i = static_cast<int>(t - e * nr);
+    for (int j = 0; j < nc; ++j)
+    {
+      pos[(e * nc + j) * stride + i] = static_cast<unsigned char>(jac_map[t * nc + j] - rs);
+    }
+    return;
+  }
   for (int j = 0; j < stride; ++j)
   {
     pos[t * stride + j] =
@@ -490,14 +504,18 @@ extern "C" int gbfem_assembly_map_create(int num_res, int num_states,
                   "AssemblyMap position readback");
         cudaCheck(cudaStreamSynchronize(s), "AssemblyMap position scan");
         deviceFree(mx);
-        if (mx_h < 256)
+        const int nr = m->uniform_res, nc = m->uniform_state;
+        if (mx_h < 256 && (nc <= 4 || nr <= 16))
         {
-          const int stride = m->uniform_state <= 4 ? 4 : ((m->uniform_state + 15) / 16) * 16;
-          m->pos_stride    = stride;
-          m->jac_pos       = deviceAlloc<unsigned char>(rows_tot * stride);
+          const bool      col_major = nc > 4;
+          const int       stride    = col_major ? 16 * ((max(nr, nc) + 15) / 16) : 4;
+          const long long records   = static_cast<long long>(num_elems) * (col_major ? nc : nr);
+          m->pos_stride             = stride;
+          m->jac_pos                = deviceAlloc<unsigned char>(records * stride);
+          cudaCheck(cudaMemsetAsync(m->jac_pos, 0, records * stride, s), "memset");
           fillInRowPos<<<blocksFor(rows_tot, 256), 256, 0, s>>>(
-              num_elems, m->uniform_res, m->uniform_state, stride, m->res_dofs,
-              m->row_ptr, m->jac_map, m->jac_pos);
+              num_elems, nr, nc, stride, col_major, m->res_dofs, m->row_ptr,
+              m->jac_map, m->jac_pos);
           cudaCheck(cudaGetLastError(), "AssemblyMap position launch");
         }
       }

@@ -226,30 +226,39 @@ struct ElemShared
   int ok;
 };
 
+// FP64 residual by direct quadrature (MIXED mode): state, geometry and the
+// per-quadrature-point reference-coordinate fluxes Ft[q][c][k], sources
+// src[q][c] and weighted divergence dq[q] of one element.
+struct Res64
+{
+  double st[16];
+  double invJ[4];
+  double ad;
+  double Ft[kNq][2][2];
+  double src[kNq][2];
+  double dq[kNq];
+};
+
 // Shared memory of one 128-thread block working on up to 8 elements.
 template <class T>
 struct ThSmem
 {
   ThRef<T>      ref;
   ElemShared<T> sh[kElemsPerBlock];
-  // Row-major staging of each element's 15x15 block (values and CSR slots)
-  // so that the scatter issues one row per half-warp instruction: lanes then
-  // hit the same row segment and the L2 reductions coalesce.
-  T   outv[kElemsPerBlock][15][16];
-  int outk[kElemsPerBlock][15][16];
+  // Each element's 15x15 block staged row by row (row stride 17, element
+  // stride 272 = 16 mod 32 words) so that both the row-wise writes and the
+  // column-wise reads of the two elements of a warp are free of bank
+  // conflicts, and the start of every row's CSR segment.
+  T   outv[kElemsPerBlock][16][17];
+  int rs[kElemsPerBlock][16];
   T   lam[kElemsPerBlock][16];
-  // FP64 residual by direct quadrature (MIXED mode): state, geometry and the
-  // per-quadrature-point reference-coordinate fluxes Ft[q][c][k], sources
-  // s[q][c] and weighted divergence dq[q].
-  struct Res64
-  {
-    double st[16];
-    double invJ[4];
-    double ad;
-    double Ft[kNq][2][2];
-    double src[kNq][2];
-    double dq[kNq];
-  } r64[kElemsPerBlock];
+};
+
+// MIXED mode adds the FP64 residual staging.
+template <class T>
+struct ThSmemMixed : ThSmem<T>
+{
+  Res64 r64[kElemsPerBlock];
 };
 
 template <class T>
@@ -281,14 +290,18 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   const bool      has = e < a.ne;
   ElemShared<T>&  S   = sm.sh[le];
 
-  auto& R64 = sm.r64[le];
+  Res64* R64 = nullptr;
+  if constexpr (kRes64)
+  {
+    R64 = &static_cast<ThSmemMixed<T>&>(sm).r64[le];
+  }
   if (has && l < 15)
   {
     const double sv = a.state[a.dofs[15 * e + l]];
     S.st[l]         = gbfem::fromF64<T>(sv);
     if (kRes64)
     {
-      R64.st[l] = sv;
+      R64->st[l] = sv;
     }
     if (kVjp)
     {
@@ -322,11 +335,11 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       {
         const double ddet = dj00 * dj11 - dj01 * dj10;
         const double dinv = 1.0 / ddet;
-        R64.invJ[0]       = dj11 * dinv;
-        R64.invJ[1]       = -dj01 * dinv;
-        R64.invJ[2]       = -dj10 * dinv;
-        R64.invJ[3]       = dj00 * dinv;
-        R64.ad            = fabs(ddet);
+        R64->invJ[0]       = dj11 * dinv;
+        R64->invJ[1]       = -dj01 * dinv;
+        R64->invJ[2]       = -dj10 * dinv;
+        R64->invJ[3]       = dj00 * dinv;
+        R64->ad            = fabs(ddet);
       }
       const T j00 = gbfem::fromF64<T>(dj00), j01 = gbfem::fromF64<T>(dj01);
       const T j10 = gbfem::fromF64<T>(dj10), j11 = gbfem::fromF64<T>(dj11);
@@ -396,7 +409,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 #pragma unroll
     for (int s2 = 0; s2 < 6; ++s2)
     {
-      const double v0 = R64.st[2 * s2], v1 = R64.st[2 * s2 + 1];
+      const double v0 = R64->st[2 * s2], v1 = R64->st[2 * s2 + 1];
       const double n = rd.N[q][s2], g0 = rd.dNr[q][s2][0], g1 = rd.dNr[q][s2][1];
       u0 += n * v0;
       u1 += n * v1;
@@ -405,7 +418,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       r10 += v1 * g0;
       r11 += v1 * g1;
     }
-    const double* iJ = R64.invJ;
+    const double* iJ = R64->invJ;
     // grad u_c [e] = sum_k r_ck invJ[k][e]
     const double G00 = r00 * iJ[0] + r01 * iJ[2], G01 = r00 * iJ[1] + r01 * iJ[3];
     const double G10 = r10 * iJ[0] + r11 * iJ[2], G11 = r10 * iJ[1] + r11 * iJ[3];
@@ -413,21 +426,21 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 #pragma unroll
     for (int b = 0; b < 3; ++b)
     {
-      pq += rd.P[q][b] * R64.st[12 + b];
+      pq += rd.P[q][b] * R64->st[12 + b];
     }
-    const double W   = rd.w[q] * R64.ad;
+    const double W   = rd.w[q] * R64->ad;
     const double nu  = a.nu;
     // physical fluxes W (nu grad u_c - p e_c), mapped by J^-1: Ft_c[k] =
     // sum_e invJ[k][e] F_c[e], so that F_c . dN_a = Ft_c . dN^_a
     const double F00 = W * (nu * G00 - pq), F01 = W * nu * G01;
     const double F10 = W * nu * G10, F11 = W * (nu * G11 - pq);
-    R64.Ft[q][0][0] = iJ[0] * F00 + iJ[1] * F01;
-    R64.Ft[q][0][1] = iJ[2] * F00 + iJ[3] * F01;
-    R64.Ft[q][1][0] = iJ[0] * F10 + iJ[1] * F11;
-    R64.Ft[q][1][1] = iJ[2] * F10 + iJ[3] * F11;
-    R64.src[q][0]   = W * (u0 * G00 + u1 * G01);
-    R64.src[q][1]   = W * (u0 * G10 + u1 * G11);
-    R64.dq[q]       = W * (G00 + G11);
+    R64->Ft[q][0][0] = iJ[0] * F00 + iJ[1] * F01;
+    R64->Ft[q][0][1] = iJ[2] * F00 + iJ[3] * F01;
+    R64->Ft[q][1][0] = iJ[0] * F10 + iJ[1] * F11;
+    R64->Ft[q][1][1] = iJ[2] * F10 + iJ[3] * F11;
+    R64->src[q][0]   = W * (u0 * G00 + u1 * G01);
+    R64->src[q][1]   = W * (u0 * G10 + u1 * G11);
+    R64->dq[q]       = W * (G00 + G11);
   }
   __syncthreads();
   if (live)
@@ -508,8 +521,8 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 #pragma unroll
         for (int q = 0; q < kNq; ++q)
         {
-          r6 += R64.Ft[q][cc][0] * rd.dNr[q][sa][0] + R64.Ft[q][cc][1] * rd.dNr[q][sa][1]
-                + R64.src[q][cc] * rd.N[q][sa];
+          r6 += R64->Ft[q][cc][0] * rd.dNr[q][sa][0] + R64->Ft[q][cc][1] * rd.dNr[q][sa][1]
+                + R64->src[q][cc] * rd.N[q][sa];
         }
       }
       else
@@ -517,36 +530,14 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 #pragma unroll
         for (int q = 0; q < kNq; ++q)
         {
-          r6 -= rd.P[q][l - 12] * R64.dq[q];
+          r6 -= rd.P[q][l - 12] * R64->dq[q];
         }
       }
       gbfem::redAdd(a.res + row_dof, r6);
     }
     if (kJac)
     {
-      const int rs = a.row_ptr[row_dof];
-      int       col[15];
-      if (a.jac_pos != nullptr)
-      {
-        const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
-        const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-        for (int j = 0; j < 15; ++j)
-        {
-          col[j] = rs + int((wd[j >> 2] >> (8 * (j & 3))) & 0xffu);
-        }
-      }
-      else
-      {
-        const int* jm = a.jac_map + 225LL * e + 15 * l;
-#pragma unroll
-        for (int j = 0; j < 15; ++j)
-        {
-          col[j] = jm[j];
-        }
-      }
-      T*   ov = sm.outv[le][l];
-      int* ok = sm.outk[le][l];
+      T* ov = sm.outv[le][l];
       if (l < 12)
       {
 #pragma unroll
@@ -570,14 +561,10 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
           ov[2 * sa]     = jcc[sa];
           ov[2 * sa + 1] = jco[sa];
         }
-        // the pressure-pressure block is structurally present and zero
-        ov[12] = ov[13] = ov[14] = T(0);
+        // the pressure-pressure block is structurally present and zero:
+        // nothing is added to it
       }
-#pragma unroll
-      for (int j = 0; j < 15; ++j)
-      {
-        ok[j] = col[j];
-      }
+      sm.rs[le][l] = a.row_ptr[row_dof];
     }
   }
   if (kJac)
@@ -585,14 +572,28 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     __syncwarp();
     if (live && l < 15)
     {
-      // lane l now owns local column l of every row of its element
-#pragma unroll 5
+      // Lane l owns local column l of every row of its element: a half-warp
+      // instruction adds one row's 15 entries, which lie in one CSR row
+      // segment, so the L2 reductions coalesce.
+      unsigned char pos[16];
+      if (a.jac_pos != nullptr)
+      {
+        const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
+        const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+        {
+          pos[i] = static_cast<unsigned char>(wd[i >> 2] >> (8 * (i & 3)));
+        }
+      }
+#pragma unroll
       for (int row = 0; row < 15; ++row)
       {
-        const double v = gbfem::toF64(sm.outv[le][row][l]);
         if (row < 12 || l < 12)
         {
-          gbfem::redAdd(a.vals + sm.outk[le][row][l], v);
+          const int slot = a.jac_pos != nullptr ? sm.rs[le][row] + pos[row]
+                                                : a.jac_map[225LL * e + 15 * row + l];
+          gbfem::redAdd(a.vals + slot, gbfem::toF64(sm.outv[le][row][l]));
         }
       }
       if (kVjp)
@@ -602,7 +603,10 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 #pragma unroll
         for (int row = 0; row < 15; ++row)
         {
-          acc += sm.outv[le][row][l] * sm.lam[le][row];
+          if (row < 12 || l < 12)
+          {
+            acc += sm.outv[le][row][l] * sm.lam[le][row];
+          }
         }
         gbfem::redAdd(a.g_state + a.dofs[15 * e + l], gbfem::toF64(acc));
       }
@@ -623,7 +627,7 @@ __global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
 // MIXED: FP32-quadrature Jacobian and FP64 residual in one pass.
 __global__ void __launch_bounds__(kThreads) thKernelMixed(ThArgs a)
 {
-  __shared__ ThSmem<float> sm;
+  __shared__ ThSmemMixed<float> sm;
   thStageRef(sm);
   __syncthreads();
   thBlock<float, true, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
