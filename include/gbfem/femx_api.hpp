@@ -11,8 +11,10 @@
 // The reference's ElementOperator is a compile-time functor
 // (femx/assembly/Assembly.hpp:138-152); a C ABI cannot take one, so this
 // layer dispatches on operator tag types (KappaPoissonP1, TaylorHoodNS) to
-// the per-physics entry points. Failures throw std::runtime_error with
-// femx's messages, like femx::require (femx/common/Checks.hpp:11-17).
+// the per-physics entry points; any other operator goes through the
+// header-only templated kernels of generic_assembly.cuh. Failures throw
+// std::runtime_error with femx's messages, like femx::require
+// (femx/common/Checks.hpp:11-17).
 // Every array is a device pointer; the stream comes from the CudaContext.
 #pragma once
 
@@ -64,8 +66,9 @@ using DeviceVectorView      = DeviceView<Real>;
 using DeviceConstVectorView = DeviceView<const Real>;
 
 /** Non-owning device geometry (femx/fem/Geometry.hpp:33-196) with a fixed
- * node count per element: node-major coords [num_nodes][2], element-major
- * connectivity [num_elems][nodes_per_elem]. */
+ * node count per element: node-major coords [num_nodes][dim], element-major
+ * connectivity [num_elems][nodes_per_elem]. The tagged fast paths are 2-D;
+ * user operators (generic_assembly.cuh) take any dim. */
 struct DeviceGeometry
 {
   Index        num_nodes{0};
@@ -73,6 +76,7 @@ struct DeviceGeometry
   Index        nodes_per_elem{0};
   const Real*  coords{nullptr};
   const Index* conn{nullptr};
+  Index        dim{2};
 };
 
 /** Shared immutable CSR pattern with a layout identity
@@ -270,7 +274,8 @@ inline void assemble(const KappaPoissonP1& op, const DeviceGeometry& geom,
   {
     detail::checkLayout(map, jac);
   }
-  require(geom.nodes_per_elem == 3, "KappaPoissonP1 expects three-node triangles");
+  require(geom.nodes_per_elem == 3 && geom.dim == 2,
+          "KappaPoissonP1 expects three-node triangles in 2-D");
   check(gbfem_assemble_p1_kappa(map.handle(), geom.num_nodes, geom.coords, geom.conn, op.kappa,
                                 op.f_nodal, state.data(), res.data(), jac.vals,
                                 static_cast<int>(op.precision), ctx.stream));
@@ -289,7 +294,8 @@ inline void assemble(const TaylorHoodNS& op, const DeviceGeometry& geom,
   {
     detail::checkLayout(map, jac);
   }
-  require(geom.nodes_per_elem == 6, "Taylor-Hood geometry expects six-node triangles");
+  require(geom.nodes_per_elem == 6 && geom.dim == 2,
+          "Taylor-Hood geometry expects six-node triangles in 2-D");
   check(gbfem_assemble_th_ns(map.handle(), geom.num_nodes, geom.coords, geom.conn, op.nu,
                              state.data(), res.data(), jac.vals,
                              static_cast<int>(op.precision), ctx.stream));
