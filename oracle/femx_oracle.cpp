@@ -16,6 +16,7 @@
 #include <limits>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace
@@ -682,6 +683,98 @@ void assembleLoop(const Map& m, const Op& op, const double* state,
   }
 }
 
+// Atomic FP64 add on the value's bit pattern (compare-exchange loop), the
+// effect of `#pragma omp atomic` on `vals[k] += v`.
+inline void atomicAddDouble(double* addr, double v)
+{
+  auto*         bits = reinterpret_cast<std::uint64_t*>(addr);
+  std::uint64_t old  = __atomic_load_n(bits, __ATOMIC_RELAXED);
+  for (;;)
+  {
+    double cur;
+    std::memcpy(&cur, &old, sizeof(double));
+    const double  nxt = cur + v;
+    std::uint64_t nb;
+    std::memcpy(&nb, &nxt, sizeof(double));
+    if (__atomic_compare_exchange_n(bits, &old, nb, true, __ATOMIC_RELAXED, __ATOMIC_RELAXED))
+    {
+      return;
+    }
+  }
+}
+
+// Multi-threaded element loop: the scheme of femx's OpenMP NS assembly
+// (femx/model/ns/NavierStokesModel.cpp:227-318): element chunks shared by
+// the threads, residual and CSR adds atomic (addElem(atomic),
+// femx/assembly/Assembly.cpp:8-41). Same operator as assembleLoop; the
+// order of the additions into one slot depends on thread timing.
+template <class Op>
+void assembleLoopThreads(const Map& m, const Op& op, const double* state, double* res,
+                         double* vals, int nthreads)
+{
+  nthreads          = std::max(1, nthreads);
+  const long long n = m.row_ptr[m.num_res];
+  {
+    std::vector<std::thread> zero;
+    for (int t = 0; t < nthreads; ++t)
+    {
+      zero.emplace_back([&, t] {
+        const long long a = n * t / nthreads, b = n * (t + 1) / nthreads;
+        std::fill(vals + a, vals + b, 0.0);
+        const long long ra = static_cast<long long>(m.num_res) * t / nthreads;
+        const long long rb = static_cast<long long>(m.num_res) * (t + 1) / nthreads;
+        std::fill(res + ra, res + rb, 0.0);
+      });
+    }
+    for (auto& th : zero)
+    {
+      th.join();
+    }
+  }
+  constexpr int            kChunk = 256;
+  int                      next   = 0;
+  std::vector<std::thread> work;
+  for (int t = 0; t < nthreads; ++t)
+  {
+    work.emplace_back([&] {
+      std::vector<double> st(m.max_state), re(m.max_res), jac(m.max_jac);
+      for (;;)
+      {
+        const int e0 = __atomic_fetch_add(&next, kChunk, __ATOMIC_RELAXED);
+        if (e0 >= m.num_elems)
+        {
+          return;
+        }
+        const int e1 = std::min(m.num_elems, e0 + kChunk);
+        for (int e = e0; e < e1; ++e)
+        {
+          const int nr = m.nrow(e), nc = m.ncol(e);
+          for (int c = 0; c < nc; ++c)
+          {
+            st[c] = state[m.state_dofs[m.state_offsets[e] + c]];
+          }
+          for (int r = 0; r < nr; ++r)
+          {
+            op.evalRow(e, r, st.data(), re[r], jac.data() + r * nc);
+          }
+          for (int r = 0; r < nr; ++r)
+          {
+            atomicAddDouble(res + m.res_dofs[m.res_offsets[e] + r], re[r]);
+          }
+          for (int i = 0; i < nr * nc; ++i)
+          {
+            atomicAddDouble(vals + m.jac_map[m.jac_offsets[e] + i], jac[i]);
+          }
+        }
+      }
+    });
+  }
+  for (auto& th : work)
+  {
+    th.join();
+  }
+}
+
 } // namespace
 
 extern "C" {
@@ -990,6 +1083,27 @@ int orc_assemble_th_range(const void* mh, const void* th, double nu,
       }
     } op{static_cast<const TaylorHoodNS*>(th), nu};
     assembleLoop(m, op, state, res, vals, e0, e1);
+  });
+}
+
+int orc_assemble_th_threads(const void* mh, const void* th, double nu,
+                            const double* state, double* res, double* vals,
+                            int nthreads)
+{
+  return guarded([&] {
+    const Map& m = *static_cast<const Map*>(mh);
+    require(m.max_res <= 15 && m.max_state <= 15,
+            "Taylor-Hood element expects 15 DOFs per element");
+    struct Op
+    {
+      const TaylorHoodNS* t;
+      double              nu;
+      void evalRow(int e, int row, const double* st, double& res, double* jac) const
+      {
+        t->evalRowNu(nu, e, row, st, res, jac);
+      }
+    } op{static_cast<const TaylorHoodNS*>(th), nu};
+    assembleLoopThreads(m, op, state, res, vals, nthreads);
   });
 }
 

@@ -115,6 +115,11 @@ void  orc_th_quad_free(void* th);
 int orc_assemble_th_range(const void* map, const void* th, double nu,
                           const double* state, double* res, double* vals,
                           int elem_begin, int elem_end);
+/* The same assembly on `nthreads` host threads with atomic adds, the scheme
+ * of femx's OpenMP NS assembly (NavierStokesModel.cpp:227-318). */
+int orc_assemble_th_threads(const void* map, const void* th, double nu,
+                            const double* state, double* res, double* vals,
+                            int nthreads);
 /* Whole-mesh convenience: builds the tables and assembles every element. */
 int orc_assemble_th_ns(const void* map, int num_p2_nodes,
                        const double* coords, const int* conn6, double nu,

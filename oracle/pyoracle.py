@@ -22,8 +22,8 @@ def build(force: bool = False) -> str:
     """Compile liboracle.so with g++ (portable flags: x86 and aarch64)."""
     if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC):
         subprocess.check_call([
-            "g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", SRC, "-o",
-            LIB_PATH,
+            "g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread", SRC,
+            "-o", LIB_PATH,
         ])
     return LIB_PATH
 
@@ -67,6 +67,7 @@ def lib():
         L.orc_th_quad_create.argtypes = [C.c_int, _f64p, C.c_int, _i32p]
         L.orc_th_quad_free.argtypes = [C.c_void_p]
         L.orc_assemble_th_range.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int, C.c_int]
+        L.orc_assemble_th_threads.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int]
         L.orc_assemble_p1_range.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, C.c_void_p, _f64p, _f64p, _f64p, C.c_int, C.c_int]
         _lib = L
     return _lib
@@ -260,6 +261,16 @@ def assemble_th_range(amap: AssemblyMap, th: THQuad, nu, state, elem_begin=0, el
     vals = np.zeros(amap.nnz) if vals is None else vals
     _check(lib().orc_assemble_th_range(amap.h, th.h, float(nu), _f64(state), res, vals,
                                        int(elem_begin), int(elem_end)))
+    return res, vals
+
+
+def assemble_th_threads(amap: AssemblyMap, th: THQuad, nu, state, nthreads, res=None,
+                        vals=None):
+    """The Taylor-Hood assembly on `nthreads` host threads (atomic adds)."""
+    res = np.zeros(amap.num_res) if res is None else res
+    vals = np.zeros(amap.nnz) if vals is None else vals
+    _check(lib().orc_assemble_th_threads(amap.h, th.h, float(nu), _f64(state), res, vals,
+                                         int(nthreads)))
     return res, vals
 
 

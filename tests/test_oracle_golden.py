@@ -159,3 +159,19 @@ def test_taylor_hood_jacobian_matches_finite_differences(golden):
     fd = (rp - rm) / (2 * h)
     jd = orc.matvec(m.row_ptr, m.col_ind, vals, d)
     assert rel_inf(jd, fd) <= 1e-6
+
+
+def test_threaded_taylor_hood_loop_matches_serial(golden):
+    """The multi-threaded loop (atomic adds, femx's OpenMP NS scheme) gives
+    the serial loop's result to rounding."""
+    g = golden("th_jit3")
+    nd = int(g["num_dofs"])
+    e = g["conn6"].shape[0]
+    offs = (np.arange(e + 1) * 15).astype(np.int32)
+    m = orc.AssemblyMap(nd, nd, offs, g["elem_dofs"], offs, g["elem_dofs"])
+    th = orc.THQuad(g["coords"], g["conn6"])
+    res1, vals1 = orc.assemble_th_range(m, th, float(g["nu"]), g["state"])
+    res4, vals4 = orc.assemble_th_threads(m, th, float(g["nu"]), g["state"], 4)
+    assert rel_inf(res4, res1) <= 1e-14
+    assert rel_inf(vals4, vals1) <= 1e-14
+    assert rel_inf(vals4, g["vals"]) <= 1e-13
