@@ -305,9 +305,10 @@ def main():
         res = torch.zeros(nd, dtype=torch.float64, device="cuda")
         jac = A.CsrMatrix(pat)
 
-        def th_step(prec):
+        def th_step(prec, det=False):
             def fn():
-                A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision=prec)
+                A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision=prec,
+                                     deterministic=det)
                 A.replaceRes(bc, state, bvals, res)
                 A.replaceRows(bc, jac, 1.0)
             return fn
@@ -328,6 +329,15 @@ def main():
             t_mixed = maxrank(timer.run(th_step("mixed"), args.steps, args.warmup))
         launches += 3 * args.steps
         amap.check()
+        # deterministic mode (row-gather, no atomics): time and bitwise check
+        t_det = timer.run(th_step("fp32_quad", det=True), args.steps, args.warmup)
+        det_runs = []
+        for _ in range(2):
+            th_step("fp32_quad", det=True)()
+            det_runs.append((res.clone(), jac.vals.clone()))
+        det_bitwise = bool(torch.equal(det_runs[0][0], det_runs[1][0])
+                           and torch.equal(det_runs[0][1], det_runs[1][1]))
+        launches += 4 * args.steps
         # kernel-only time of the fast assembly (no BC kernels)
         t_kern = timer.run(lambda: A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac,
                                                         precision="fp32_quad"),
@@ -380,6 +390,11 @@ def main():
                            "speedup_of_fast_path": t_plain / t_fast},
             "rel_err_vs_fp64": {"jacobian": err_j, "residual": err_r,
                                 "gate": 1e-6, "norm": "inf, relative"},
+            "deterministic_fp32": {"value": world * e / t_det, "unit": "elements/s",
+                                   "ms_per_step": t_det * 1e3,
+                                   "bitwise_equal_over_runs": det_bitwise,
+                                   "scheme": "element rows as records, CSR rows summed in "
+                                             "element order, no atomics"},
             "mixed_newton": {"value": world * e / t_mixed, "unit": "elements/s",
                              "ms_per_step": t_mixed * 1e3,
                              "precision": "Jacobian fp32 quadrature, residual fp64",

@@ -22,6 +22,7 @@ GBFEM_ENOMEM = 4
 PREC_FP64 = 0
 PREC_FP32_QUAD = 1
 PREC_MIXED = 2
+DETERMINISTIC = 0x100
 
 
 class GbfemError(RuntimeError):
@@ -79,6 +80,7 @@ SIGNATURES = {
     "gbfem_assembly_map_get_view": (_i, [_vp, C.POINTER(AssemblyMapView)]),
     "gbfem_assembly_map_destroy": (None, [_vp]),
     "gbfem_assembly_map_check": (_i, [_vp, _vp]),
+    "gbfem_assembly_map_enable_gather": (_i, [_vp, _vp]),
     "gbfem_boundary_map_create": (_i, [_i, _vp, _i, _i, _vp, _vp, C.c_ulonglong, _vp,
                                        C.POINTER(_vp)]),
     "gbfem_boundary_map_get_view": (_i, [_vp, C.POINTER(BoundaryMapView)]),

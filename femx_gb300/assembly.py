@@ -171,6 +171,13 @@ class AssemblyMap:
         offs = _view_i32(offs_ptr, self._v.num_elems + 1, self)
         return int(offs[-1].item()) if offs.numel() else 0
 
+    def enableDeterministic(self):
+        """Build the row-gather tables behind deterministic assembly (setup,
+        once per map; synchronizes the current stream)."""
+        if not getattr(self, "_gather", False):
+            call("gbfem_assembly_map_enable_gather", self._h, _stream())
+            self._gather = True
+
     def check(self):
         """Raise if a kernel met invalid data (e.g. a degenerate element)."""
         call("gbfem_assembly_map_check", self._h, _stream())
@@ -321,14 +328,21 @@ def vjpP1Kappa(amap: AssemblyMap, coords, kappa, u, lam, g_u=None, g_m=None, con
 
 
 def assembleTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, res, jac=None,
-                       precision: str = "fp64"):
+                       precision: str = "fp64", deterministic: bool = False):
+    """Taylor-Hood Newton residual (and Jacobian when jac is given).
+    deterministic=True sums element rows per CSR row in element order (no
+    atomics): bitwise reproducible; the first call on a map builds its
+    row-gather tables (amap.enableDeterministic())."""
     coords = _dev(coords, torch.float64, "coords")
     conn6 = _dev(conn6, torch.int32, "conn6")
     state = _check_vec(state, amap.numStates(), "state")
     res = _check_vec(res, amap.numRes(), "residual")
+    mode = PRECISIONS[precision]
+    if deterministic:
+        amap.enableDeterministic()
+        mode |= _lib.DETERMINISTIC
     call("gbfem_assemble_th_ns", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn6),
-         float(nu), _ptr(state), _ptr(res), _jac_ptr(amap, jac), PRECISIONS[precision],
-         _stream())
+         float(nu), _ptr(state), _ptr(res), _jac_ptr(amap, jac), mode, _stream())
 
 
 def matvec(mat: CsrMatrix, x, y, alpha: float = 1.0, beta: float = 0.0):

@@ -40,6 +40,27 @@ struct gbfem_assembly_map
   unsigned char* jac_pos    = nullptr;
   int            pos_stride = 0;
 
+  // Row-gather tables, built on request by gbfem_assembly_map_enable_gather
+  // (uniform maps with 6..16 residual and state DOFs per element and rows up
+  // to 256 entries, e.g. Taylor-Hood). A record is one
+  // element row (e, i); records are numbered row by row, and within a
+  // residual row in ascending (e, i) order:
+  //   gather_off[r] .. gather_off[r + 1]   records adding into row r
+  //   gather_slot[e * nr + i]              record index of element row (e, i)
+  //   gather_pos[k * 16 + j]               in-row CSR position of entry j
+  // Element kernels write record k (16 values: the row's entries, padded)
+  // to gather_eb and the row's residual term to gather_res; a row kernel
+  // then sums each row's records in record order. No atomics: results are
+  // bitwise reproducible run to run. gather_eb holds 16 doubles per record
+  // (the FP32 path uses the first half of each as 16 floats).
+  int            max_in_row_pos = -1; // largest in-row position (uniform maps)
+  int            gather_records = 0;
+  int*           gather_off     = nullptr;
+  int*           gather_slot    = nullptr;
+  unsigned char* gather_pos     = nullptr;
+  double*        gather_eb      = nullptr;
+  double*        gather_res     = nullptr;
+
   // Status word written by hot-path kernels that meet invalid data
   // (degenerate elements); read by gbfem_assembly_map_check().
   gbfem::DeviceStatus* status = nullptr;

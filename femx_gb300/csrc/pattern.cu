@@ -25,6 +25,7 @@ using gbfem::DeviceStatus;
 
 constexpr int kWarpsPerBlock = 8;
 constexpr int kStageCap      = 512; // candidates staged in shared memory per warp
+constexpr int kGatherMaxRowEntries = 256; // in-row positions are bytes
 
 // Offsets must start at 0 and be non-decreasing; checked before any DOF
 // table is read, so no later kernel can index past the copied tables.
@@ -271,6 +272,68 @@ __global__ void fillInRowPos(int ne, int nr, int nc, int stride, bool col_major,
   }
 }
 
+// Row-gather tables: records per residual row, placed, then each row's
+// records put in ascending (e, i) order, so the numbering is deterministic.
+__global__ void countGatherRows(long long n, const int* __restrict__ rd, int* __restrict__ cnt)
+{
+  const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (t < n)
+  {
+    atomicAdd(cnt + rd[t], 1);
+  }
+}
+
+__global__ void placeGatherRecords(long long n, const int* __restrict__ rd,
+                                   const int* __restrict__ off, int* __restrict__ fill,
+                                   int* __restrict__ keys)
+{
+  const long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (t < n)
+  {
+    const int r                        = rd[t];
+    keys[off[r] + atomicAdd(fill + r, 1)] = static_cast<int>(t);
+  }
+}
+
+__global__ void sortGatherRows(int num_res, const int* __restrict__ off, int* __restrict__ keys)
+{
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= num_res)
+  {
+    return;
+  }
+  for (int a = off[r] + 1; a < off[r + 1]; ++a)
+  {
+    const int v = keys[a];
+    int       b = a - 1;
+    while (b >= off[r] && keys[b] > v)
+    {
+      keys[b + 1] = keys[b];
+      --b;
+    }
+    keys[b + 1] = v;
+  }
+}
+
+__global__ void fillGatherRecords(long long n, int nc, const int* __restrict__ keys,
+                                  const int* __restrict__ rd, const int* __restrict__ row_ptr,
+                                  const int* __restrict__ jac_map, int* __restrict__ slot,
+                                  unsigned char* __restrict__ pos)
+{
+  const long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (k >= n)
+  {
+    return;
+  }
+  const int t  = keys[k];
+  slot[t]      = static_cast<int>(k);
+  const int rs = row_ptr[rd[t]];
+  for (int j = 0; j < 16; ++j)
+  {
+    pos[k * 16 + j] = j < nc ? static_cast<unsigned char>(jac_map[static_cast<long long>(t) * nc + j] - rs) : 0;
+  }
+}
+
 __global__ void compareTables(long long n, const int* __restrict__ a,
                               const int* __restrict__ b, int* __restrict__ diff)
 {
@@ -305,17 +368,52 @@ struct Scratch
   }
 };
 
+void buildGatherTables(gbfem_assembly_map* m, cudaStream_t s)
+{
+  using gbfem::blocksFor;
+  using gbfem::cudaCheck;
+  using gbfem::deviceAlloc;
+  const int       nr = m->uniform_res, nc = m->uniform_state;
+  const long long n  = static_cast<long long>(m->num_elems) * nr;
+  Scratch         tmp;
+  int*            cnt  = deviceAlloc<int>(m->num_res + 1LL);
+  tmp.p[0]             = cnt;
+  int*            keys = deviceAlloc<int>(n);
+  tmp.p[1]             = keys;
+  cudaCheck(cudaMemsetAsync(cnt, 0, sizeof(int) * (m->num_res + 1LL), s), "memset");
+  countGatherRows<<<blocksFor(n, 256), 256, 0, s>>>(n, m->res_dofs, cnt);
+  cudaCheck(cudaGetLastError(), "gather count launch");
+  m->gather_off = deviceAlloc<int>(m->num_res + 1LL);
+  gbfem::exclusiveScan(cnt, m->gather_off, m->num_res, s);
+  cudaCheck(cudaMemsetAsync(cnt, 0, sizeof(int) * (m->num_res + 1LL), s), "memset");
+  placeGatherRecords<<<blocksFor(n, 256), 256, 0, s>>>(n, m->res_dofs, m->gather_off, cnt, keys);
+  sortGatherRows<<<blocksFor(m->num_res, 256), 256, 0, s>>>(m->num_res, m->gather_off, keys);
+  m->gather_slot = deviceAlloc<int>(n);
+  m->gather_pos  = deviceAlloc<unsigned char>(n * 16);
+  fillGatherRecords<<<blocksFor(n, 256), 256, 0, s>>>(n, nc, keys, m->res_dofs, m->row_ptr,
+                                                      m->jac_map, m->gather_slot,
+                                                      m->gather_pos);
+  cudaCheck(cudaGetLastError(), "gather fill launch");
+  m->gather_eb      = deviceAlloc<double>(n * 16);
+  m->gather_res     = deviceAlloc<double>(n);
+  m->gather_records = static_cast<int>(n);
+  cudaCheck(cudaStreamSynchronize(s), "gather tables");
+}
+
 } // namespace
 
 gbfem_assembly_map::~gbfem_assembly_map()
 {
   for (int* p : {res_offsets, res_dofs, state_offsets, state_dofs, jac_offsets,
-                 jac_map, row_ptr, col_ind})
+                 jac_map, row_ptr, col_ind, gather_off, gather_slot})
   {
     gbfem::deviceFree(p);
   }
   gbfem::deviceFree(status);
   gbfem::deviceFree(jac_pos);
+  gbfem::deviceFree(gather_pos);
+  gbfem::deviceFree(gather_eb);
+  gbfem::deviceFree(gather_res);
 }
 
 namespace gbfem
@@ -518,6 +616,7 @@ extern "C" int gbfem_assembly_map_create(int num_res, int num_states,
               m->jac_map, m->jac_pos);
           cudaCheck(cudaGetLastError(), "AssemblyMap position launch");
         }
+        m->max_in_row_pos = mx_h;
       }
       cudaCheck(cudaStreamSynchronize(s), "AssemblyMap build");
     }
@@ -553,6 +652,41 @@ extern "C" int gbfem_assembly_map_get_view(const gbfem_assembly_map* m,
     info->jac_map       = m->jac_map;
     info->row_ptr       = m->row_ptr;
     info->col_ind       = m->col_ind;
+  });
+}
+
+extern "C" int gbfem_assembly_map_enable_gather(gbfem_assembly_map* m, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(m != nullptr, "AssemblyMap handle is null");
+    if (m->gather_off != nullptr || m->num_elems == 0)
+    {
+      return;
+    }
+    const int nr = m->uniform_res, nc = m->uniform_state;
+    require(nr >= 6 && nr <= 16 && nc >= 6 && nc <= 16 && m->max_in_row_pos >= 0
+                && m->max_in_row_pos < kGatherMaxRowEntries,
+            "AssemblyMap layout does not support deterministic row-gather assembly "
+            "(uniform blocks of 6..16 DOFs and rows up to 256 entries)");
+    try
+    {
+      buildGatherTables(m, asStream(stream));
+    }
+    catch (...)
+    {
+      for (void* p : {static_cast<void*>(m->gather_off), static_cast<void*>(m->gather_slot),
+                      static_cast<void*>(m->gather_pos), static_cast<void*>(m->gather_eb),
+                      static_cast<void*>(m->gather_res)})
+      {
+        deviceFree(p);
+      }
+      m->gather_off = m->gather_slot = nullptr;
+      m->gather_pos                  = nullptr;
+      m->gather_eb = m->gather_res = nullptr;
+      m->gather_records            = 0;
+      throw;
+    }
   });
 }
 

@@ -211,6 +211,11 @@ struct ThArgs
   const double*        lam;     // adjoint for the fused state VJP, or null
   double*              g_state; // J^T lam accumulated here when lam != null
   DeviceStatus*        status;
+  // row-gather output (kGather): record index of element row (e, l), the
+  // records' 16 values (float or double) and residual terms
+  const int*           gslot;
+  void*                geb;
+  double*              gres;
 };
 
 template <class T>
@@ -272,6 +277,52 @@ __device__ __forceinline__ void thStageRef(ThSmem<T>& sm)
   }
 }
 
+// FP64 residual of local row l from the staged quadrature-point fluxes.
+__device__ __forceinline__ double rowRes64(const Res64& R, int l)
+{
+  const ThRef<double>& rd = kRefD;
+  double               r6 = 0;
+  if (l < 12)
+  {
+    const int sa = l >> 1, cc = l & 1;
+#pragma unroll
+    for (int q = 0; q < kNq; ++q)
+    {
+      r6 += R.Ft[q][cc][0] * rd.dNr[q][sa][0] + R.Ft[q][cc][1] * rd.dNr[q][sa][1]
+            + R.src[q][cc] * rd.N[q][sa];
+    }
+  }
+  else
+  {
+#pragma unroll
+    for (int q = 0; q < kNq; ++q)
+    {
+      r6 -= rd.P[q][l - 12] * R.dq[q];
+    }
+  }
+  return r6;
+}
+
+// One 16-value record, 16-byte aligned: vector stores.
+__device__ __forceinline__ void storeRecord(float* dst, const float (&v)[16])
+{
+  float4* d = reinterpret_cast<float4*>(dst);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+  {
+    d[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  }
+}
+__device__ __forceinline__ void storeRecord(double* dst, const double (&v)[16])
+{
+  double2* d = reinterpret_cast<double2*>(dst);
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+  {
+    d[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  }
+}
+
 // The whole block works on elements [e_base, e_base + 8). Call from every
 // thread of a kThreads-wide block after thStageRef + __syncthreads.
 // kRes64 (with kRes = false): the residual is evaluated in FP64 by direct
@@ -279,10 +330,11 @@ __device__ __forceinline__ void thStageRef(ThSmem<T>& sm)
 //   R_(a,c) = sum_q [ Ft_c(q) . dN^_a(q) + src_c(q) N^_a(q) ],
 //   Ft_c = J^-1 W (nu grad u_c - p e_c),  src_c = W u . grad u_c,
 //   R_p(b)  = -sum_q psi^_b(q) W div u(q).
-template <class T, bool kJac, bool kRes, bool kVjp, bool kRes64 = false>
+template <class T, bool kJac, bool kRes, bool kVjp, bool kRes64 = false, bool kGather = false>
 __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& sm)
 {
   static_assert(!(kRes && kRes64), "one residual precision at a time");
+  static_assert(!(kGather && kVjp), "the fused VJP scatters its column sums");
   const ThRef<T>& ref = sm.ref;
   const int       l   = threadIdx.x & (kLanes - 1);
   const int       le  = threadIdx.x / kLanes;
@@ -504,36 +556,76 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       r += jcc[sa] * S.st[2 * sa] + jco[sa] * S.st[2 * sa + 1];
     }
   }
-  if (row_lane)
+  if (kGather && row_lane)
+  {
+    // one record per element row: its 15 entries (+ one pad) and its
+    // residual term; the row kernel sums the records of each CSR row
+    const int k = a.gslot[15 * e + l];
+    if (kRes)
+    {
+      a.gres[k] = gbfem::toF64(r);
+    }
+    if constexpr (kRes64)
+    {
+      a.gres[k] = rowRes64(*R64, l);
+    }
+    if (kJac)
+    {
+      T v[16];
+      if (l < 12)
+      {
+#pragma unroll
+        for (int b = 0; b < 6; ++b)
+        {
+          v[2 * b]     = c ? jco[b] : jcc[b];
+          v[2 * b + 1] = c ? jcc[b] : jco[b];
+        }
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+        {
+          v[12 + b] = jp[b];
+        }
+      }
+      else
+      {
+#pragma unroll
+        for (int sa = 0; sa < 6; ++sa)
+        {
+          v[2 * sa]     = jcc[sa];
+          v[2 * sa + 1] = jco[sa];
+        }
+        v[12] = v[13] = v[14] = T(0);
+      }
+      v[15] = T(0);
+      storeRecord(static_cast<T*>(a.geb) + 16LL * k, v);
+    }
+  }
+  if (kGather && has && !live && l < 15)
+  {
+    // a rejected element (reported through the status word) adds nothing
+    const int k = a.gslot[15 * e + l];
+    a.gres[k]   = 0.0;
+    if (kJac)
+    {
+      T z[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+      {
+        z[i] = T(0);
+      }
+      storeRecord(static_cast<T*>(a.geb) + 16LL * k, z);
+    }
+  }
+  if (!kGather && row_lane)
   {
     const int row_dof = a.dofs[15 * e + l];
     if (kRes)
     {
       gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
     }
-    if (kRes64)
+    if constexpr (kRes64)
     {
-      const ThRef<double>& rd = kRefD;
-      double               r6 = 0;
-      if (l < 12)
-      {
-        const int sa = l >> 1, cc = l & 1;
-#pragma unroll
-        for (int q = 0; q < kNq; ++q)
-        {
-          r6 += R64->Ft[q][cc][0] * rd.dNr[q][sa][0] + R64->Ft[q][cc][1] * rd.dNr[q][sa][1]
-                + R64->src[q][cc] * rd.N[q][sa];
-        }
-      }
-      else
-      {
-#pragma unroll
-        for (int q = 0; q < kNq; ++q)
-        {
-          r6 -= rd.P[q][l - 12] * R64->dq[q];
-        }
-      }
-      gbfem::redAdd(a.res + row_dof, r6);
+      gbfem::redAdd(a.res + row_dof, rowRes64(*R64, l));
     }
     if (kJac)
     {
@@ -567,7 +659,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       sm.rs[le][l] = a.row_ptr[row_dof];
     }
   }
-  if (kJac)
+  if (kJac && !kGather)
   {
     __syncwarp();
     if (live && l < 15)
@@ -631,6 +723,24 @@ __global__ void __launch_bounds__(kThreads) thKernelMixed(ThArgs a)
   thStageRef(sm);
   __syncthreads();
   thBlock<float, true, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+// Row-gather variants: the element pass writes records, no atomics.
+template <class T, bool kJac, bool kRes>
+__global__ void __launch_bounds__(kThreads) thKernelGather(ThArgs a)
+{
+  __shared__ ThSmem<T> sm;
+  thStageRef(sm);
+  __syncthreads();
+  thBlock<T, kJac, kRes, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+__global__ void __launch_bounds__(kThreads) thKernelMixedGather(ThArgs a)
+{
+  __shared__ ThSmemMixed<float> sm;
+  thStageRef(sm);
+  __syncthreads();
+  thBlock<float, true, false, false, true, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
 
 } // namespace

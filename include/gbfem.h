@@ -42,6 +42,12 @@ extern "C" {
 #define GBFEM_PREC_FP64 0
 #define GBFEM_PREC_FP32_QUAD 1
 #define GBFEM_PREC_MIXED 2
+/* OR-ed into a Taylor-Hood precision argument: deterministic assembly —
+ * element rows are written as records and each CSR row sums its records in
+ * element order (no atomics, no zero-fill), so repeated calls agree bit for
+ * bit, like femx's serial CPU loop. Needs gbfem_assembly_map_enable_gather
+ * on the map first. */
+#define GBFEM_DETERMINISTIC 0x100
 
 GBFEM_API const char* gbfem_last_error(void);
 GBFEM_API int         gbfem_version(void);
@@ -78,6 +84,15 @@ GBFEM_API void gbfem_assembly_map_destroy(gbfem_assembly_map* map);
  * Jacobian." from ElementValues::invJacobian, ElementValues.cpp:210-229).
  * Synchronizes `stream`; returns GBFEM_EDATA with the message if set. */
 GBFEM_API int  gbfem_assembly_map_check(const gbfem_assembly_map* map, void* stream);
+/* Builds the row-gather tables behind GBFEM_DETERMINISTIC assembly (setup:
+ * allocates and synchronizes `stream`; later calls return at once). A record
+ * per element row, numbered row by row in ascending element order; about
+ * 150 bytes of device memory per element row. Needs a uniform layout with
+ * 6..16 DOFs per element and rows up to 256 entries (Taylor-Hood: yes);
+ * otherwise GBFEM_EINVAL. Not to be called concurrently with other work on
+ * the same map. No counterpart in the reference, whose CPU loop is serial
+ * and deterministic by construction (Assembly.hpp:186-223). */
+GBFEM_API int  gbfem_assembly_map_enable_gather(gbfem_assembly_map* map, void* stream);
 
 /* ---------------------------------------------------------------------------
  * BoundaryMap — replaces femx::assembly::makeBoundaryMap(dofs, pattern)

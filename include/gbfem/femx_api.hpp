@@ -116,6 +116,11 @@ public:
   }
   const gbfem_assembly_map_view& view() const { return v_; }
   gbfem_assembly_map*            handle() const { return h_.get(); }
+  /** Builds the row-gather tables deterministic assembly needs (setup). */
+  void enableDeterministic(CudaContext& ctx) const
+  {
+    check(gbfem_assembly_map_enable_gather(h_.get(), ctx.stream));
+  }
 
 private:
   std::shared_ptr<gbfem_assembly_map> h_;
@@ -258,6 +263,7 @@ struct TaylorHoodNS
 {
   Real      nu{1.0};
   Precision precision{Precision::FP64};
+  bool      deterministic{false}; // needs map.enableDeterministic(ctx) first
 };
 
 /** assemble(op, geom, map, state, res, jac, ctx) for KappaPoissonP1
@@ -296,9 +302,9 @@ inline void assemble(const TaylorHoodNS& op, const DeviceGeometry& geom,
   }
   require(geom.nodes_per_elem == 6 && geom.dim == 2,
           "Taylor-Hood geometry expects six-node triangles in 2-D");
+  const int mode = static_cast<int>(op.precision) | (op.deterministic ? GBFEM_DETERMINISTIC : 0);
   check(gbfem_assemble_th_ns(map.handle(), geom.num_nodes, geom.coords, geom.conn, op.nu,
-                             state.data(), res.data(), jac.vals,
-                             static_cast<int>(op.precision), ctx.stream));
+                             state.data(), res.data(), jac.vals, mode, ctx.stream));
 }
 
 /** Residual VJPs of KappaPoissonP1: g_u = (dR/du)^T lam, g_m = (dR/dm)^T lam

@@ -369,3 +369,46 @@ def test_taylor_hood_cavity_matches_oracle():
         _, res, vals = th_gpu(cp2, conn6, dofs, nd, 1e-3, state, precision)
         assert rel_inf(res, rres) <= tol_r
         assert rel_inf(vals, rvals) <= tol_j
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_quad", "mixed"])
+def test_taylor_hood_assembly_is_bitwise_reproducible(precision):
+    """Deterministic mode: element records summed per CSR row in element
+    order, no atomics, so repeated assemblies agree bit for bit (also
+    residual-only calls)."""
+    c3, k3 = meshes.jittered_tri(20, seed=9)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    state = meshes.cavity_state(cp2, nv, seed=9)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    coords, c6, st = dev(cp2), dev(conn6, torch.int32), dev(state)
+    outs = []
+    for _ in range(3):
+        res = torch.full((nd,), 7.0, dtype=torch.float64, device="cuda")
+        jac = A.CsrMatrix(m.pattern(), torch.full((m.pattern().nnz,), -3.0,
+                                                  dtype=torch.float64, device="cuda"))
+        A.assembleTaylorHood(m, coords, c6, 1e-3, st, res, jac, precision=precision,
+                             deterministic=True)
+        r_only = torch.full((nd,), 5.0, dtype=torch.float64, device="cuda")
+        A.assembleTaylorHood(m, coords, c6, 1e-3, st, r_only, None, precision=precision,
+                             deterministic=True)
+        outs.append((res, jac.vals, r_only))
+    m.check()
+    for res, vals, r_only in outs[1:]:
+        assert torch.equal(res, outs[0][0])
+        assert torch.equal(vals, outs[0][1])
+        assert torch.equal(r_only, outs[0][2])
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-3, state)
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert rel_inf(host(outs[0][1]), rvals) <= tol
+    assert rel_inf(host(outs[0][0]), rres) <= (1e-12 if precision != "fp32_quad" else 1e-6)
+
+
+def test_deterministic_mode_needs_a_supported_layout():
+    coords, conn = meshes.structured_tri(4)
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    n = coords.shape[0]
+    m = gpu_map(n, n, offs, dofs, offs, dofs)
+    with pytest.raises(A.GbfemError, match="row-gather"):
+        m.enableDeterministic()
