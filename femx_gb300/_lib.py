@@ -55,6 +55,13 @@ class BoundaryMapView(C.Structure):
     ]
 
 
+class CsrTransposeView(C.Structure):
+    _fields_ = [
+        ("rows", C.c_int), ("cols", C.c_int), ("nnz", C.c_int),
+        ("row_ptr", C.c_void_p), ("col_ind", C.c_void_p), ("src_slot", C.c_void_p),
+    ]
+
+
 class BatchInstance(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("map", C.c_void_p), ("num_nodes", C.c_int),
@@ -92,10 +99,15 @@ SIGNATURES = {
     "gbfem_prepare_forward_solve_noalloc": (_i, [_i, _vp, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbfem_spmv": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp]),
     "gbfem_spmv_t": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp]),
+    "gbfem_csr_transpose_create": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
+    "gbfem_csr_transpose_get_view": (_i, [_vp, _vp]),
+    "gbfem_csr_transpose_apply": (_i, [_vp, _vp, _vp, _vp]),
+    "gbfem_csr_transpose_destroy": (None, [_vp]),
     "gbfem_axpby": (_i, [_i, _d, _vp, _d, _vp, _vp]),
     "gbfem_assemble_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_vjp_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
+    "gbfem_vjp_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
     "gbfem_probe_fp64_fma": (_i, [_i, _i, _i, _vp, _vp]),
     "gbfem_batch_create": (_i, [_i, C.POINTER(BatchInstance), _vp, C.POINTER(_vp)]),
     "gbfem_batch_run": (_i, [_vp, _i, _i, _i, _i, _vp]),

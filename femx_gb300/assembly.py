@@ -32,7 +32,7 @@ __all__ = [
     "makeAssemblyMap", "makeAssemblyMapFromElems", "makeBoundaryMap",
     "replaceRows", "replaceRes", "zeroBoundary", "prepareForwardSolve",
     "assembleP1Kappa", "vjpP1Kappa", "assembleTaylorHood", "matvec", "matvecT",
-    "axpby", "PRECISIONS",
+    "axpby", "transpose", "vjpTaylorHood", "PRECISIONS",
 ]
 
 PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32_quad": _lib.PREC_FP32_QUAD,
@@ -345,6 +345,18 @@ def assembleTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, res, jac=Non
          float(nu), _ptr(state), _ptr(res), _jac_ptr(amap, jac), mode, _stream())
 
 
+def vjpTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, lam, g_state,
+                  precision: str = "fp64"):
+    """g_state = J(state)^T lam of the Taylor-Hood residual, without forming J."""
+    coords = _dev(coords, torch.float64, "coords")
+    conn6 = _dev(conn6, torch.int32, "conn6")
+    state = _check_vec(state, amap.numStates(), "state")
+    lam = _check_vec(lam, amap.numRes(), "adjoint")
+    g_state = _check_vec(g_state, amap.numStates(), "VJP output")
+    call("gbfem_vjp_th_ns", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn6),
+         float(nu), _ptr(state), _ptr(lam), _ptr(g_state), PRECISIONS[precision], _stream())
+
+
 def matvec(mat: CsrMatrix, x, y, alpha: float = 1.0, beta: float = 0.0):
     x = _check_vec(x, mat.cols, "matvec input")
     y = _check_vec(y, mat.rows, "matvec output")
@@ -358,6 +370,46 @@ def matvecT(mat: CsrMatrix, x, y, alpha: float = 1.0, beta: float = 0.0):
     call("gbfem_spmv_t", mat.rows, mat.cols, _ptr(mat.pattern.row_ptr),
          _ptr(mat.pattern.col_ind), _ptr(mat.vals), _ptr(x), _ptr(y), float(alpha),
          float(beta), _stream())
+
+
+class _CsrTranspose:
+    """Cached transposed pattern + value permutation of one source layout
+    (femx MatrixHandler::transpose, MatrixHandler.cpp:140-155)."""
+
+    _next_layout = 1 << 62
+
+    def __init__(self, pattern: CsrPattern):
+        h = C.c_void_p()
+        call("gbfem_csr_transpose_create", pattern.rows, pattern.cols, _ptr(pattern.row_ptr),
+             _ptr(pattern.col_ind), _stream(), C.byref(h))
+        self._h = h
+        v = _lib.CsrTransposeView()
+        call("gbfem_csr_transpose_get_view", self._h, C.byref(v))
+        _CsrTranspose._next_layout += 1
+        self.pattern = CsrPattern(v.rows, v.cols, _view_i32(v.row_ptr, v.rows + 1, self),
+                                  _view_i32(v.col_ind, v.nnz, self), _CsrTranspose._next_layout)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib._lib is not None:
+            _lib._lib.gbfem_csr_transpose_destroy(h)
+            self._h = None
+
+
+def transpose(src: CsrMatrix, dst: CsrMatrix | None = None) -> CsrMatrix:
+    """Explicit transpose dst = src^T. The transposed pattern is built once
+    per source layout and reused; a dst on that pattern is updated in place
+    (values only), otherwise a new matrix is returned."""
+    t = getattr(src.pattern, "_transpose", None)
+    if t is None:
+        t = _CsrTranspose(src.pattern)
+        src.pattern._transpose = t
+    if dst is not None and dst.vals.data_ptr() == src.vals.data_ptr():
+        raise GbfemError(_lib.GBFEM_EINVAL, "CSR transpose does not support in-place output")
+    if dst is None or dst.pattern.layout_id != t.pattern.layout_id:
+        dst = CsrMatrix(t.pattern)
+    call("gbfem_csr_transpose_apply", t._h, _ptr(src.vals), _ptr(dst.vals), _stream())
+    return dst
 
 
 def axpby(a: float, x, b: float, y):

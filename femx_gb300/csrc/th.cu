@@ -147,3 +147,54 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     cudaCheck(cudaGetLastError(), "Taylor-Hood assembly launch");
   });
 }
+
+extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
+                               const double* coords, const int* conn6, double nu,
+                               const double* state, const double* lam, double* g_state,
+                               int precision, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(map != nullptr, "AssemblyMap handle is null");
+    require(map->num_elems == 0
+                || (map->uniform_res == 15 && map->uniform_state == 15),
+            "Taylor-Hood element expects 15 DOFs per element");
+    require(map->num_res == map->num_states && map->same_dofs,
+            "Taylor-Hood assembly expects identical residual and state DOF "
+            "tables");
+    require(num_p2_nodes >= 0, "Geometry node count must be non-negative");
+    require(map->num_elems == 0 || (coords && conn6 && state && lam),
+            "VJP inputs must not be null");
+    require(g_state != nullptr, "VJP output is null");
+    require(g_state != state && g_state != lam, "VJP output must not alias its inputs");
+    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD
+                || precision == GBFEM_PREC_MIXED,
+            "unknown precision mode");
+    require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
+            "Geometry coordinates must be 16-byte aligned");
+    cudaStream_t s = asStream(stream);
+    cudaCheck(cudaMemsetAsync(g_state, 0, sizeof(double) * map->num_states, s), "VJP zero");
+    if (map->num_elems == 0)
+    {
+      return;
+    }
+    ThArgs a{};
+    a.ne        = map->num_elems;
+    a.num_nodes = num_p2_nodes;
+    a.dofs      = map->state_dofs;
+    a.conn6     = conn6;
+    a.coords    = reinterpret_cast<const double2*>(coords);
+    a.nu        = nu;
+    a.state     = state;
+    a.row_ptr   = map->row_ptr;
+    a.jac_map   = map->jac_map;
+    a.lam       = lam;
+    a.g_state   = g_state;
+    a.status    = map->status;
+    const unsigned blocks = blocksFor(a.ne, kElemsPerBlock);
+    // MIXED keeps the Jacobian (and so J^T lam) in FP32 quadrature
+    precision == GBFEM_PREC_FP64 ? thVjpKernel<double, false><<<blocks, kThreads, 0, s>>>(a)
+                                 : thVjpKernel<float, false><<<blocks, kThreads, 0, s>>>(a);
+    cudaCheck(cudaGetLastError(), "Taylor-Hood VJP launch");
+  });
+}

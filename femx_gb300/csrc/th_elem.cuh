@@ -667,25 +667,28 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       // Lane l owns local column l of every row of its element: a half-warp
       // instruction adds one row's 15 entries, which lie in one CSR row
       // segment, so the L2 reductions coalesce.
-      unsigned char pos[16];
-      if (a.jac_pos != nullptr)
+      if (a.vals != nullptr) // null: J^T lam only (the element block is staged, not kept)
       {
-        const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
-        const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
+        unsigned char pos[16];
+        if (a.jac_pos != nullptr)
         {
-          pos[i] = static_cast<unsigned char>(wd[i >> 2] >> (8 * (i & 3)));
+          const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
+          const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+          {
+            pos[i] = static_cast<unsigned char>(wd[i >> 2] >> (8 * (i & 3)));
+          }
         }
-      }
 #pragma unroll
-      for (int row = 0; row < 15; ++row)
-      {
-        if (row < 12 || l < 12)
+        for (int row = 0; row < 15; ++row)
         {
-          const int slot = a.jac_pos != nullptr ? sm.rs[le][row] + pos[row]
-                                                : a.jac_map[225LL * e + 15 * row + l];
-          gbfem::redAdd(a.vals + slot, gbfem::toF64(sm.outv[le][row][l]));
+          if (row < 12 || l < 12)
+          {
+            const int slot = a.jac_pos != nullptr ? sm.rs[le][row] + pos[row]
+                                                  : a.jac_map[225LL * e + 15 * row + l];
+            gbfem::redAdd(a.vals + slot, gbfem::toF64(sm.outv[le][row][l]));
+          }
         }
       }
       if (kVjp)
@@ -723,6 +726,17 @@ __global__ void __launch_bounds__(kThreads) thKernelMixed(ThArgs a)
   thStageRef(sm);
   __syncthreads();
   thBlock<float, true, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+// State VJP g += J(u)^T lam without storing J (vals null), plus the
+// residual when kRes.
+template <class T, bool kRes>
+__global__ void __launch_bounds__(kThreads) thVjpKernel(ThArgs a)
+{
+  __shared__ ThSmem<T> sm;
+  thStageRef(sm);
+  __syncthreads();
+  thBlock<T, true, kRes, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
 
 // Row-gather variants: the element pass writes records, no atomics.

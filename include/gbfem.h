@@ -173,6 +173,33 @@ GBFEM_API int gbfem_spmv_t(int rows, int cols, const int* row_ptr, const int* co
                  const double* vals, const double* x, double* y, double alpha,
                  double beta, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Explicit CSR transpose — replaces MatrixHandler::transpose(src, dst)
+ * (femx/linalg/handler/MatrixHandler.cpp:140-155, MatrixHandler.cu:401-512).
+ * _create builds, once per source layout, the transposed pattern (rows =
+ * source cols; column indices ascending, as femx's transposeCsr) and the
+ * value permutation (setup: allocates, synchronizes `stream`). _apply moves
+ * the values only: t_vals[p] = vals[src_slot[p]] (in-place is rejected, as
+ * in femx). The handle owns the transposed pattern.
+ * ------------------------------------------------------------------------ */
+typedef struct gbfem_csr_transpose gbfem_csr_transpose;
+
+typedef struct
+{
+  int        rows, cols, nnz;   /* of the transpose */
+  const int *row_ptr, *col_ind; /* transposed pattern */
+  const int* src_slot;          /* source slot of every transposed slot */
+} gbfem_csr_transpose_view;
+
+GBFEM_API int  gbfem_csr_transpose_create(int rows, int cols, const int* row_ptr,
+                                          const int* col_ind, void* stream,
+                                          gbfem_csr_transpose** out);
+GBFEM_API int  gbfem_csr_transpose_get_view(const gbfem_csr_transpose* t,
+                                            gbfem_csr_transpose_view* view);
+GBFEM_API int  gbfem_csr_transpose_apply(const gbfem_csr_transpose* t, const double* vals,
+                                         double* t_vals, void* stream);
+GBFEM_API void gbfem_csr_transpose_destroy(gbfem_csr_transpose* t);
+
 /* y = a x + b y — VectorHandler<Cuda>::axpby (femx/linalg/handler/
  * VectorHandler.cu:124-136), used by the state solvers for rhs = -res
  * (femx/state/StateSolver.hpp:90-108). y is not read when b == 0. */
@@ -218,6 +245,15 @@ GBFEM_API int gbfem_assemble_th_ns(const gbfem_assembly_map* map, int num_p2_nod
                          const double* coords, const int* conn6, double nu,
                          const double* state, double* res, double* vals,
                          int precision, void* stream);
+/* State VJP of the Taylor-Hood residual: g_state = J(state)^T lam, computed
+ * element by element without forming J (the transpose action behind
+ * Residual::applyJacT / adjoint solves, femx/state/Residual.hpp:42-59,
+ * TimeResidual.hpp:223-227). g_state is overwritten. FP64, or FP32
+ * quadrature (FP32_QUAD and MIXED) with FP64 accumulation. */
+GBFEM_API int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
+                              const double* coords, const int* conn6, double nu,
+                              const double* state, const double* lam, double* g_state,
+                              int precision, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Batched assembly: many independent instances (meshes of uneven size, P1

@@ -322,4 +322,20 @@ inline void applyJacT(const KappaPoissonP1& op, const DeviceGeometry& geom,
                            static_cast<int>(op.precision), ctx.stream));
 }
 
+/** State VJP of TaylorHoodNS: g_state = J(state)^T lam without forming J
+ * (Residual::applyJacT, femx/state/Residual.hpp:42-59). */
+inline void applyJacT(const TaylorHoodNS& op, const DeviceGeometry& geom,
+                      const DeviceAssemblyMap& map, DeviceConstVectorView state,
+                      DeviceConstVectorView lam, DeviceVectorView g_state, CudaContext& ctx)
+{
+  require(lam.size() == map.numRes() && state.size() == map.numStates()
+              && g_state.size() == map.numStates(),
+          "VJP vectors have incompatible sizes");
+  require(geom.nodes_per_elem == 6 && geom.dim == 2,
+          "Taylor-Hood geometry expects six-node triangles in 2-D");
+  check(gbfem_vjp_th_ns(map.handle(), geom.num_nodes, geom.coords, geom.conn, op.nu,
+                        state.data(), lam.data(), g_state.data(),
+                        static_cast<int>(op.precision), ctx.stream));
+}
+
 } // namespace gbfem

@@ -412,3 +412,68 @@ def test_deterministic_mode_needs_a_supported_layout():
     m = gpu_map(n, n, offs, dofs, offs, dofs)
     with pytest.raises(A.GbfemError, match="row-gather"):
         m.enableDeterministic()
+
+
+def test_csr_transpose_known_answer():
+    """femx's csrMatrixTranspose (tests/unit/linalg/runLinalgTests.cpp:307-355)."""
+    pat = A.CsrPattern(3, 4, dev(np.array([0, 2, 4, 7]), torch.int32),
+                       dev(np.array([0, 2, 1, 3, 0, 2, 3]), torch.int32), 12345)
+    src = A.CsrMatrix(pat, dev(np.array([2.0, -1.0, 3.0, 4.0, -2.0, 5.0, 1.0])))
+    dst = A.transpose(src)
+    assert (dst.rows, dst.cols, dst.nnz) == (4, 3, 7)
+    assert host(dst.pattern.row_ptr).tolist() == [0, 2, 3, 5, 7]
+    assert host(dst.pattern.col_ind).tolist() == [0, 2, 1, 0, 2, 1, 2]
+    assert host(dst.vals).tolist() == [2.0, -2.0, 3.0, -1.0, 5.0, 4.0, 1.0]
+    ptrs = (dst.pattern.row_ptr.data_ptr(), dst.pattern.col_ind.data_ptr(), dst.vals.data_ptr())
+    src.vals.copy_(dev(np.array([-1.0, 2.0, 0.5, -3.0, 4.0, 1.0, -2.0])))
+    again = A.transpose(src, dst)
+    assert again is dst
+    assert ptrs == (dst.pattern.row_ptr.data_ptr(), dst.pattern.col_ind.data_ptr(),
+                    dst.vals.data_ptr())
+    assert host(dst.vals).tolist() == [-1.0, 4.0, 0.5, 2.0, 1.0, -3.0, -2.0]
+    with pytest.raises(A.GbfemError, match="in-place"):
+        A.transpose(src, src)
+
+
+def test_csr_transpose_of_taylor_hood_jacobian():
+    import scipy.sparse as sp
+    c3, k3 = meshes.jittered_tri(10, seed=4)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2,
+                         dev(meshes.cavity_state(cp2, nv, seed=4)), res, jac)
+    jt = A.transpose(jac)
+    ref = jac.to_scipy().T.tocsr()
+    ref.sort_indices()
+    assert np.array_equal(host(jt.pattern.row_ptr), ref.indptr)
+    assert np.array_equal(host(jt.pattern.col_ind), ref.indices)
+    assert np.array_equal(host(jt.vals), ref.data)
+    # A^T x through the explicit transpose equals matvecT
+    x = dev(np.random.default_rng(4).standard_normal(nd))
+    y1 = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    y2 = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    A.matvec(jt, x, y1)
+    A.matvecT(jac, x, y2)
+    assert rel_inf(host(y1), host(y2)) <= 1e-14
+    assert isinstance(ref, sp.csr_matrix)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_quad", 1e-6), ("mixed", 1e-6)])
+def test_taylor_hood_state_vjp_matches_oracle(precision, tol):
+    """J(u)^T lam without forming J, against the oracle's J transposed."""
+    c3, k3 = meshes.jittered_tri(12, seed=21)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    state = meshes.cavity_state(cp2, nv, seed=21)
+    lam = np.random.default_rng(21).standard_normal(nd)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    g = torch.full((nd,), 3.0, dtype=torch.float64, device="cuda")
+    A.vjpTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), dev(lam), g,
+                    precision=precision)
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    _, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-2, state)
+    ref = orc.matvec_t(om.row_ptr, om.col_ind, rvals, lam, nd)
+    assert rel_inf(host(g), ref) <= tol
