@@ -775,6 +775,245 @@ void assembleLoopThreads(const Map& m, const Op& op, const double* state, double
   }
 }
 
+// ---------------------------------------------------------------------------
+// femx's equal-order GLS Navier-Stokes time operator, restated
+// (femx/model/ns/Components.hpp:330-577: evalQp, elemLength, advDeriv,
+// gradDot, NavierOperator::evalPhysicsRow). P1 triangles in 2-D: 3 nodes,
+// local DOFs vdof(in, c) = 2 in + c then pdof(in) = 6 + in; element data
+// from P1Quad (makeNavierData = ElementValues over the order-2 rule).
+// Templated on the scalar so that the forward-mode Dual below gives exact
+// history derivatives (the role Enzyme plays in femx, Components.cpp:67-125).
+
+struct Dual
+{
+  double v = 0.0, d = 0.0;
+  Dual() = default;
+  Dual(double x) : v(x) {}
+  Dual(double x, double dx) : v(x), d(dx) {}
+};
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator-(Dual a) { return {-a.v, -a.d}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(Dual a, Dual b)
+{
+  return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)};
+}
+inline Dual& operator+=(Dual& a, Dual b) { return a = a + b; }
+inline Dual& operator-=(Dual& a, Dual b) { return a = a - b; }
+inline double val(double x) { return x; }
+inline double val(Dual x) { return x.v; }
+inline double sqrtS(double x) { return std::sqrt(x); }
+// sqrt at 0 gets the derivative 0 (its one-sided limit of the squared
+// quantities it feeds is 0: flow = (2|u|/h)^2 is smooth in u).
+inline Dual sqrtS(Dual x)
+{
+  const double r = std::sqrt(x.v);
+  return {r, r > 0.0 ? 0.5 * x.d / r : 0.0};
+}
+inline double absS(double x) { return x >= 0.0 ? x : -x; }
+inline Dual absS(Dual x) { return x.v >= 0.0 ? x : -x; }
+
+template <class S>
+struct NsQp
+{
+  S u[2], adv[2], grad[2][2], adv_grad[2], tau;
+};
+
+struct NavierGLS
+{
+  const P1Quad* q;
+  double        rho, mu, dt;
+  int           step, num_hist;
+
+  double N(int iq, int in) const { return q->N[iq * 3 + in]; }
+  double dNdx(int e, int iq, int in, int d) const
+  {
+    return q->dNdx[((std::size_t(e) * q->nq + iq) * 3 + in) * 2 + d];
+  }
+  double JxW(int e, int iq) const { return q->JxW[std::size_t(e) * q->nq + iq]; }
+
+  template <class S>
+  S elemLength(const NsQp<S>& qp, int e, int iq) const
+  {
+    S speed2 = 0.0;
+    for (int d = 0; d < 2; ++d)
+    {
+      speed2 += qp.u[d] * qp.u[d];
+    }
+    const S speed = sqrtS(speed2);
+    S       dir[2];
+    if (val(speed) > 1.0e-10)
+    {
+      for (int d = 0; d < 2; ++d)
+      {
+        dir[d] = qp.u[d] / speed;
+      }
+    }
+    else
+    {
+      const double c = 1.0 / std::sqrt(2.0);
+      dir[0]         = c;
+      dir[1]         = c;
+    }
+    S sum = 0.0;
+    for (int in = 0; in < 3; ++in)
+    {
+      S g = 0.0;
+      for (int d = 0; d < 2; ++d)
+      {
+        g += dir[d] * dNdx(e, iq, in, d);
+      }
+      sum += absS(g);
+    }
+    return val(sum) > 1.0e-14 ? S(2.0) / sum : S(0.0);
+  }
+
+  template <class S>
+  void evalQp(int e, int iq, const S* h0, const S* h1, NsQp<S>& qp) const
+  {
+    for (int c = 0; c < 2; ++c)
+    {
+      qp.u[c] = qp.adv[c] = qp.adv_grad[c] = 0.0;
+      qp.grad[c][0] = qp.grad[c][1] = 0.0;
+    }
+    for (int in = 0; in < 3; ++in)
+    {
+      const double Nv = N(iq, in);
+      for (int c = 0; c < 2; ++c)
+      {
+        const int id = 2 * in + c;
+        const S   v  = h0[id];
+        qp.u[c] += Nv * v;
+        for (int d = 0; d < 2; ++d)
+        {
+          qp.grad[c][d] += dNdx(e, iq, in, d) * v;
+        }
+        S adv = v;
+        if (step > 0 && num_hist > 1)
+        {
+          adv = 1.5 * v - 0.5 * h1[id];
+        }
+        qp.adv[c] += Nv * adv;
+      }
+    }
+    S speed2 = 0.0;
+    for (int c = 0; c < 2; ++c)
+    {
+      speed2 += qp.u[c] * qp.u[c];
+      for (int d = 0; d < 2; ++d)
+      {
+        qp.adv_grad[c] += qp.grad[c][d] * qp.adv[d];
+      }
+    }
+    const S      speed = sqrtS(speed2);
+    const S      h     = elemLength(qp, e, iq);
+    const double nu    = mu / rho;
+    const double time  = (2.0 / dt) * (2.0 / dt);
+    S            flow  = 0.0, diff = 0.0;
+    if (val(h) > 0.0)
+    {
+      flow = (2.0 * speed / h) * (2.0 * speed / h);
+      diff = (4.0 * nu / (h * h)) * (4.0 * nu / (h * h));
+    }
+    qp.tau = S(1.0) / sqrtS(time + flow + diff);
+  }
+
+  template <class S>
+  S advDeriv(const NsQp<S>& qp, int e, int iq, int in) const
+  {
+    S v = 0.0;
+    for (int d = 0; d < 2; ++d)
+    {
+      v += dNdx(e, iq, in, d) * qp.adv[d];
+    }
+    return v;
+  }
+
+  double gradDot(int e, int iq, int i, int j) const
+  {
+    double v = 0.0;
+    for (int d = 0; d < 2; ++d)
+    {
+      v += dNdx(e, iq, i, d) * dNdx(e, iq, j, d);
+    }
+    return v;
+  }
+
+  // Row `row` of K (next-state Jacobian) into K[9]; returns K nxt - F.
+  template <class S>
+  S evalRowT(int e, int row, const S* h0, const S* h1, const double* nxt, S* K) const
+  {
+    for (int col = 0; col < 9; ++col)
+    {
+      K[col] = 0.0;
+    }
+    const bool vel_row = row < 6;
+    const int  i       = vel_row ? row / 2 : row - 6;
+    const int  c       = vel_row ? row - 2 * i : 0;
+    S          F       = 0.0;
+    for (int iq = 0; iq < q->nq; ++iq)
+    {
+      NsQp<S> qp;
+      evalQp(e, iq, h0, h1, qp);
+      const double Jw  = JxW(e, iq);
+      const double Ni  = N(iq, i);
+      const S      dvi = advDeriv(qp, e, iq, i);
+      if (vel_row)
+      {
+        S grad_u = 0.0;
+        for (int d = 0; d < 2; ++d)
+        {
+          grad_u += dNdx(e, iq, i, d) * qp.grad[c][d];
+        }
+        F += (rho / dt * Ni * qp.u[c] - 0.5 * rho * Ni * qp.adv_grad[c] - 0.5 * mu * grad_u
+              + qp.tau * rho / dt * dvi * qp.u[c] - 0.5 * qp.tau * rho * dvi * qp.adv_grad[c])
+             * Jw;
+        for (int j = 0; j < 3; ++j)
+        {
+          const double Nj  = N(iq, j);
+          const S      dvj = advDeriv(qp, e, iq, j);
+          K[2 * j + c] += (rho / dt * Ni * Nj + 0.5 * rho * Ni * dvj
+                           + 0.5 * mu * gradDot(e, iq, i, j) + qp.tau * rho / dt * dvi * Nj
+                           + 0.5 * qp.tau * rho * dvi * dvj)
+                          * Jw;
+          K[6 + j] += (-dNdx(e, iq, i, c) * Nj + qp.tau * dvi * dNdx(e, iq, j, c)) * Jw;
+        }
+      }
+      else
+      {
+        S div_u = 0.0, div_adv = 0.0;
+        for (int d = 0; d < 2; ++d)
+        {
+          const double g = dNdx(e, iq, i, d);
+          div_u += g * qp.u[d];
+          div_adv += g * qp.adv_grad[d];
+        }
+        F += (qp.tau / dt * div_u - 0.5 * qp.tau * div_adv) * Jw;
+        for (int j = 0; j < 3; ++j)
+        {
+          const double Nj  = N(iq, j);
+          const S      dvj = advDeriv(qp, e, iq, j);
+          for (int d = 0; d < 2; ++d)
+          {
+            const double gi = dNdx(e, iq, i, d);
+            K[2 * j + d] += (Ni * dNdx(e, iq, j, d) + qp.tau / dt * gi * Nj
+                             + 0.5 * qp.tau * gi * dvj)
+                            * Jw;
+          }
+          K[6 + j] += qp.tau / rho * gradDot(e, iq, i, j) * Jw;
+        }
+      }
+    }
+    S out = -F;
+    for (int col = 0; col < 9; ++col)
+    {
+      out += K[col] * nxt[col];
+    }
+    return out;
+  }
+};
+
 } // namespace
 
 extern "C" {
@@ -1134,6 +1373,94 @@ int orc_assemble_p1_range(const void* mh, const void* qh, const int* conn,
             "Geometry and AssemblyMap have different element counts");
     const KappaPoissonP1 op{&q, conn, kappa, f_nodal};
     assembleLoop(m, op, u, res, vals, e0, e1);
+  });
+}
+
+
+int orc_assemble_navier(const void* mh, const void* qh, double rho, double mu, double dt,
+                        int step, int num_hist, const double* hist, const double* nxt,
+                        double* res, double* vals)
+{
+  return guarded([&] {
+    const Map&    m = *static_cast<const Map*>(mh);
+    const P1Quad& q = *static_cast<const P1Quad*>(qh);
+    require(q.ne == m.num_elems, "Geometry and AssemblyMap have different element counts");
+    require(m.max_res <= 9 && m.max_state <= 9,
+            "Navier operator expects nine DOFs per P1 triangle");
+    require(num_hist > 0, "Time assembly state dimensions do not match AssemblyMap");
+    const NavierGLS op{&q, rho, mu, dt, step, num_hist};
+    std::fill(res, res + m.num_res, 0.0);
+    if (vals != nullptr)
+    {
+      std::fill(vals, vals + m.row_ptr[m.num_res], 0.0);
+    }
+    double h0[9], h1[9], xn[9], K[9];
+    for (int e = 0; e < m.num_elems; ++e)
+    {
+      for (int c = 0; c < 9; ++c)
+      {
+        const int dof = m.state_dofs[m.state_offsets[e] + c];
+        h0[c]         = hist[dof];
+        h1[c]         = num_hist > 1 ? hist[std::size_t(m.num_states) + dof] : 0.0;
+        xn[c]         = nxt[dof];
+      }
+      for (int r = 0; r < 9; ++r)
+      {
+        const double rr = op.evalRowT<double>(e, r, h0, h1, xn, K);
+        res[m.res_dofs[m.res_offsets[e] + r]] += rr;
+        if (vals != nullptr)
+        {
+          for (int c = 0; c < 9; ++c)
+          {
+            vals[m.jac_map[m.jac_offsets[e] + 9 * r + c]] += K[c];
+          }
+        }
+      }
+    }
+  });
+}
+
+int orc_vjp_navier_hist(const void* mh, const void* qh, double rho, double mu, double dt,
+                        int step, int num_hist, const double* hist, const double* nxt,
+                        const double* adj, double* out)
+{
+  return guarded([&] {
+    const Map&    m = *static_cast<const Map*>(mh);
+    const P1Quad& q = *static_cast<const P1Quad*>(qh);
+    require(q.ne == m.num_elems, "Geometry and AssemblyMap have different element counts");
+    require(num_hist > 0, "Time assembly state dimensions do not match AssemblyMap");
+    const NavierGLS op{&q, rho, mu, dt, step, num_hist};
+    std::fill(out, out + std::size_t(num_hist) * m.num_states, 0.0);
+    double xn[9], a[9];
+    Dual   h0[9], h1[9], K[9];
+    for (int e = 0; e < m.num_elems; ++e)
+    {
+      int dofs[9];
+      for (int c = 0; c < 9; ++c)
+      {
+        dofs[c] = m.state_dofs[m.state_offsets[e] + c];
+        xn[c]   = nxt[dofs[c]];
+        a[c]    = adj[m.res_dofs[m.res_offsets[e] + c]];
+      }
+      for (int lag = 0; lag < std::min(num_hist, 2); ++lag)
+      {
+        for (int k = 0; k < 9; ++k)
+        {
+          for (int c = 0; c < 9; ++c)
+          {
+            h0[c] = Dual(hist[dofs[c]], lag == 0 && c == k ? 1.0 : 0.0);
+            h1[c] = Dual(num_hist > 1 ? hist[std::size_t(m.num_states) + dofs[c]] : 0.0,
+                         lag == 1 && c == k ? 1.0 : 0.0);
+          }
+          double g = 0.0;
+          for (int r = 0; r < 9; ++r)
+          {
+            g += a[r] * op.evalRowT<Dual>(e, r, h0, h1, xn, K).d;
+          }
+          out[std::size_t(lag) * m.num_states + dofs[k]] += g;
+        }
+      }
+    }
   });
 }
 

@@ -131,6 +131,22 @@ int orc_assemble_p1_range(const void* map, const void* quad, const int* conn,
                           const double* u, double* res, double* vals,
                           int elem_begin, int elem_end);
 
+/* femx's equal-order GLS Navier-Stokes time operator on P1 triangles
+ * (NavierOperator, femx/model/ns/Components.hpp:397-577) through the
+ * generic time loop with wrt = NextState (Assembly.hpp:235-303): res =
+ * K(hist) nxt - F(hist), vals = K. `quad` is an order-2 orc_p1_quad (femx's
+ * makeNavierData); hist is lag-major with num_states values per lag, lag 0
+ * the current state; vals may be null. */
+int orc_assemble_navier(const void* map, const void* quad, double rho, double mu,
+                        double dt, int step, int num_hist, const double* hist,
+                        const double* nxt, double* res, double* vals);
+/* out[lag][dof] = d/d hist[lag][dof] of sum_rows adj . R (femx's history
+ * VJP, Components.cpp:67-125, there by Enzyme), here by forward-mode dual
+ * numbers per history entry: exact to rounding, for testing. */
+int orc_vjp_navier_hist(const void* map, const void* quad, double rho, double mu,
+                        double dt, int step, int num_hist, const double* hist,
+                        const double* nxt, const double* adj, double* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -67,6 +67,8 @@ def lib():
         L.orc_th_quad_create.argtypes = [C.c_int, _f64p, C.c_int, _i32p]
         L.orc_th_quad_free.argtypes = [C.c_void_p]
         L.orc_assemble_th_range.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int, C.c_int]
+        L.orc_assemble_navier.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _f64p, _f64p, _f64p, C.c_void_p]
+        L.orc_vjp_navier_hist.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _f64p, _f64p, _f64p, _f64p]
         L.orc_assemble_th_threads.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int]
         L.orc_assemble_p1_range.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, C.c_void_p, _f64p, _f64p, _f64p, C.c_int, C.c_int]
         _lib = L
@@ -282,3 +284,23 @@ def assemble_p1_range(amap: AssemblyMap, quad: P1Quad, kappa, f_nodal, u, elem_b
     _check(lib().orc_assemble_p1_range(amap.h, quad.h, quad.conn, _f64(kappa), _ptr(f), _f64(u),
                                        res, vals, int(elem_begin), int(elem_end)))
     return res, vals
+
+
+def assemble_navier(amap: AssemblyMap, quad: P1Quad, rho, mu, dt, step, hist, nxt,
+                    num_hist=2, jac=True):
+    """femx's GLS NS time operator (order-2 P1Quad): (res, vals or None)."""
+    res = np.zeros(amap.num_res)
+    vals = np.zeros(amap.nnz) if jac else None
+    _check(lib().orc_assemble_navier(amap.h, quad.h, float(rho), float(mu), float(dt), int(step),
+                                     int(num_hist), _f64(hist), _f64(nxt), res,
+                                     None if vals is None else vals.ctypes.data))
+    return res, vals
+
+
+def vjp_navier_hist(amap: AssemblyMap, quad: P1Quad, rho, mu, dt, step, hist, nxt, adj,
+                    num_hist=2):
+    """Exact history VJP (dual numbers): [num_hist * num_states]."""
+    out = np.zeros(num_hist * amap.num_states)
+    _check(lib().orc_vjp_navier_hist(amap.h, quad.h, float(rho), float(mu), float(dt), int(step),
+                                     int(num_hist), _f64(hist), _f64(nxt), _f64(adj), out))
+    return out

@@ -9,7 +9,11 @@
 // so that the reference's own assemble, AssemblyMap, DirichletBC, BoundaryMap,
 // MatrixHandler and ReducedFunctional produce the numbers.
 //
-// Usage: ref_driver <kind> <case_dir>, kind in {kat, p1, th, inverse}.
+// kind "navier" runs femx's own equal-order GLS Navier-Stokes time operator
+// (femx/model/ns/Components.hpp:397-577) unchanged, with femx's
+// makeNavierData on a P1 triangle mesh and femx's mixed-space DOF layout.
+//
+// Usage: ref_driver <kind> <case_dir>, kind in {kat, p1, th, inverse, navier}.
 // Inputs and outputs are raw little-endian arrays named <name>.bin in
 // case_dir; scalar parameters are read from params.txt ("key value" lines).
 
@@ -39,6 +43,8 @@
 #include <femx/inverse/ReducedFunctional.hpp>
 #include <femx/linalg/handler/MatrixHandler.hpp>
 #include <femx/linalg/native/DenseLinearSolver.hpp>
+#include <femx/fem/MixedFESpace.hpp>
+#include <femx/model/ns/Components.hpp>
 #include <femx/state/Residual.hpp>
 #include <femx/state/StateSolver.hpp>
 
@@ -762,11 +768,70 @@ void runInverse()
 
 } // namespace
 
+// femx's NS time step operator on P1 triangles (velocity + pressure, equal
+// order; order-2 quadrature as NavierStokesModel.cpp:34). Inputs: coords,
+// conn, hist (2 lags x num_dofs, lag-major), nxt; params rho, mu, dt, step.
+// Outputs: the mixed-space element DOF tables, the CSR map, res and the
+// next-state Jacobian from the reference's time assemble
+// (Assembly.hpp:235-303).
+void runNavier()
+{
+  auto       p      = readParams();
+  const auto coords = readBin<double>("coords");
+  const auto conn   = readBin<int>("conn");
+  const auto hist   = readBin<double>("hist");
+  const auto nxt    = readBin<double>("nxt");
+
+  fem::Mesh               mesh = triMesh(coords, conn, 3);
+  fem::LagrangeTriangleP1 fe;
+  fem::FESpace            u_space(&mesh, &fe, 2);
+  fem::FESpace            p_space(&mesh, &fe);
+  fem::MixedFESpace       space;
+  space.addField(u_space);
+  space.addField(p_space);
+  space.setup();
+  u_space.setup();
+  const auto map  = assembly::makeAssemblyMap(fem::DofLayout(space));
+  const auto data = model::ns::makeNavierData(
+      u_space, fem::GaussQuadrature::make(fe.referenceElement(), 2));
+  const model::ns::NavierOperator<MemorySpace::Host> op(
+      data.view(), model::ns::KernelFluid{p["rho"], p["mu"]}, p["dt"]);
+
+  HostVector hv(static_cast<Index>(hist.size())), nv(static_cast<Index>(nxt.size()));
+  for (std::size_t i = 0; i < hist.size(); ++i)
+  {
+    hv[Index(i)] = hist[i];
+  }
+  for (std::size_t i = 0; i < nxt.size(); ++i)
+  {
+    nv[Index(i)] = nxt[i];
+  }
+  HostCsrMatrix jac(map.pattern());
+  HostVector    res;
+  CpuContext    ctx;
+  const Index   step = static_cast<Index>(p["step"]);
+  const auto    t0   = std::chrono::steady_clock::now();
+  assembly::assemble(op, step, 2, state::VariableBlock::NextState, map, hv, nv, res, jac, ctx);
+  const auto t1 = std::chrono::steady_clock::now();
+  std::printf("assemble_seconds %.6f\n", std::chrono::duration<double>(t1 - t0).count());
+
+  const auto v = map.view();
+  writeBin("res_offsets", v.res_offsets, std::size_t(map.numElems() + 1));
+  writeBin("res_dofs", v.res_dofs, std::size_t(v.res_offsets[map.numElems()]));
+  writeBin("state_offsets", v.state_offsets, std::size_t(map.numElems() + 1));
+  writeBin("state_dofs", v.state_dofs, std::size_t(v.state_offsets[map.numElems()]));
+  writeMap(map);
+  writeVec("res", res);
+  writeVec("vals", jac.vals());
+  const Index nd = space.numDofs();
+  writeBin("num_dofs", &nd, 1);
+}
+
 int main(int argc, char** argv)
 {
   if (argc != 3)
   {
-    std::cerr << "usage: ref_driver <kat|p1|th|inverse> <case_dir>\n";
+    std::cerr << "usage: ref_driver <kat|p1|th|inverse|navier> <case_dir>\n";
     return 2;
   }
   const std::string kind = argv[1];
@@ -788,6 +853,10 @@ int main(int argc, char** argv)
     else if (kind == "inverse")
     {
       runInverse();
+    }
+    else if (kind == "navier")
+    {
+      runNavier();
     }
     else
     {

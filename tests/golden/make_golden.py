@@ -17,6 +17,13 @@ Cases
   th_jit3      3x3 jittered, permuted Taylor-Hood mesh, nu = 1e-3
   inverse_12   12x12 Poisson inverse: femx ReducedFunctional gradient with
                DenseLinearSolver, misfit 0.5|u - d|^2, kappa = exp(m)
+  ns_gls_*     femx's own equal-order GLS Navier-Stokes time operator
+               (NavierOperator, CN + AB2) on P1 triangles through femx's time
+               assemble: 5x5 jittered permuted mesh at step 0 (no AB2) and
+               step 3 (AB2 advection), and a fluid at rest (zero velocity
+               history: the elemLength fallback direction)
+
+    python tests/golden/make_golden.py --only ns_gls   # one family of cases
 """
 from __future__ import annotations
 
@@ -142,12 +149,56 @@ def case_inverse(tmp, nx, seed):
                 u=read(d2, "u", np.float64))
 
 
+def case_navier(tmp, name, coords, conn, rho, mu, dt, step, seed, still=False):
+    d = os.path.join(tmp, name)
+    os.makedirs(d, exist_ok=True)
+    n = coords.shape[0]
+    nd = 3 * n
+    rng = np.random.default_rng(seed)
+    hist = rng.standard_normal(2 * nd)
+    if still:
+        hist[: 2 * n] = 0.0  # velocity of the current state (lag 0) at rest
+    nxt = rng.standard_normal(nd)
+    write(d, "coords", coords.astype(np.float64))
+    write(d, "conn", conn.astype(np.int32))
+    write(d, "hist", hist)
+    write(d, "nxt", nxt)
+    run("navier", d, {"rho": rho, "mu": mu, "dt": dt, "step": step})
+    out = {"coords": coords, "conn": conn, "hist": hist, "nxt": nxt,
+           "rho": np.array([rho]), "mu": np.array([mu]), "dt": np.array([dt]),
+           "step": np.array([step])}
+    for k in ("res_offsets", "res_dofs", "state_offsets", "state_dofs", "row_ptr", "col_ind",
+              "jac_offsets", "jac_map", "num_dofs"):
+        out[k] = read(d, k, np.int32)
+    for k in ("res", "vals"):
+        out[k] = read(d, k, np.float64)
+    assert int(out["num_dofs"][0]) == nd
+    return out
+
+
+def navier_cases(tmp):
+    coords, conn = meshes.jittered_tri(5, seed=31, permute=True)
+    np.savez_compressed(os.path.join(HERE, "ns_gls_jit5_s0.npz"),
+                        **case_navier(tmp, "ns_s0", coords, conn, 1.0, 1e-2, 0.05, 0, 41))
+    np.savez_compressed(os.path.join(HERE, "ns_gls_jit5_s3.npz"),
+                        **case_navier(tmp, "ns_s3", coords, conn, 1.2, 5e-3, 0.02, 3, 42))
+    c2, k2 = meshes.structured_tri(4)
+    np.savez_compressed(os.path.join(HERE, "ns_gls_still4.npz"),
+                        **case_navier(tmp, "ns_still", c2, k2, 1.0, 1e-3, 0.1, 2, 43, still=True))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--only", default="", help="generate one family: ns_gls")
     args = ap.parse_args()
     build(args.ref)
+    if args.only == "ns_gls":
+        with tempfile.TemporaryDirectory() as tmp:
+            navier_cases(tmp)
+        return
     with tempfile.TemporaryDirectory() as tmp:
+        navier_cases(tmp)
         np.savez_compressed(os.path.join(HERE, "kat.npz"), **case_kat(tmp))
 
         coords, conn = meshes.structured_tri(32)
