@@ -32,7 +32,7 @@ __all__ = [
     "makeAssemblyMap", "makeAssemblyMapFromElems", "makeBoundaryMap",
     "replaceRows", "replaceRes", "zeroBoundary", "prepareForwardSolve",
     "assembleP1Kappa", "vjpP1Kappa", "assembleTaylorHood", "matvec", "matvecT",
-    "axpby", "transpose", "vjpTaylorHood", "PRECISIONS",
+    "axpby", "transpose", "vjpTaylorHood", "assembleNavier", "vjpNavierHist", "PRECISIONS",
 ]
 
 PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32_quad": _lib.PREC_FP32_QUAD,
@@ -355,6 +355,35 @@ def vjpTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, lam, g_state,
     g_state = _check_vec(g_state, amap.numStates(), "VJP output")
     call("gbfem_vjp_th_ns", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn6),
          float(nu), _ptr(state), _ptr(lam), _ptr(g_state), PRECISIONS[precision], _stream())
+
+
+def assembleNavier(amap: AssemblyMap, coords, conn, rho, mu, dt, step, hist, nxt, res,
+                   jac=None, num_hist: int = 2):
+    """femx's GLS Navier-Stokes time step (NavierOperator) on P1 triangles:
+    res = K(hist) nxt - F(hist) and, with jac, K (next-state Jacobian).
+    hist is lag-major [num_hist * numStates()], lag 0 the current state."""
+    coords = _dev(coords, torch.float64, "coords")
+    conn = _dev(conn, torch.int32, "conn")
+    hist = _check_vec(hist, num_hist * amap.numStates(), "history")
+    nxt = _check_vec(nxt, amap.numStates(), "next state")
+    res = _check_vec(res, amap.numRes(), "residual")
+    call("gbfem_assemble_navier", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
+         float(rho), float(mu), float(dt), int(step), int(num_hist), _ptr(hist), _ptr(nxt),
+         _ptr(res), _jac_ptr(amap, jac), _stream())
+
+
+def vjpNavierHist(amap: AssemblyMap, coords, conn, rho, mu, dt, step, hist, nxt, adj, out,
+                  num_hist: int = 2):
+    """out = d(adj . R)/d hist for femx's NS time operator (both lags)."""
+    coords = _dev(coords, torch.float64, "coords")
+    conn = _dev(conn, torch.int32, "conn")
+    hist = _check_vec(hist, num_hist * amap.numStates(), "history")
+    nxt = _check_vec(nxt, amap.numStates(), "next state")
+    adj = _check_vec(adj, amap.numRes(), "adjoint")
+    out = _check_vec(out, num_hist * amap.numStates(), "VJP output")
+    call("gbfem_vjp_navier_hist", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
+         float(rho), float(mu), float(dt), int(step), int(num_hist), _ptr(hist), _ptr(nxt),
+         _ptr(adj), _ptr(out), _stream())
 
 
 def matvec(mat: CsrMatrix, x, y, alpha: float = 1.0, beta: float = 0.0):

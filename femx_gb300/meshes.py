@@ -147,6 +147,20 @@ def th_elem_dofs(conn6: np.ndarray, num_p2_nodes: int):
     return offsets, np.ascontiguousarray(d.reshape(-1), dtype=np.int32), nd
 
 
+def navier_elem_dofs(conn: np.ndarray, num_nodes: int):
+    """Equal-order P1/P1 element DOFs of femx's NS model (MixedFESpace of a
+    2-component velocity field and a pressure field, Helper.cpp:40-50):
+    velocity dof = 2*node + comp at local 2*a + comp, pressure dof =
+    2*num_nodes + node at local 6 + a. Returns (offsets, dofs, num_dofs)."""
+    e = conn.shape[0]
+    d = np.empty((e, 9), dtype=np.int64)
+    d[:, 0:6:2] = 2 * conn
+    d[:, 1:6:2] = 2 * conn + 1
+    d[:, 6:9] = 2 * num_nodes + conn
+    offsets = (np.arange(e + 1, dtype=np.int64) * 9).astype(np.int32)
+    return offsets, np.ascontiguousarray(d.reshape(-1), dtype=np.int32), 3 * num_nodes
+
+
 def boundary_nodes(coords: np.ndarray, tol: float = 1e-12) -> np.ndarray:
     x, y = coords[:, 0], coords[:, 1]
     return (np.abs(x) < tol) | (np.abs(x - 1) < tol) | (np.abs(y) < tol) | (np.abs(y - 1) < tol)

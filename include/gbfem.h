@@ -256,6 +256,34 @@ GBFEM_API int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
                               int precision, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * femx's NS time operator — the equal-order GLS Navier-Stokes step of
+ * NavierOperator (femx/model/ns/Components.hpp:330-577) on P1 triangles,
+ * assembled like femx's time assemble with wrt = NextState
+ * (Assembly.hpp:235-303, CudaAssembly.hpp:367-413, the kernel
+ * assembleTimeKernel): res = K(hist) nxt - F(hist), vals = K (the
+ * next-state Jacobian; null for the residual alone, assembleResidual
+ * CudaAssembly.hpp:420-472). Crank-Nicolson with AB2 advection at step > 0
+ * when num_hist > 1; GLS tau with femx's streamline element length.
+ * Local DOFs in femx's mixed layout: velocity (node, comp) then pressure
+ * (9 per element); conn = the 3 vertices; hist lag-major (num_hist x
+ * num_states, lag 0 = current state). FP64.
+ * gbfem_vjp_navier_hist: out[lag][dof] = d(adj . R)/d hist[lag][dof] — the
+ * history VJP femx obtains from Enzyme (histVjp / histVjpKernel,
+ * Components.cpp:67-125, Components.cu:25-98), here reverse mode written
+ * out by hand; out (num_hist x num_states) is overwritten.
+ * ------------------------------------------------------------------------ */
+GBFEM_API int gbfem_assemble_navier(const gbfem_assembly_map* map, int num_nodes,
+                                    const double* coords, const int* conn, double rho,
+                                    double mu, double dt, int step, int num_hist,
+                                    const double* hist, const double* nxt, double* res,
+                                    double* vals, void* stream);
+GBFEM_API int gbfem_vjp_navier_hist(const gbfem_assembly_map* map, int num_nodes,
+                                    const double* coords, const int* conn, double rho,
+                                    double mu, double dt, int step, int num_hist,
+                                    const double* hist, const double* nxt, const double* adj,
+                                    double* out, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Batched assembly: many independent instances (meshes of uneven size, P1
  * Poisson and Taylor-Hood NS mixed) assembled by one persistent launch.
  * Each instance is the work of one gbfem_assemble_p1_kappa /
