@@ -17,6 +17,10 @@ Sub-results in the same line:
                  grads/s (one gradient = both VJPs once)
   poisson        P1 Poisson 1024x1024 FP64: assembly + rhs = -res +
                  prepareForwardSolve + 10 SpMVs, elements/s
+  navier         femx's own GLS Navier-Stokes time operator (CN + AB2) on
+                 the 256x256 P1 triangulation: residual + next-state
+                 Jacobian, and the history VJP, elements/s, with the oracle
+                 (femx's operator restated) on every host core beside it
 Inputs are seeded synthetic fields with the configured shapes (no dataset).
 Timing: CUDA events on the launch stream, 512 MB L2 flush before each step
 (outside the events), warm-up steps untimed. e2e: same step through the
@@ -45,6 +49,7 @@ METRIC = "NS P2/P1 Jacobian elems/s & VJP grads/s vs plain FP64 GPU path at stat
 TH_NX, NU = 256, 1.0e-3
 VJP_NX = 512
 POISSON_NX, NSPMV, SPMV_SCALE = 1024, 10, 0.125
+NS_NX = 256
 
 
 def peaks():
@@ -246,7 +251,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--only", default="", help="run one workload: th, th64, vjp, poisson")
+    ap.add_argument("--only", default="",
+                    help="run one workload: th, th64, vjp, poisson, navier, batch")
     ap.add_argument("--soak", type=float, default=1.0,
                     help="seconds of untimed headline steps before timing (clock sampling)")
     args = ap.parse_args()
@@ -589,6 +595,68 @@ def main():
                               if t_lib is not None else {"unavailable": lib_err}),
         }
         del amap, bc, jac
+
+    # ---------------- femx's GLS NS time operator (P1/P1, 256x256) ----------
+    if only in ("", "navier"):
+        from femx_gb300 import meshes
+        c2, k2 = meshes.structured_tri(NS_NX)
+        nn, e = c2.shape[0], k2.shape[0]
+        offs, dofs, nd = meshes.navier_elem_dofs(k2, nn)
+        rng = np.random.default_rng(6)
+        hist_h = np.concatenate([meshes.stream_velocity(c2, seed=6).reshape(-1),
+                                 rng.standard_normal(nn),
+                                 meshes.stream_velocity(c2, seed=7).reshape(-1),
+                                 rng.standard_normal(nn)])
+        nxt_h = hist_h[:nd] + 1e-2 * rng.standard_normal(nd)
+        adj_h = rng.standard_normal(nd)
+        prm = (1.0, 1.0e-3, 1.0e-2, 2)  # rho, mu (Re 1000), dt, step (AB2 on)
+        amap = A.makeAssemblyMap(nd, nd, d(offs), d(dofs), d(offs), d(dofs))
+        coords, conn = d(c2), d(k2)
+        hist, nxt, adj = d(hist_h), d(nxt_h), d(adj_h)
+        res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        jac = A.CsrMatrix(amap.pattern())
+        g_hist = torch.zeros(2 * nd, dtype=torch.float64, device="cuda")
+
+        def ns_asm():
+            A.assembleNavier(amap, coords, conn, *prm, hist, nxt, res, jac)
+
+        def ns_vjp():
+            A.vjpNavierHist(amap, coords, conn, *prm, hist, nxt, adj, g_hist)
+
+        t_asm = maxrank(timer.run(ns_asm, args.steps, args.warmup))
+        t_vjp = maxrank(timer.run(ns_vjp, args.steps, args.warmup))
+        launches += 2 * args.steps
+        ns_asm()
+        amap.check()
+        entry = {
+            "workload": f"femx_gls_navier_stokes_p1p1_{NS_NX}x{NS_NX}_cn_ab2_step",
+            "elements": e, "dofs": nd, "nnz": amap.pattern().nnz,
+            "operator": "femx NavierOperator (equal-order GLS, CN + AB2), FP64",
+            "assemble_next": {"elements_per_s": world * e / t_asm, "ms": t_asm * 1e3},
+            "history_vjp": {"elements_per_s": world * e / t_vjp, "ms": t_vjp * 1e3,
+                            "note": "femx computes this with Enzyme; reverse mode by hand here"},
+        }
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            from oracle import pyoracle as orc
+            om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+            q = orc.P1Quad(c2, k2, order=2)
+            cores = host_cores()
+            r_o, v_o = np.zeros(nd), np.zeros(om.nnz)
+            n_s, tot = 0, 0.0
+            while tot < 6.0 and n_s < 10:
+                t0 = time.perf_counter()
+                orc.assemble_navier_threads(om, q, *prm, hist_h, nxt_h, cores, res=r_o, vals=v_o)
+                tot += time.perf_counter() - t0
+                n_s += 1
+            entry["cpu_baseline"] = {
+                "elements_per_s": e * n_s / tot, "cores": cores, "kind": "port",
+                "sample": f"{n_s} full assemblies (oracle restatement of femx's NavierOperator, "
+                          f"bit-identical to the reference on the golden cases; atomic adds)"}
+            entry["rel_err_vs_oracle_full_size"] = {
+                "residual": float(np.abs(res.cpu().numpy() - r_o).max() / np.abs(r_o).max()),
+                "jacobian": float(np.abs(jac.vals.cpu().numpy() - v_o).max() / np.abs(v_o).max())}
+        line["navier"] = entry
+        del amap, jac
 
     # ---------------- batched uneven instances (config 5) ----------------
     if only in ("", "batch"):

@@ -108,8 +108,8 @@ SIGNATURES = {
     "gbfem_vjp_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
     "gbfem_vjp_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
-    "gbfem_assemble_navier": (_i, [_vp, _i, _vp, _vp, _d, _d, _d, _i, _i, _vp, _vp, _vp, _vp,
-                                   _vp]),
+    "gbfem_assemble_navier": (_i, [_vp, _i, _vp, _vp, _d, _d, _d, _i, _i, _i, _vp, _vp, _vp,
+                                   _vp, _vp]),
     "gbfem_vjp_navier_hist": (_i, [_vp, _i, _vp, _vp, _d, _d, _d, _i, _i, _vp, _vp, _vp, _vp,
                                    _vp]),
     "gbfem_probe_fp64_fma": (_i, [_i, _i, _i, _vp, _vp]),

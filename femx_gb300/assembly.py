@@ -358,9 +358,10 @@ def vjpTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, lam, g_state,
 
 
 def assembleNavier(amap: AssemblyMap, coords, conn, rho, mu, dt, step, hist, nxt, res,
-                   jac=None, num_hist: int = 2):
+                   jac=None, num_hist: int = 2, wrt_hist_lag: int = -1):
     """femx's GLS Navier-Stokes time step (NavierOperator) on P1 triangles:
-    res = K(hist) nxt - F(hist) and, with jac, K (next-state Jacobian).
+    res = K(hist) nxt - F(hist) and, with jac, the Jacobian block wrt
+    (-1: next state, K; a history lag: zero, as femx's operator).
     hist is lag-major [num_hist * numStates()], lag 0 the current state."""
     coords = _dev(coords, torch.float64, "coords")
     conn = _dev(conn, torch.int32, "conn")
@@ -368,8 +369,8 @@ def assembleNavier(amap: AssemblyMap, coords, conn, rho, mu, dt, step, hist, nxt
     nxt = _check_vec(nxt, amap.numStates(), "next state")
     res = _check_vec(res, amap.numRes(), "residual")
     call("gbfem_assemble_navier", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
-         float(rho), float(mu), float(dt), int(step), int(num_hist), _ptr(hist), _ptr(nxt),
-         _ptr(res), _jac_ptr(amap, jac), _stream())
+         float(rho), float(mu), float(dt), int(step), int(num_hist), int(wrt_hist_lag),
+         _ptr(hist), _ptr(nxt), _ptr(res), _jac_ptr(amap, jac), _stream())
 
 
 def vjpNavierHist(amap: AssemblyMap, coords, conn, rho, mu, dt, step, hist, nxt, adj, out,

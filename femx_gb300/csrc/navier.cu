@@ -11,17 +11,25 @@
 // femx's streamline element length h. Local DOFs: velocity (node, comp) at
 // 2 node + comp, then pressure at 6 + node; order-2 rule (3 points).
 //
-// Layout (FP64 throughout: this is the drop-in): a 16-lane group owns one
-// element, 8 elements per 128-thread block. Lane 15 forms the geometry
-// (constant gradients of the affine P1 map, as ElementValues does), lanes
-// 0..2 evaluate the quadrature-point state once per element (femx repeats
-// it for every row), lanes 0..8 produce the nine rows, and the block is
-// added into CSR row-coalesced through the column-major in-row position map
-// (one FP64 reduction instruction per row). The history VJP is reverse mode
-// written out by hand (no Enzyme): per quadrature point the adjoint
-// contractions give dL/d(u, grad u, adv, tau), tau's dependence on u
-// (through |u| and the streamline length) is chained in, and lanes 0..11
-// scatter the velocity history entries of both lags.
+// GB300 formulation (FP64 throughout: this is the drop-in). The FP64 pipe is
+// the bound, so the element is factorised instead of evaluated row by row
+// (femx re-evaluates every quadrature point for every row): on the affine
+// triangle the shape gradients g_i and grad u^n are constant, and with
+//   s_i = N_i + tau dv_i,  phi_j = (2/dt) N_j + dv_j,  dv_i = adv . g_i,
+//   w_c = u_c/dt - ag_c/2  (ag = (adv . grad) u^n)
+// every block of the element matrix is a short sum over the 3 points:
+//   K(ic,jc)  = sum_q Jw [rho/2 s_i phi_j + mu/2 g_i.g_j]
+//   K(ic,pj)  = sum_q Jw [-g_i[c] N_j + tau dv_i g_j[c]]
+//   K(pi,jd)  = sum_q Jw [N_i g_j[d] + tau/2 g_i[d] phi_j]
+//   K(pi,pj)  = sum_q Jw tau/rho g_i.g_j
+//   F(ic)     = sum_q Jw [rho s_i w_c - mu/2 g_i . grad_c],  F(pi) = sum_q Jw tau g_i . w
+// — algebraically the terms of evalPhysicsRow, at about 450 FP64
+// operations per element. One thread owns one element (all 32 lanes busy);
+// it scatter-adds the 81 entries and 9 residual terms with FP64 reductions.
+// The history VJP is reverse mode written out by hand (no Enzyme): per point
+// the adjoint contractions give dL/d(u, grad u, adv, tau), tau's dependence
+// on u (through |u| and the streamline length) is chained in, and the 12
+// velocity history entries of both lags are reduced per element.
 #include "maps.cuh"
 
 namespace
@@ -29,11 +37,9 @@ namespace
 
 using gbfem::DeviceStatus;
 
-constexpr int kLanes    = 16;
-constexpr int kElems    = 8;
-constexpr int kThreads  = kLanes * kElems;
-constexpr int kQ        = 3;
-constexpr int kDofs     = 9;
+constexpr int kThreads = 128;
+constexpr int kQ       = 3;
+constexpr int kDofs    = 9;
 
 // order-2 rule points (GaussQuadrature.hpp:189-198) and P1 basis values there,
 // formed as femx forms them (N = 1 - r - s, r, s)
@@ -65,166 +71,111 @@ struct NsArgs
   DeviceStatus*        status;
 };
 
+// One element's inputs, geometry and the history-only per-element fields.
+struct NsElem
+{
+  int    dofs[kDofs];
+  double h0[6], an[6];   // lag-0 velocity, AB2 advection velocity at the nodes
+  double g[3][2];        // dN_i/dx_d, constant on the affine triangle
+  double jxw;            // |det| w, equal at the three points
+  double grad[2][2];     // grad u^n (constant)
+  bool   ab2;
+};
+
+// Geometry as ElementValues forms it (J = sum x dN^/dr, invJ, dN/dx).
+__device__ bool loadElement(const NsArgs& a, int e, NsElem& E)
+{
+  int n[3];
+  for (int k = 0; k < 3; ++k)
+  {
+    n[k] = a.conn[3 * e + k];
+    if (static_cast<unsigned>(n[k]) >= static_cast<unsigned>(a.num_nodes))
+    {
+      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+      return false;
+    }
+  }
+  const double2 x0 = a.coords[n[0]], x1 = a.coords[n[1]], x2 = a.coords[n[2]];
+  const double  J0 = x0.x * -1.0 + x1.x * 1.0 + x2.x * 0.0;
+  const double  J1 = x0.x * -1.0 + x1.x * 0.0 + x2.x * 1.0;
+  const double  J2 = x0.y * -1.0 + x1.y * 1.0 + x2.y * 0.0;
+  const double  J3 = x0.y * -1.0 + x1.y * 0.0 + x2.y * 1.0;
+  const double  det = J0 * J3 - J1 * J2;
+  if (!(fabs(det) >= 1.0e-30))
+  {
+    gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+    return false;
+  }
+  const double inv = 1.0 / det;
+  const double i0 = J3 * inv, i1 = -J1 * inv, i2 = -J2 * inv, i3 = J0 * inv;
+  // dN/dx_d = sum_b dN^/dr_b invJ[b][d], dN^/dr = (-1,-1), (1,0), (0,1)
+  E.g[0][0] = -i0 - i2;
+  E.g[0][1] = -i1 - i3;
+  E.g[1][0] = i0;
+  E.g[1][1] = i1;
+  E.g[2][0] = i2;
+  E.g[2][1] = i3;
+  E.jxw     = fabs(det) * kW;
+  for (int k = 0; k < kDofs; ++k)
+  {
+    E.dofs[k] = a.dofs[kDofs * e + k];
+  }
+  E.ab2 = a.step > 0 && a.num_hist > 1;
+  for (int k = 0; k < 6; ++k)
+  {
+    const double v = a.hist[E.dofs[k]];
+    E.h0[k]        = v;
+    E.an[k] = E.ab2 ? 1.5 * v - 0.5 * a.hist[static_cast<long long>(a.num_states) + E.dofs[k]]
+                    : v;
+  }
+  for (int c = 0; c < 2; ++c)
+  {
+    for (int d = 0; d < 2; ++d)
+    {
+      E.grad[c][d] = E.g[0][d] * E.h0[c] + E.g[1][d] * E.h0[2 + c] + E.g[2][d] * E.h0[4 + c];
+    }
+  }
+  return true;
+}
+
+// Point state: u, adv, ag = (adv . grad) u, tau and femx's streamline length
+// pieces (elemLength, Components.hpp:273-327; evalQp :330-395).
 struct NsQp
 {
-  double u[2], adv[2], grad[2][2], ag[2], tau;
-  // for the VJP: streamline length pieces
-  double speed, h, sum, dir[2];
+  double N[3], u[2], adv[2], ag[2], tau, speed, h, sum, dir[2];
   bool   fallback;
 };
 
-struct NsElem
+__device__ __forceinline__ void pointState(const NsArgs& a, const NsElem& E, int q, NsQp& P)
 {
-  double h0[16], h1[16], x[16], a[16];
-  double g[3][2]; // dN_in/dx_d (constant on the affine triangle)
-  double jxw;     // |det| * w, equal at the three points
-  int    ok;
-  NsQp   qp[kQ];
-};
-
-struct NsSmem
-{
-  NsElem el[kElems];
-  double kv[kElems][kDofs][kDofs + 1]; // staged rows (odd stride: no conflicts)
-  int    rs[kElems][16];
-};
-
-__device__ __forceinline__ double advDeriv(const NsElem& E, const NsQp& qp, int in)
-{
-  double v = 0.0;
-  for (int d = 0; d < 2; ++d)
+  for (int i = 0; i < 3; ++i)
   {
-    v += E.g[in][d] * qp.adv[d];
+    P.N[i] = basisN(q, i);
   }
-  return v;
-}
-
-// Gather + geometry (lane 15). Returns whether the element is live.
-__device__ bool stageElement(const NsArgs& a, NsElem& E, int e, int l, bool has, bool vjp)
-{
-  if (has && l < kDofs)
-  {
-    const int dof = a.dofs[kDofs * e + l];
-    E.h0[l]       = a.hist[dof];
-    E.h1[l]       = a.num_hist > 1 ? a.hist[static_cast<long long>(a.num_states) + dof] : 0.0;
-    E.x[l]        = a.nxt[dof];
-    if (vjp)
-    {
-      E.a[l] = a.adj[dof];
-    }
-  }
-  if (has && l == 15)
-  {
-    E.ok          = 0;
-    bool nodes_ok = true;
-    for (int k = 0; k < 3; ++k)
-    {
-      nodes_ok = nodes_ok
-                 && static_cast<unsigned>(a.conn[3 * e + k]) < static_cast<unsigned>(a.num_nodes);
-    }
-    if (!nodes_ok)
-    {
-      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
-    }
-    else
-    {
-      // ElementValues: J[a][b] = sum_in x_a(in) dN^_in/dr_b, invJ, dN/dx
-      const double2 x0 = a.coords[a.conn[3 * e + 0]];
-      const double2 x1 = a.coords[a.conn[3 * e + 1]];
-      const double2 x2 = a.coords[a.conn[3 * e + 2]];
-      double        J[4];
-      J[0] = x0.x * -1.0 + x1.x * 1.0 + x2.x * 0.0;
-      J[1] = x0.x * -1.0 + x1.x * 0.0 + x2.x * 1.0;
-      J[2] = x0.y * -1.0 + x1.y * 1.0 + x2.y * 0.0;
-      J[3] = x0.y * -1.0 + x1.y * 0.0 + x2.y * 1.0;
-      const double det = J[0] * J[3] - J[1] * J[2];
-      if (fabs(det) >= 1.0e-30)
-      {
-        const double inv     = 1.0 / det;
-        const double invJ[4] = {J[3] * inv, -J[1] * inv, -J[2] * inv, J[0] * inv};
-        const double dr[3][2] = {{-1.0, -1.0}, {1.0, 0.0}, {0.0, 1.0}};
-        for (int i = 0; i < 3; ++i)
-        {
-          for (int d = 0; d < 2; ++d)
-          {
-            double v = 0.0;
-            for (int b = 0; b < 2; ++b)
-            {
-              v += dr[i][b] * invJ[b * 2 + d];
-            }
-            E.g[i][d] = v;
-          }
-        }
-        E.jxw = fabs(det) * kW;
-        E.ok  = 1;
-      }
-      else
-      {
-        gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
-      }
-    }
-  }
-  __syncthreads();
-  return has && E.ok;
-}
-
-// evalQp + elemLength (Components.hpp:273-395) at point q.
-__device__ void evalQp(const NsArgs& a, NsElem& E, int q)
-{
-  NsQp& qp = E.qp[q];
   for (int c = 0; c < 2; ++c)
   {
-    qp.u[c] = qp.adv[c] = qp.ag[c] = 0.0;
-    qp.grad[c][0] = qp.grad[c][1] = 0.0;
+    P.u[c]   = P.N[0] * E.h0[c] + P.N[1] * E.h0[2 + c] + P.N[2] * E.h0[4 + c];
+    P.adv[c] = P.N[0] * E.an[c] + P.N[1] * E.an[2 + c] + P.N[2] * E.an[4 + c];
   }
-  const bool ab2 = a.step > 0 && a.num_hist > 1;
-  for (int in = 0; in < 3; ++in)
-  {
-    const double N = basisN(q, in);
-    for (int c = 0; c < 2; ++c)
-    {
-      const int    id = 2 * in + c;
-      const double v  = E.h0[id];
-      qp.u[c] += N * v;
-      for (int d = 0; d < 2; ++d)
-      {
-        qp.grad[c][d] += E.g[in][d] * v;
-      }
-      const double adv = ab2 ? 1.5 * v - 0.5 * E.h1[id] : v;
-      qp.adv[c] += N * adv;
-    }
-  }
-  double speed2 = 0.0;
   for (int c = 0; c < 2; ++c)
   {
-    speed2 += qp.u[c] * qp.u[c];
-    for (int d = 0; d < 2; ++d)
-    {
-      qp.ag[c] += qp.grad[c][d] * qp.adv[d];
-    }
+    P.ag[c] = E.grad[c][0] * P.adv[0] + E.grad[c][1] * P.adv[1];
   }
-  const double speed = sqrt(speed2);
-  // elemLength: streamline direction (or the diagonal at rest)
-  double     dir[2];
-  const bool fallback = !(speed > 1.0e-10);
-  if (!fallback)
+  const double speed = sqrt(P.u[0] * P.u[0] + P.u[1] * P.u[1]);
+  P.fallback         = !(speed > 1.0e-10);
+  if (!P.fallback)
   {
-    dir[0] = qp.u[0] / speed;
-    dir[1] = qp.u[1] / speed;
+    P.dir[0] = P.u[0] / speed;
+    P.dir[1] = P.u[1] / speed;
   }
   else
   {
-    dir[0] = dir[1] = 1.0 / sqrt(2.0);
+    P.dir[0] = P.dir[1] = 1.0 / sqrt(2.0);
   }
   double sum = 0.0;
-  for (int in = 0; in < 3; ++in)
+  for (int i = 0; i < 3; ++i)
   {
-    double gr = 0.0;
-    for (int d = 0; d < 2; ++d)
-    {
-      gr += dir[d] * E.g[in][d];
-    }
-    sum += gr >= 0.0 ? gr : -gr;
+    sum += fabs(P.dir[0] * E.g[i][0] + P.dir[1] * E.g[i][1]);
   }
   const double h    = sum > 1.0e-14 ? 2.0 / sum : 0.0;
   const double nu   = a.mu / a.rho;
@@ -235,274 +186,277 @@ __device__ void evalQp(const NsArgs& a, NsElem& E, int q)
     flow = (2.0 * speed / h) * (2.0 * speed / h);
     diff = (4.0 * nu / (h * h)) * (4.0 * nu / (h * h));
   }
-  qp.tau      = 1.0 / sqrt(time + flow + diff);
-  qp.speed    = speed;
-  qp.h        = h;
-  qp.sum      = sum;
-  qp.dir[0]   = dir[0];
-  qp.dir[1]   = dir[1];
-  qp.fallback = fallback;
+  P.tau   = 1.0 / sqrt(time + flow + diff);
+  P.speed = speed;
+  P.h     = h;
+  P.sum   = sum;
 }
 
-// Row `row` of K into K[9] and the residual K x - F
-// (NavierOperator::evalPhysicsRow, Components.hpp:473-575).
-__device__ double evalRow(const NsArgs& a, const NsElem& E, int row, double* K)
+__device__ __forceinline__ int csrSlot(const NsArgs& a, int e, const int* rs, int i, int j,
+                                       const uint4* pw)
 {
-  for (int col = 0; col < kDofs; ++col)
+  if (a.jac_pos != nullptr)
   {
-    K[col] = 0.0;
+    const unsigned w = (&pw[j].x)[i >> 2];
+    return rs[i] + static_cast<int>((w >> (8 * (i & 3))) & 0xffu);
   }
-  const bool   vel = row < 6;
-  const int    i   = vel ? row / 2 : row - 6;
-  const int    c   = vel ? row - 2 * i : 0;
-  const double rho = a.rho, mu = a.mu, dt = a.dt;
-  double       F   = 0.0;
-  for (int q = 0; q < kQ; ++q)
-  {
-    const NsQp&  qp  = E.qp[q];
-    const double Jw  = E.jxw;
-    const double Ni  = basisN(q, i);
-    const double dvi = advDeriv(E, qp, i);
-    if (vel)
-    {
-      double grad_u = 0.0;
-      for (int d = 0; d < 2; ++d)
-      {
-        grad_u += E.g[i][d] * qp.grad[c][d];
-      }
-      F += (rho / dt * Ni * qp.u[c] - 0.5 * rho * Ni * qp.ag[c] - 0.5 * mu * grad_u
-            + qp.tau * rho / dt * dvi * qp.u[c] - 0.5 * qp.tau * rho * dvi * qp.ag[c])
-           * Jw;
-      for (int j = 0; j < 3; ++j)
-      {
-        const double Nj  = basisN(q, j);
-        const double dvj = advDeriv(E, qp, j);
-        const double gd  = E.g[i][0] * E.g[j][0] + E.g[i][1] * E.g[j][1];
-        K[2 * j + c] += (rho / dt * Ni * Nj + 0.5 * rho * Ni * dvj + 0.5 * mu * gd
-                         + qp.tau * rho / dt * dvi * Nj + 0.5 * qp.tau * rho * dvi * dvj)
-                        * Jw;
-        K[6 + j] += (-E.g[i][c] * Nj + qp.tau * dvi * E.g[j][c]) * Jw;
-      }
-    }
-    else
-    {
-      double div_u = 0.0, div_adv = 0.0;
-      for (int d = 0; d < 2; ++d)
-      {
-        div_u += E.g[i][d] * qp.u[d];
-        div_adv += E.g[i][d] * qp.ag[d];
-      }
-      F += (qp.tau / dt * div_u - 0.5 * qp.tau * div_adv) * Jw;
-      for (int j = 0; j < 3; ++j)
-      {
-        const double Nj  = basisN(q, j);
-        const double dvj = advDeriv(E, qp, j);
-        for (int d = 0; d < 2; ++d)
-        {
-          const double gi = E.g[i][d];
-          K[2 * j + d] += (Ni * E.g[j][d] + qp.tau / dt * gi * Nj + 0.5 * qp.tau * gi * dvj) * Jw;
-        }
-        const double gd = E.g[i][0] * E.g[j][0] + E.g[i][1] * E.g[j][1];
-        K[6 + j] += qp.tau / rho * gd * Jw;
-      }
-    }
-  }
-  double out = -F;
-  for (int col = 0; col < kDofs; ++col)
-  {
-    out += K[col] * E.x[col];
-  }
-  return out;
+  return a.jac_map[81LL * e + kDofs * i + j];
 }
 
 template <bool kJac>
 __global__ void __launch_bounds__(kThreads) nsAssembleKernel(NsArgs a)
 {
-  __shared__ NsSmem sm;
-  const int  l   = threadIdx.x & (kLanes - 1);
-  const int  le  = threadIdx.x / kLanes;
-  const int  e   = blockIdx.x * kElems + le;
-  const bool has = e < a.ne;
-  NsElem&    E   = sm.el[le];
-  const bool live = stageElement(a, E, e, l, has, false);
-  if (live && l < kQ)
+  const int e = blockIdx.x * kThreads + threadIdx.x;
+  if (e >= a.ne)
   {
-    evalQp(a, E, l);
+    return;
   }
-  __syncthreads();
-  if (live && l < kDofs)
+  NsElem E;
+  if (!loadElement(a, e, E))
   {
-    double    K[kDofs];
-    const double r   = evalRow(a, E, l, K);
-    const int    dof = a.dofs[kDofs * e + l];
-    gbfem::redAdd(a.res + dof, r);
-    if (kJac)
+    return; // reported through the status word; the element adds nothing
+  }
+  const double rho = a.rho, mu = a.mu, dt = a.dt;
+  double       Ss[3][3] = {}, T[3] = {}, Pj[3] = {}, Fv[3][2] = {}, V[2] = {}, Tt = 0.0;
+  double       Nsum[3] = {};
+  for (int q = 0; q < kQ; ++q)
+  {
+    NsQp P;
+    pointState(a, E, q, P);
+    double dv[3], s[3], phi[3];
+    for (int i = 0; i < 3; ++i)
     {
-      for (int col = 0; col < kDofs; ++col)
-      {
-        sm.kv[le][l][col] = K[col];
-      }
-      sm.rs[le][l] = a.row_ptr[dof];
+      dv[i]  = E.g[i][0] * P.adv[0] + E.g[i][1] * P.adv[1];
+      s[i]   = P.N[i] + P.tau * dv[i];
+      phi[i] = (2.0 / dt) * P.N[i] + dv[i];
+      Nsum[i] += P.N[i];
     }
+    const double w[2] = {P.u[0] / dt - 0.5 * P.ag[0], P.u[1] / dt - 0.5 * P.ag[1]};
+    for (int i = 0; i < 3; ++i)
+    {
+      for (int j = 0; j < 3; ++j)
+      {
+        Ss[i][j] += s[i] * phi[j];
+      }
+      T[i] += P.tau * dv[i];
+      Pj[i] += P.tau * phi[i];
+      Fv[i][0] += s[i] * w[0];
+      Fv[i][1] += s[i] * w[1];
+    }
+    V[0] += P.tau * w[0];
+    V[1] += P.tau * w[1];
+    Tt += P.tau;
   }
+  const double Jw = E.jxw, J3 = 3.0 * E.jxw;
+  double       x[kDofs];
+  for (int k = 0; k < kDofs; ++k)
+  {
+    x[k] = a.nxt[E.dofs[k]];
+  }
+  int   rs[kDofs];
+  uint4 pw[kDofs];
   if (kJac)
   {
-    __syncwarp();
-    if (live && l < kDofs)
+    for (int k = 0; k < kDofs; ++k)
     {
-      // lane l owns local column l: one reduction instruction per row
-      unsigned char pos[16];
+      rs[k] = a.row_ptr[E.dofs[k]];
       if (a.jac_pos != nullptr)
       {
-        const uint4    w4    = *reinterpret_cast<const uint4*>(a.jac_pos + (9LL * e + l) * 16);
-        const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-        for (int i = 0; i < 16; ++i)
-        {
-          pos[i] = static_cast<unsigned char>(wd[i >> 2] >> (8 * (i & 3)));
-        }
-      }
-#pragma unroll
-      for (int row = 0; row < kDofs; ++row)
-      {
-        const int slot = a.jac_pos != nullptr ? sm.rs[le][row] + pos[row]
-                                              : a.jac_map[81LL * e + kDofs * row + l];
-        gbfem::redAdd(a.vals + slot, sm.kv[le][row][l]);
+        pw[k] = *reinterpret_cast<const uint4*>(a.jac_pos + (9LL * e + k) * 16);
       }
     }
+  }
+  // velocity rows (i, c)
+  for (int i = 0; i < 3; ++i)
+  {
+    double kvv[3], kvp[2][3];
+    for (int j = 0; j < 3; ++j)
+    {
+      const double gd = E.g[i][0] * E.g[j][0] + E.g[i][1] * E.g[j][1];
+      kvv[j]          = 0.5 * rho * Jw * Ss[i][j] + 0.5 * mu * J3 * gd;
+      for (int c = 0; c < 2; ++c)
+      {
+        kvp[c][j] = -E.g[i][c] * Jw * Nsum[j] + E.g[j][c] * Jw * T[i];
+      }
+    }
+    for (int c = 0; c < 2; ++c)
+    {
+      const double gradc = E.g[i][0] * E.grad[c][0] + E.g[i][1] * E.grad[c][1];
+      double       r     = -(rho * Jw * Fv[i][c] - 0.5 * mu * J3 * gradc);
+      for (int j = 0; j < 3; ++j)
+      {
+        r += kvv[j] * x[2 * j + c] + kvp[c][j] * x[6 + j];
+      }
+      const int row = 2 * i + c;
+      gbfem::redAdd(a.res + E.dofs[row], r);
+      if (kJac)
+      {
+        for (int j = 0; j < 3; ++j)
+        {
+          gbfem::redAdd(a.vals + csrSlot(a, e, rs, row, 2 * j + c, pw), kvv[j]);
+          gbfem::redAdd(a.vals + csrSlot(a, e, rs, row, 6 + j, pw), kvp[c][j]);
+        }
+        // the cross-component entries (j, 1 - c) are structurally zero
+      }
+    }
+  }
+  // pressure rows i
+  for (int i = 0; i < 3; ++i)
+  {
+    const int row = 6 + i;
+    double    r   = -(Jw * (E.g[i][0] * V[0] + E.g[i][1] * V[1]));
+    for (int j = 0; j < 3; ++j)
+    {
+      const double gd  = E.g[i][0] * E.g[j][0] + E.g[i][1] * E.g[j][1];
+      const double kpp = gd * Jw * Tt / rho;
+      r += kpp * x[6 + j];
+      for (int dd = 0; dd < 2; ++dd)
+      {
+        const double kpv = E.g[j][dd] * Jw * Nsum[i] + 0.5 * E.g[i][dd] * Jw * Pj[j];
+        r += kpv * x[2 * j + dd];
+        if (kJac)
+        {
+          gbfem::redAdd(a.vals + csrSlot(a, e, rs, row, 2 * j + dd, pw), kpv);
+        }
+      }
+      if (kJac)
+      {
+        gbfem::redAdd(a.vals + csrSlot(a, e, rs, row, 6 + j, pw), kpp);
+      }
+    }
+    gbfem::redAdd(a.res + E.dofs[row], r);
   }
 }
 
 // History VJP: out[lag][dof] += d/d hist[lag][dof] of sum_rows adj . R.
+// With the adjoint and next-state fields at a point (X, A, Xp, AP; their
+// constant gradients Gx, GA, Gp, GAP), the adjoint-weighted integrand is
+//   E = sum_c [rho/dt A_c (X_c - u_c) + rho/2 A_c (Dv_c + ag_c)
+//              + mu/2 GA_c.(Gx_c + grad_c) + tau rho/dt Av_c (X_c - u_c)
+//              + tau rho/2 Av_c (Dv_c + ag_c) - GA_c[c] Xp + tau Av_c Gp_c]
+//     + AP div(X) + tau GAP.(X/dt + Dv/2 + Gp/rho - u/dt + ag/2),
+// Dv_c = adv.Gx_c, Av_c = adv.GA_c; its partials in (u, grad, adv, tau) are
+// chained back to the nodal history values.
 __global__ void __launch_bounds__(kThreads) nsHistVjpKernel(NsArgs a)
 {
-  __shared__ NsSmem sm;
-  __shared__ double dEu[kElems][kQ][2], dEg[kElems][kQ][2][2], dEa[kElems][kQ][2];
-  const int  l    = threadIdx.x & (kLanes - 1);
-  const int  le   = threadIdx.x / kLanes;
-  const int  e    = blockIdx.x * kElems + le;
-  const bool has  = e < a.ne;
-  NsElem&    E    = sm.el[le];
-  const bool live = stageElement(a, E, e, l, has, true);
-  if (live && l < kQ)
+  const int e = blockIdx.x * kThreads + threadIdx.x;
+  if (e >= a.ne)
   {
-    const int q = l;
-    evalQp(a, E, q);
-    const NsQp&  qp  = E.qp[q];
-    const double rho = a.rho, mu = a.mu, dt = a.dt, tau = qp.tau;
-    // next-state and adjoint fields at the point
-    double X[2] = {0, 0}, Gx[2][2] = {{0, 0}, {0, 0}}, Xp = 0, Gp[2] = {0, 0};
-    double A[2] = {0, 0}, GA[2][2] = {{0, 0}, {0, 0}}, AP = 0, GAP[2] = {0, 0};
+    return;
+  }
+  NsElem E;
+  if (!loadElement(a, e, E))
+  {
+    return;
+  }
+  const double rho = a.rho, mu = a.mu, dt = a.dt, nu = mu / rho;
+  double       x[kDofs], ad[kDofs];
+  for (int k = 0; k < kDofs; ++k)
+  {
+    x[k]  = a.nxt[E.dofs[k]];
+    ad[k] = a.adj[E.dofs[k]];
+  }
+  double Gx[2][2], GA[2][2], Gp[2], GAP[2];
+  for (int d = 0; d < 2; ++d)
+  {
+    for (int c = 0; c < 2; ++c)
+    {
+      Gx[c][d] = E.g[0][d] * x[c] + E.g[1][d] * x[2 + c] + E.g[2][d] * x[4 + c];
+      GA[c][d] = E.g[0][d] * ad[c] + E.g[1][d] * ad[2 + c] + E.g[2][d] * ad[4 + c];
+    }
+    Gp[d]  = E.g[0][d] * x[6] + E.g[1][d] * x[7] + E.g[2][d] * x[8];
+    GAP[d] = E.g[0][d] * ad[6] + E.g[1][d] * ad[7] + E.g[2][d] * ad[8];
+  }
+  double SU[3][2] = {}, SA[3][2] = {}, SG[2][2] = {};
+  for (int q = 0; q < kQ; ++q)
+  {
+    NsQp P;
+    pointState(a, E, q, P);
+    const double tau = P.tau;
+    double       X[2], A[2], Xp = 0.0, AP = 0.0;
+    for (int c = 0; c < 2; ++c)
+    {
+      X[c] = P.N[0] * x[c] + P.N[1] * x[2 + c] + P.N[2] * x[4 + c];
+      A[c] = P.N[0] * ad[c] + P.N[1] * ad[2 + c] + P.N[2] * ad[4 + c];
+    }
     for (int j = 0; j < 3; ++j)
     {
-      const double N = basisN(q, j);
-      for (int c = 0; c < 2; ++c)
-      {
-        X[c] += N * E.x[2 * j + c];
-        A[c] += N * E.a[2 * j + c];
-        for (int d = 0; d < 2; ++d)
-        {
-          Gx[c][d] += E.g[j][d] * E.x[2 * j + c];
-          GA[c][d] += E.g[j][d] * E.a[2 * j + c];
-        }
-      }
-      Xp += N * E.x[6 + j];
-      AP += N * E.a[6 + j];
-      for (int d = 0; d < 2; ++d)
-      {
-        Gp[d] += E.g[j][d] * E.x[6 + j];
-        GAP[d] += E.g[j][d] * E.a[6 + j];
-      }
+      Xp += P.N[j] * x[6 + j];
+      AP += P.N[j] * ad[6 + j];
     }
     double Dv[2], Av[2];
     for (int c = 0; c < 2; ++c)
     {
-      Dv[c] = qp.adv[0] * Gx[c][0] + qp.adv[1] * Gx[c][1];
-      Av[c] = qp.adv[0] * GA[c][0] + qp.adv[1] * GA[c][1];
+      Dv[c] = P.adv[0] * Gx[c][0] + P.adv[1] * Gx[c][1];
+      Av[c] = P.adv[0] * GA[c][0] + P.adv[1] * GA[c][1];
     }
-    // partial derivatives of the adjoint-weighted integrand
     double Ptau = 0.0, W[2], PAv[2], du[2];
     for (int c = 0; c < 2; ++c)
     {
-      const double xm = X[c] - qp.u[c], dg = Dv[c] + qp.ag[c];
+      const double xm = X[c] - P.u[c], dg = Dv[c] + P.ag[c];
       Ptau += rho / dt * Av[c] * xm + 0.5 * rho * Av[c] * dg + Av[c] * Gp[c];
-      Ptau += GAP[c] * (X[c] / dt + 0.5 * Dv[c] + Gp[c] / rho - qp.u[c] / dt + 0.5 * qp.ag[c]);
+      Ptau += GAP[c] * (X[c] / dt + 0.5 * Dv[c] + Gp[c] / rho - P.u[c] / dt + 0.5 * P.ag[c]);
       W[c]   = 0.5 * rho * A[c] + 0.5 * tau * rho * Av[c] + 0.5 * tau * GAP[c];
       PAv[c] = tau * rho / dt * xm + 0.5 * tau * rho * dg + tau * Gp[c];
       du[c]  = -rho / dt * A[c] - tau * rho / dt * Av[c] - tau / dt * GAP[c];
     }
-    // tau(u): through |u| and the streamline length h(u/|u|)
-    if (qp.h > 0.0)
+    // tau(u) through |u| and h(u/|u|): dtau = -tau^3/2 d(flow + diff)
+    if (P.h > 0.0)
     {
       double dh[2] = {0.0, 0.0};
-      if (!qp.fallback)
+      if (!P.fallback)
       {
-        // dh/du_c = -2/sum^2 sum_in sgn(g_in) sum_d dN_in/dx_d (delta_dc - dir_d dir_c)/|u|
-        for (int in = 0; in < 3; ++in)
+        for (int i = 0; i < 3; ++i)
         {
-          const double gr = qp.dir[0] * E.g[in][0] + qp.dir[1] * E.g[in][1];
+          const double gr = P.dir[0] * E.g[i][0] + P.dir[1] * E.g[i][1];
           const double sg = gr >= 0.0 ? 1.0 : -1.0;
-          for (int c = 0; c < 2; ++c)
-          {
-            dh[c] += sg * (E.g[in][c] - gr * qp.dir[c]);
-          }
+          dh[0] += sg * (E.g[i][0] - gr * P.dir[0]);
+          dh[1] += sg * (E.g[i][1] - gr * P.dir[1]);
         }
-        for (int c = 0; c < 2; ++c)
-        {
-          dh[c] *= -2.0 / (qp.sum * qp.sum * qp.speed);
-        }
+        const double f = -2.0 / (P.sum * P.sum * P.speed);
+        dh[0] *= f;
+        dh[1] *= f;
       }
-      const double nu  = mu / rho;
-      const double h   = qp.h;
-      const double t3  = tau * tau * tau;
+      const double h = P.h, t3 = tau * tau * tau;
       for (int c = 0; c < 2; ++c)
       {
-        const double dflow = 8.0 * (qp.u[c] * h - qp.speed * qp.speed * dh[c]) / (h * h * h);
+        const double dflow = 8.0 * (P.u[c] * h - P.speed * P.speed * dh[c]) / (h * h * h);
         const double ddiff = -64.0 * nu * nu * dh[c] / (h * h * h * h * h);
         du[c] += Ptau * (-0.5 * t3 * (dflow + ddiff));
       }
     }
-    const double Jw = E.jxw;
     for (int c = 0; c < 2; ++c)
     {
-      dEu[le][q][c] = Jw * du[c];
-      double da     = 0.0;
+      double da = 0.0;
       for (int cc = 0; cc < 2; ++cc)
       {
-        da += W[cc] * (qp.grad[cc][c] + Gx[cc][c]) + PAv[cc] * GA[cc][c];
+        da += W[cc] * (E.grad[cc][c] + Gx[cc][c]) + PAv[cc] * GA[cc][c];
       }
-      dEa[le][q][c] = Jw * da;
+      for (int i = 0; i < 3; ++i)
+      {
+        SU[i][c] += P.N[i] * du[c];
+        SA[i][c] += P.N[i] * da;
+      }
       for (int d = 0; d < 2; ++d)
       {
-        dEg[le][q][c][d] = Jw * (0.5 * mu * GA[c][d] + W[c] * qp.adv[d]);
+        SG[c][d] += 0.5 * mu * GA[c][d] + W[c] * P.adv[d];
       }
     }
   }
-  __syncthreads();
-  if (live && l < 12)
+  const double Jw  = E.jxw;
+  const double al0 = E.ab2 ? 1.5 : 1.0;
+  for (int i = 0; i < 3; ++i)
   {
-    // velocity history entry: lag l / 6, local velocity DOF l % 6
-    const int  lag = l / 6, vd = l % 6, in = vd / 2, c = vd % 2;
-    const bool ab2 = a.step > 0 && a.num_hist > 1;
-    if (lag == 0 || ab2)
+    for (int c = 0; c < 2; ++c)
     {
-      const double al0 = ab2 ? 1.5 : 1.0, al1 = -0.5;
-      double       v   = 0.0;
-      for (int q = 0; q < kQ; ++q)
+      const int    dof = E.dofs[2 * i + c];
+      const double v0 =
+          Jw * (SU[i][c] + E.g[i][0] * SG[c][0] + E.g[i][1] * SG[c][1] + al0 * SA[i][c]);
+      gbfem::redAdd(a.out + dof, v0);
+      if (E.ab2)
       {
-        const double N = basisN(q, in);
-        if (lag == 0)
-        {
-          v += N * dEu[le][q][c] + E.g[in][0] * dEg[le][q][c][0] + E.g[in][1] * dEg[le][q][c][1]
-               + al0 * N * dEa[le][q][c];
-        }
-        else
-        {
-          v += al1 * N * dEa[le][q][c];
-        }
+        gbfem::redAdd(a.out + static_cast<long long>(a.num_states) + dof, Jw * -0.5 * SA[i][c]);
       }
-      const int dof = a.dofs[kDofs * e + vd];
-      gbfem::redAdd(a.out + static_cast<long long>(lag) * a.num_states + dof, v);
     }
   }
 }
@@ -557,12 +511,14 @@ void checkCommon(const gbfem_assembly_map* map, int num_nodes, const double* coo
 extern "C" int gbfem_assemble_navier(const gbfem_assembly_map* map, int num_nodes,
                                      const double* coords, const int* conn, double rho,
                                      double mu, double dt, int step, int num_hist,
-                                     const double* hist, const double* nxt, double* res,
-                                     double* vals, void* stream)
+                                     int wrt_hist_lag, const double* hist, const double* nxt,
+                                     double* res, double* vals, void* stream)
 {
   using namespace gbfem;
   return guarded([&] {
     checkCommon(map, num_nodes, coords, conn, rho, mu, dt, num_hist, hist, nxt);
+    require(wrt_hist_lag >= -1 && wrt_hist_lag < num_hist,
+            "Time assembly variable block is invalid");
     require(res != nullptr, "Assembly residual output is null");
     require(res != hist && res != nxt && vals != hist && vals != nxt
                 && (vals == nullptr || res != vals),
@@ -579,10 +535,12 @@ extern "C" int gbfem_assemble_navier(const gbfem_assembly_map* map, int num_node
     }
     NsArgs a = makeArgs(map, num_nodes, coords, conn, rho, mu, dt, step, num_hist, hist, nxt);
     a.res    = res;
-    a.vals   = vals;
-    const unsigned blocks = blocksFor(a.ne, kElems);
-    vals != nullptr ? nsAssembleKernel<true><<<blocks, kThreads, 0, s>>>(a)
-                    : nsAssembleKernel<false><<<blocks, kThreads, 0, s>>>(a);
+    // femx's operator has no history Jacobian rows (history derivatives are
+    // VJPs, Components.hpp:412-435): a history block is the zero matrix
+    a.vals   = wrt_hist_lag < 0 ? vals : nullptr;
+    const unsigned blocks = blocksFor(a.ne, kThreads);
+    a.vals != nullptr ? nsAssembleKernel<true><<<blocks, kThreads, 0, s>>>(a)
+                      : nsAssembleKernel<false><<<blocks, kThreads, 0, s>>>(a);
     cudaCheck(cudaGetLastError(), "Navier assembly launch");
   });
 }
@@ -609,7 +567,7 @@ extern "C" int gbfem_vjp_navier_hist(const gbfem_assembly_map* map, int num_node
     NsArgs a = makeArgs(map, num_nodes, coords, conn, rho, mu, dt, step, num_hist, hist, nxt);
     a.adj    = adj;
     a.out    = out;
-    nsHistVjpKernel<<<blocksFor(a.ne, kElems), kThreads, 0, s>>>(a);
+    nsHistVjpKernel<<<blocksFor(a.ne, kThreads), kThreads, 0, s>>>(a);
     cudaCheck(cudaGetLastError(), "Navier history VJP launch");
   });
 }

@@ -266,7 +266,10 @@ GBFEM_API int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
  * when num_hist > 1; GLS tau with femx's streamline element length.
  * Local DOFs in femx's mixed layout: velocity (node, comp) then pressure
  * (9 per element); conn = the 3 vertices; hist lag-major (num_hist x
- * num_states, lag 0 = current state). FP64.
+ * num_states, lag 0 = current state). FP64. wrt_hist_lag selects the
+ * Jacobian block as femx's VariableBlock: -1 = NextState (K); a history lag
+ * gives the zero matrix, as femx's operator does (its history derivatives
+ * are VJPs only, Components.hpp:412-435).
  * gbfem_vjp_navier_hist: out[lag][dof] = d(adj . R)/d hist[lag][dof] — the
  * history VJP femx obtains from Enzyme (histVjp / histVjpKernel,
  * Components.cpp:67-125, Components.cu:25-98), here reverse mode written
@@ -275,8 +278,8 @@ GBFEM_API int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
 GBFEM_API int gbfem_assemble_navier(const gbfem_assembly_map* map, int num_nodes,
                                     const double* coords, const int* conn, double rho,
                                     double mu, double dt, int step, int num_hist,
-                                    const double* hist, const double* nxt, double* res,
-                                    double* vals, void* stream);
+                                    int wrt_hist_lag, const double* hist, const double* nxt,
+                                    double* res, double* vals, void* stream);
 GBFEM_API int gbfem_vjp_navier_hist(const gbfem_assembly_map* map, int num_nodes,
                                     const double* coords, const int* conn, double rho,
                                     double mu, double dt, int step, int num_hist,

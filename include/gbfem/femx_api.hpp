@@ -25,11 +25,44 @@
 
 #include "../gbfem.h"
 
+#if defined(__CUDACC__)
+#define GBFEM_HD __host__ __device__
+#else
+#define GBFEM_HD
+#endif
+
 namespace gbfem
 {
 
 using Real  = double;       // femx/common/Types.hpp:17
 using Index = std::int32_t; // femx/common/Types.hpp:19
+
+/** Jacobian block of a time residual (femx/state/TimeResidual.hpp:94-166). */
+class VariableBlock
+{
+public:
+  enum class Kind : int
+  {
+    HistoryState,
+    NextState,
+    Param
+  };
+  GBFEM_HD constexpr VariableBlock(Kind kind = Kind::HistoryState, Index lag = 0)
+    : kind_(kind), lag_(lag)
+  {
+  }
+  GBFEM_HD static constexpr VariableBlock hist(Index lag) { return {Kind::HistoryState, lag}; }
+  GBFEM_HD static constexpr VariableBlock next() { return {Kind::NextState, 0}; }
+  GBFEM_HD static constexpr VariableBlock param() { return {Kind::Param, 0}; }
+  GBFEM_HD constexpr bool  isHistoryState() const { return kind_ == Kind::HistoryState; }
+  GBFEM_HD constexpr bool  isNextState() const { return kind_ == Kind::NextState; }
+  GBFEM_HD constexpr bool  isParam() const { return kind_ == Kind::Param; }
+  GBFEM_HD constexpr Index historyLag() const { return lag_; }
+
+private:
+  Kind  kind_;
+  Index lag_;
+};
 
 inline void check(int rc)
 {
@@ -320,6 +353,63 @@ inline void applyJacT(const KappaPoissonP1& op, const DeviceGeometry& geom,
   check(gbfem_vjp_p1_kappa(map.handle(), geom.num_nodes, geom.coords, geom.conn, op.kappa,
                            state.data(), lam.data(), g_u.data(), g_m.data(),
                            static_cast<int>(op.precision), ctx.stream));
+}
+
+/** Element operator tag: femx's equal-order GLS Navier-Stokes time step
+ * (NavierOperator, femx/model/ns/Components.hpp:397-577) on P1 triangles;
+ * femx carries the element data in the operator (NavierDataView), this tag
+ * carries the geometry it is computed from. */
+struct NavierGLS
+{
+  DeviceGeometry geom;
+  Real           rho{1.0}, mu{1.0}, dt{1.0};
+};
+
+/** Time assemble (femx/assembly/CudaAssembly.hpp:367-413) for NavierGLS:
+ * res = K(hist) nxt - F(hist) and the Jacobian block `wrt` (K for the next
+ * state; zero for a history lag, as femx's operator). jac.vals may be null. */
+inline void assemble(const NavierGLS& op, Index step, Index num_hist, VariableBlock wrt,
+                     const DeviceAssemblyMap& map, DeviceConstVectorView hist,
+                     DeviceConstVectorView nxt, DeviceVectorView res, DeviceCsrMatrix& jac,
+                     CudaContext& ctx)
+{
+  require(num_hist > 0 && hist.size() == num_hist * map.numStates()
+              && nxt.size() == map.numStates(),
+          "Time assembly state dimensions do not match AssemblyMap");
+  require(!wrt.isParam()
+              && (!wrt.isHistoryState()
+                  || (wrt.historyLag() >= 0 && wrt.historyLag() < num_hist)),
+          "Time assembly variable block is invalid");
+  require(res.size() == map.numRes(), "Time assembly residual size does not match AssemblyMap");
+  if (jac.vals != nullptr)
+  {
+    require(jac.pattern.layout_id == map.pattern().layout_id,
+            "Time assembly matrix must use the AssemblyMap CSR layout");
+  }
+  require(op.geom.nodes_per_elem == 3 && op.geom.dim == 2,
+          "Navier operator expects three-node triangles in 2-D");
+  check(gbfem_assemble_navier(map.handle(), op.geom.num_nodes, op.geom.coords, op.geom.conn,
+                              op.rho, op.mu, op.dt, step, num_hist,
+                              wrt.isNextState() ? -1 : wrt.historyLag(), hist.data(),
+                              nxt.data(), res.data(), jac.vals, ctx.stream));
+}
+
+/** History VJP of NavierGLS: out = (dR/d hist)^T adj for every lag
+ * (num_hist x numStates, lag-major) — femx's histVjp (Components.cpp:67-125)
+ * behind ConstrainedTimeResidual::applyJacT (:379-405), which zeroes the
+ * constrained adjoint entries first (zeroBoundary). */
+inline void applyHistJacT(const NavierGLS& op, Index step, Index num_hist,
+                          const DeviceAssemblyMap& map, DeviceConstVectorView hist,
+                          DeviceConstVectorView nxt, DeviceConstVectorView adj,
+                          DeviceVectorView out, CudaContext& ctx)
+{
+  require(num_hist > 0 && hist.size() == num_hist * map.numStates()
+              && nxt.size() == map.numStates() && adj.size() == map.numRes()
+              && out.size() == num_hist * map.numStates(),
+          "Navier history VJP element dimensions do not match");
+  check(gbfem_vjp_navier_hist(map.handle(), op.geom.num_nodes, op.geom.coords, op.geom.conn,
+                              op.rho, op.mu, op.dt, step, num_hist, hist.data(), nxt.data(),
+                              adj.data(), out.data(), ctx.stream));
 }
 
 /** State VJP of TaylorHoodNS: g_state = J(state)^T lam without forming J

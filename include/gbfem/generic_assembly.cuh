@@ -66,36 +66,6 @@ struct TimeElementView
   }
 };
 
-/** Jacobian block of a time residual (femx/state/TimeResidual.hpp:94-166). */
-class VariableBlock
-{
-public:
-  enum class Kind : int
-  {
-    HistoryState,
-    NextState,
-    Param
-  };
-  __host__ __device__ constexpr VariableBlock(Kind kind = Kind::HistoryState, Index lag = 0)
-    : kind_(kind), lag_(lag)
-  {
-  }
-  __host__ __device__ static constexpr VariableBlock hist(Index lag)
-  {
-    return {Kind::HistoryState, lag};
-  }
-  __host__ __device__ static constexpr VariableBlock next() { return {Kind::NextState, 0}; }
-  __host__ __device__ static constexpr VariableBlock param() { return {Kind::Param, 0}; }
-  __host__ __device__ constexpr bool  isHistoryState() const { return kind_ == Kind::HistoryState; }
-  __host__ __device__ constexpr bool  isNextState() const { return kind_ == Kind::NextState; }
-  __host__ __device__ constexpr bool  isParam() const { return kind_ == Kind::Param; }
-  __host__ __device__ constexpr Index historyLag() const { return lag_; }
-
-private:
-  Kind  kind_;
-  Index lag_;
-};
-
 namespace detail
 {
 constexpr int kGenericWarps = 4;

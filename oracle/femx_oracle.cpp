@@ -1464,4 +1464,43 @@ int orc_vjp_navier_hist(const void* mh, const void* qh, double rho, double mu, d
   });
 }
 
+
+int orc_assemble_navier_threads(const void* mh, const void* qh, double rho, double mu,
+                                double dt, int step, int num_hist, const double* hist,
+                                const double* nxt, double* res, double* vals, int nthreads)
+{
+  return guarded([&] {
+    const Map&    m = *static_cast<const Map*>(mh);
+    const P1Quad& q = *static_cast<const P1Quad*>(qh);
+    require(q.ne == m.num_elems, "Geometry and AssemblyMap have different element counts");
+    require(m.max_res <= 9 && m.max_state <= 9,
+            "Navier operator expects nine DOFs per P1 triangle");
+    const NavierGLS op{&q, rho, mu, dt, step, num_hist};
+    struct Row
+    {
+      const NavierGLS* op;
+      const double*    hist;
+      const double*    nxt;
+      std::size_t      ns;
+      const Map*       m;
+      void evalRow(int e, int r, const double* st, double& res, double* jac) const
+      {
+        (void) st;
+        double h0[9], h1[9], xn[9];
+        for (int c = 0; c < 9; ++c)
+        {
+          const int dof = m->state_dofs[m->state_offsets[e] + c];
+          h0[c]         = hist[dof];
+          h1[c]         = op->num_hist > 1 ? hist[ns + dof] : 0.0;
+          xn[c]         = nxt[dof];
+        }
+        res = op->evalRowT<double>(e, r, h0, h1, xn, jac);
+      }
+    } row{&op, hist, nxt, std::size_t(m.num_states), &m};
+    // the generic threaded loop gathers `state` per element; the operator
+    // reads the history and next state itself, so pass nxt as the state
+    assembleLoopThreads(m, row, nxt, res, vals, nthreads);
+  });
+}
+
 } // extern "C"

@@ -147,6 +147,12 @@ int orc_vjp_navier_hist(const void* map, const void* quad, double rho, double mu
                         double dt, int step, int num_hist, const double* hist,
                         const double* nxt, const double* adj, double* out);
 
+/* The same on `nthreads` host threads with atomic adds (femx's OpenMP NS
+ * assembly scheme, NavierStokesModel.cpp:227-318); vals must not be null. */
+int orc_assemble_navier_threads(const void* map, const void* quad, double rho, double mu,
+                                double dt, int step, int num_hist, const double* hist,
+                                const double* nxt, double* res, double* vals, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,6 +69,7 @@ def lib():
         L.orc_assemble_th_range.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int, C.c_int]
         L.orc_assemble_navier.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _f64p, _f64p, _f64p, C.c_void_p]
         L.orc_vjp_navier_hist.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _f64p, _f64p, _f64p, _f64p]
+        L.orc_assemble_navier_threads.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, _f64p, _f64p, _f64p, _f64p, C.c_int]
         L.orc_assemble_th_threads.argtypes = [C.c_void_p, C.c_void_p, C.c_double, _f64p, _f64p, _f64p, C.c_int]
         L.orc_assemble_p1_range.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, C.c_void_p, _f64p, _f64p, _f64p, C.c_int, C.c_int]
         _lib = L
@@ -304,3 +305,14 @@ def vjp_navier_hist(amap: AssemblyMap, quad: P1Quad, rho, mu, dt, step, hist, nx
     _check(lib().orc_vjp_navier_hist(amap.h, quad.h, float(rho), float(mu), float(dt), int(step),
                                      int(num_hist), _f64(hist), _f64(nxt), _f64(adj), out))
     return out
+
+
+def assemble_navier_threads(amap: AssemblyMap, quad: P1Quad, rho, mu, dt, step, hist, nxt,
+                            nthreads, num_hist=2, res=None, vals=None):
+    """femx's GLS NS time operator on `nthreads` host threads (atomic adds)."""
+    res = np.zeros(amap.num_res) if res is None else res
+    vals = np.zeros(amap.nnz) if vals is None else vals
+    _check(lib().orc_assemble_navier_threads(amap.h, quad.h, float(rho), float(mu), float(dt),
+                                             int(step), int(num_hist), _f64(hist), _f64(nxt),
+                                             res, vals, int(nthreads)))
+    return res, vals

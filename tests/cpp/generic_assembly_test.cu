@@ -16,7 +16,11 @@
 // C++ BoundaryMap calls and a matvec; raw outputs go back to the directory
 // for comparison with the CPU oracle.
 //
+// Part 3 ("navier" mode) runs femx's NS time operator through the NavierGLS
+// tag (next-state block, a history block, the history VJP) on a golden case.
+//
 // Usage: generic_assembly_test [dir num_nodes num_elems num_bcs]
+//        generic_assembly_test navier dir num_nodes num_elems
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -381,6 +385,44 @@ void poissonThroughTheCppLayer(const std::string& dir, Index nn, Index ne, Index
   writeFile(dir + "/col_ind.i32", hostOf(map.pattern().col_ind, nnz));
   std::printf("POISSON written nnz=%d\n", nnz);
 }
+// femx's NS time operator through the C++ tag: next-state block, a history
+// block (zero) and the history VJP, for one golden case written by the test.
+void navierThroughTheCppLayer(const std::string& dir, Index nn, Index ne, gbfem::CudaContext& ctx)
+{
+  const Index nd     = 3 * nn;
+  const auto  xy     = readFile<Real>(dir + "/coords.f64", 2 * static_cast<size_t>(nn));
+  const auto  conn   = readFile<Index>(dir + "/conn.i32", 3 * static_cast<size_t>(ne));
+  const auto  dofs   = readFile<Index>(dir + "/dofs.i32", 9 * static_cast<size_t>(ne));
+  const auto  hist   = readFile<Real>(dir + "/hist.f64", 2 * static_cast<size_t>(nd));
+  const auto  nxt    = readFile<Real>(dir + "/nxt.f64", nd);
+  const auto  adj    = readFile<Real>(dir + "/adj.f64", nd);
+  const auto  prm    = readFile<Real>(dir + "/prm.f64", 4);
+  std::vector<Index> offs(ne + 1);
+  for (Index e = 0; e <= ne; ++e)
+  {
+    offs[e] = 9 * e;
+  }
+  Dev<Real>  dxy(xy), dh(hist), dx(nxt), da(adj);
+  Dev<Index> dconn(conn), doffs(offs), ddofs(dofs);
+  auto map = gbfem::makeAssemblyMap(nd, nd, ne, doffs.p, ddofs.p, doffs.p, ddofs.p, ctx);
+  const gbfem::NavierGLS op{{nn, ne, 3, dxy.p, dconn.p, 2}, prm[0], prm[1], prm[2]};
+  const Index            step = static_cast<Index>(prm[3]);
+  Dev<Real>              res(nd), vals(map.pattern().nnz), res_h(nd), vals_h(map.pattern().nnz);
+  Dev<Real>              out(2 * nd);
+  gbfem::DeviceCsrMatrix jac{map.pattern(), vals.p}, jac_h{map.pattern(), vals_h.p};
+  gbfem::assemble(op, step, 2, gbfem::VariableBlock::next(), map, dh.cview(), dx.cview(),
+                  res.view(), jac, ctx);
+  gbfem::assemble(op, step, 2, gbfem::VariableBlock::hist(0), map, dh.cview(), dx.cview(),
+                  res_h.view(), jac_h, ctx);
+  gbfem::applyHistJacT(op, step, 2, map, dh.cview(), dx.cview(), da.cview(), out.view(), ctx);
+  cuda(cudaDeviceSynchronize(), "navier");
+  writeFile(dir + "/ns_res.f64", res.host());
+  writeFile(dir + "/ns_vals.f64", vals.host());
+  writeFile(dir + "/ns_res_hist.f64", res_h.host());
+  writeFile(dir + "/ns_vals_hist.f64", vals_h.host());
+  writeFile(dir + "/ns_vjp.f64", out.host());
+  std::printf("NAVIER written\n");
+}
 } // namespace
 
 int main(int argc, char** argv)
@@ -391,7 +433,11 @@ int main(int argc, char** argv)
   try
   {
     knownAnswers(ctx);
-    if (argc == 5)
+    if (argc == 5 && std::string(argv[1]) == "navier")
+    {
+      navierThroughTheCppLayer(argv[2], std::atoi(argv[3]), std::atoi(argv[4]), ctx);
+    }
+    else if (argc == 5)
     {
       poissonThroughTheCppLayer(argv[1], std::atoi(argv[2]), std::atoi(argv[3]),
                                 std::atoi(argv[4]), ctx);

@@ -88,3 +88,37 @@ def test_user_operator_tag_and_boundary_calls_match_the_oracle(program, tmp_path
     assert rel_inf(rd("rhs.f64", np.float64), rhs) <= 1e-12
     y = orc.matvec(om.row_ptr, om.col_ind, rvals, u)
     assert rel_inf(rd("y.f64", np.float64), y) <= 1e-12
+
+
+def test_navier_tag_through_the_cpp_layer(program, tmp_path):
+    from conftest import load_golden
+    g = load_golden("ns_gls_jit5_s3")
+    nd = int(g["num_dofs"][0])
+    n, e = g["coords"].shape[0], g["conn"].shape[0]
+    d = str(tmp_path)
+    adj = np.random.default_rng(3).standard_normal(nd)
+    np.ascontiguousarray(g["coords"], dtype=np.float64).tofile(os.path.join(d, "coords.f64"))
+    np.ascontiguousarray(g["conn"], dtype=np.int32).tofile(os.path.join(d, "conn.i32"))
+    np.ascontiguousarray(g["res_dofs"], dtype=np.int32).tofile(os.path.join(d, "dofs.i32"))
+    g["hist"].tofile(os.path.join(d, "hist.f64"))
+    g["nxt"].tofile(os.path.join(d, "nxt.f64"))
+    adj.tofile(os.path.join(d, "adj.f64"))
+    np.array([g["rho"][0], g["mu"][0], g["dt"][0], float(g["step"][0])]).tofile(
+        os.path.join(d, "prm.f64"))
+    p = subprocess.run([program, "navier", d, str(n), str(e)], capture_output=True, text=True,
+                       timeout=120)
+    assert p.returncode == 0, p.stdout + p.stderr
+
+    def rd(name):
+        return np.fromfile(os.path.join(d, name), dtype=np.float64)
+
+    assert rel_inf(rd("ns_res.f64"), g["res"]) <= 1e-12
+    assert rel_inf(rd("ns_vals.f64"), g["vals"]) <= 1e-12
+    assert rel_inf(rd("ns_res_hist.f64"), g["res"]) <= 1e-12
+    assert not rd("ns_vals_hist.f64").any()
+    om = orc.AssemblyMap(nd, nd, g["res_offsets"], g["res_dofs"], g["state_offsets"],
+                         g["state_dofs"])
+    q = orc.P1Quad(g["coords"], g["conn"], order=2)
+    ref = orc.vjp_navier_hist(om, q, g["rho"][0], g["mu"][0], g["dt"][0], int(g["step"][0]),
+                              g["hist"], g["nxt"], adj)
+    assert rel_inf(rd("ns_vjp.f64"), ref) <= 1e-12

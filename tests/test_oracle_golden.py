@@ -220,3 +220,13 @@ def test_navier_history_vjp_matches_finite_differences(golden):
         rm, _ = orc.assemble_navier(m, q, *args, g["hist"] - h * dh, g["nxt"], jac=False)
         fd = float((rp - rm) @ adj) / (2 * h)
         assert abs(fd - vjp @ dh) <= 1e-7 * max(1.0, abs(fd))
+
+
+def test_threaded_navier_loop_matches_serial(golden):
+    g = golden("ns_gls_jit5_s3")
+    nd, m, q = ns_setup(g)
+    args = (g["rho"][0], g["mu"][0], g["dt"][0], int(g["step"][0]), g["hist"], g["nxt"])
+    r1, v1 = orc.assemble_navier(m, q, *args)
+    r4, v4 = orc.assemble_navier_threads(m, q, *args, 4)
+    assert rel_inf(r4, r1) <= 1e-14
+    assert rel_inf(v4, v1) <= 1e-14
