@@ -39,6 +39,9 @@ struct gbfem_assembly_map
   // 256 entries; kernels then fall back to jac_map.
   unsigned char* jac_pos    = nullptr;
   int            pos_stride = 0;
+  // Row-major twin of a column-major jac_pos (blocks of 5..16 columns):
+  // jac_pos_rows[(e * uniform_res + i) * 16 + j].
+  unsigned char* jac_pos_rows = nullptr;
 
   // Row-gather tables, built on request by gbfem_assembly_map_enable_gather
   // (uniform maps with 6..16 residual and state DOFs per element and rows up

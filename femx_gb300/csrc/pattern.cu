@@ -411,6 +411,7 @@ gbfem_assembly_map::~gbfem_assembly_map()
   }
   gbfem::deviceFree(status);
   gbfem::deviceFree(jac_pos);
+  gbfem::deviceFree(jac_pos_rows);
   gbfem::deviceFree(gather_pos);
   gbfem::deviceFree(gather_eb);
   gbfem::deviceFree(gather_res);
@@ -615,6 +616,17 @@ extern "C" int gbfem_assembly_map_create(int num_res, int num_states,
               num_elems, nr, nc, stride, col_major, m->res_dofs, m->row_ptr,
               m->jac_map, m->jac_pos);
           cudaCheck(cudaGetLastError(), "AssemblyMap position launch");
+          if (col_major && nc <= 16)
+          {
+            // the row-major twin for thread-per-element kernels, which
+            // stage one element row at a time
+            m->jac_pos_rows = deviceAlloc<unsigned char>(rows_tot * 16);
+            cudaCheck(cudaMemsetAsync(m->jac_pos_rows, 0, rows_tot * 16, s), "memset");
+            fillInRowPos<<<blocksFor(rows_tot, 256), 256, 0, s>>>(
+                num_elems, nr, nc, 16, false, m->res_dofs, m->row_ptr, m->jac_map,
+                m->jac_pos_rows);
+            cudaCheck(cudaGetLastError(), "AssemblyMap position launch");
+          }
         }
         m->max_in_row_pos = mx_h;
       }

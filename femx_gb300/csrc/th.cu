@@ -142,6 +142,230 @@ __global__ void __launch_bounds__(128) thResidual64Kernel(ThArgs a)
   }
 }
 
+// Plain FP64 Jacobian + residual, one thread per element. The same
+// factorised element as thBlock (diffusion from the reference tensors S,
+// convection from the quadrature transforms, reaction from the vertex
+// gradients, pressure blocks from C) with the reference tables in constant
+// memory (warp-uniform operands). FP64 issue is the bound on GB300, and an
+// FP64 warp instruction costs the same with 1 or 32 active lanes, so every
+// lane owns a whole element: about half the FP64 warp instructions of the
+// 16-lane layout, whose geometry and quadrature stages run on few lanes.
+// Rows are produced one at a time (warp-uniform), staged in shared memory
+// and added row-coalesced: a half-warp adds one element row per FP64
+// reduction instruction, positions from the row-major in-row map (loaded
+// before the row's values are computed and staged next to them).
+__global__ void __launch_bounds__(128) thElemKernel64(ThArgs a, const unsigned char* pos_rows)
+{
+  __shared__ double buf[4][32][17];
+  __shared__ int    rsb[4][32];
+  __shared__ uint4  posb[4][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e0   = blockIdx.x * 128 + warp * 32;
+  const int e    = e0 + lane;
+  bool      live = e < a.ne;
+  const ThRef<double>& R = kRefC;
+
+  double aInvJ[4] = {0, 0, 0, 0}, G3[3] = {0, 0, 0};
+  if (live)
+  {
+    for (int k = 0; k < 6; ++k)
+    {
+      if (static_cast<unsigned>(a.conn6[6 * e + k]) >= static_cast<unsigned>(a.num_nodes))
+      {
+        gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+        live = false;
+      }
+    }
+  }
+  if (live)
+  {
+    const double2 x0 = a.coords[a.conn6[6 * e + 0]];
+    const double2 x1 = a.coords[a.conn6[6 * e + 1]];
+    const double2 x2 = a.coords[a.conn6[6 * e + 2]];
+    const double  j00 = x1.x - x0.x, j01 = x2.x - x0.x;
+    const double  j10 = x1.y - x0.y, j11 = x2.y - x0.y;
+    const double  det = j00 * j11 - j01 * j10;
+    const double  ad  = det < 0.0 ? -det : det;
+    if (ad >= 1.0e-30)
+    {
+      const double inv = 1.0 / det;
+      const double i00 = j11 * inv, i01 = -j01 * inv, i10 = -j10 * inv, i11 = j00 * inv;
+      aInvJ[0]         = ad * i00;
+      aInvJ[1]         = ad * i01;
+      aInvJ[2]         = ad * i10;
+      aInvJ[3]         = ad * i11;
+      const double nad = a.nu * ad;
+      G3[0]            = nad * (i00 * i00 + i01 * i01);
+      G3[1]            = nad * (i10 * i10 + i11 * i11);
+      G3[2]            = nad * (i00 * i10 + i01 * i11);
+    }
+    else
+    {
+      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+      live = false;
+    }
+  }
+  double st[15];
+#pragma unroll
+  for (int l = 0; l < 15; ++l)
+  {
+    st[l] = live ? a.state[a.dofs[15 * e + l]] : 0.0;
+  }
+  double Gv[3][2][2] = {}, ut[kNq][2] = {};
+  if (live)
+  {
+#pragma unroll
+    for (int v = 0; v < 3; ++v)
+    {
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+      {
+        double g0 = 0, g1 = 0;
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2)
+        {
+          g0 += st[2 * s2 + c] * R.dNv[v][s2][0];
+          g1 += st[2 * s2 + c] * R.dNv[v][s2][1];
+        }
+        Gv[v][c][0] = g0 * aInvJ[0] + g1 * aInvJ[2];
+        Gv[v][c][1] = g0 * aInvJ[1] + g1 * aInvJ[3];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kNq; ++q)
+    {
+      double u0 = 0, u1 = 0;
+#pragma unroll
+      for (int s2 = 0; s2 < 6; ++s2)
+      {
+        u0 += R.N[q][s2] * st[2 * s2];
+        u1 += R.N[q][s2] * st[2 * s2 + 1];
+      }
+      ut[q][0] = aInvJ[0] * u0 + aInvJ[1] * u1;
+      ut[q][1] = aInvJ[2] * u0 + aInvJ[3] * u1;
+    }
+  }
+
+  const bool jac = a.vals != nullptr;
+  // row l: CSR start and positions (loaded ahead of the values)
+  auto rowRef = [&](int l, int& rs, uint4& pw) {
+    rs = -1;
+    pw = make_uint4(0, 0, 0, 0);
+    if (live && jac)
+    {
+      rs = a.row_ptr[a.dofs[15 * e + l]];
+      if (pos_rows != nullptr)
+      {
+        pw = *reinterpret_cast<const uint4*>(pos_rows + (15LL * e + l) * 16);
+      }
+    }
+  };
+  auto stage = [&](int l, int rs, const uint4& pw, const double (&v)[15], double r) {
+    if (live)
+    {
+      gbfem::redAdd(a.res + a.dofs[15 * e + l], r);
+    }
+    if (jac)
+    {
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        buf[warp][lane][j] = v[j];
+      }
+      rsb[warp][lane]  = rs;
+      posb[warp][lane] = pw;
+    }
+  };
+  auto scatterRow = [&](int l) {
+    if (!jac)
+    {
+      return;
+    }
+    __syncwarp();
+    const int j = lane & 15;
+#pragma unroll 4
+    for (int t2 = 0; t2 < 16; ++t2)
+    {
+      const int t  = 2 * t2 + (lane >> 4);
+      const int rs = rsb[warp][t];
+      if (j < 15 && rs >= 0 && (l < 12 || j < 12))
+      {
+        const int slot = pos_rows != nullptr
+                             ? rs + reinterpret_cast<const unsigned char*>(&posb[warp][t])[j]
+                             : a.jac_map[225LL * (e0 + t) + 15 * l + j];
+        gbfem::redAdd(a.vals + slot, buf[warp][t][j]);
+      }
+    }
+    __syncwarp();
+  };
+
+#pragma unroll
+  for (int sa = 0; sa < 6; ++sa)
+  {
+    double da[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b)
+    {
+      double d = G3[0] * R.S00[sa][b] + G3[1] * R.S11[sa][b] + G3[2] * R.S01[sa][b];
+#pragma unroll
+      for (int q = 0; q < kNq; ++q)
+      {
+        d += R.wN[q][sa] * (R.dNr[q][b][0] * ut[q][0] + R.dNr[q][b][1] * ut[q][1]);
+      }
+      da[b] = d;
+    }
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+    {
+      int   rs;
+      uint4 pw;
+      rowRef(2 * sa + c, rs, pw);
+      const int oc = c ^ 1;
+      double    v[15];
+      double    r = 0;
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
+      {
+        const double mcc = R.T[0][sa][b] * Gv[0][c][c] + R.T[1][sa][b] * Gv[1][c][c]
+                           + R.T[2][sa][b] * Gv[2][c][c];
+        const double mco = R.T[0][sa][b] * Gv[0][c][oc] + R.T[1][sa][b] * Gv[1][c][oc]
+                           + R.T[2][sa][b] * Gv[2][c][oc];
+        v[2 * b + c]  = da[b] + mcc;
+        v[2 * b + oc] = mco;
+        r += da[b] * st[2 * b + c];
+      }
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+      {
+        v[12 + b] = -(aInvJ[c] * R.C[0][sa][b] + aInvJ[2 + c] * R.C[1][sa][b]);
+        r += v[12 + b] * st[12 + b];
+      }
+      stage(2 * sa + c, rs, pw, v, r);
+      scatterRow(2 * sa + c);
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+  {
+    int   rs;
+    uint4 pw;
+    rowRef(12 + b, rs, pw);
+    double v[15];
+    double r = 0;
+#pragma unroll
+    for (int sa = 0; sa < 6; ++sa)
+    {
+      const double c0 = R.C[0][sa][b], c1 = R.C[1][sa][b];
+      v[2 * sa]       = -(aInvJ[0] * c0 + aInvJ[2] * c1);
+      v[2 * sa + 1]   = -(aInvJ[1] * c0 + aInvJ[3] * c1);
+      r += v[2 * sa] * st[2 * sa] + v[2 * sa + 1] * st[2 * sa + 1];
+    }
+    v[12] = v[13] = v[14] = 0.0; // structurally present, nothing added
+    stage(12 + b, rs, pw, v, r);
+    scatterRow(12 + b);
+  }
+}
+
 } // namespace
 
 extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
@@ -245,7 +469,7 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     const unsigned eblocks = blocksFor(a.ne, 128);
     if (precision == GBFEM_PREC_FP64 && jac)
     {
-      thKernel<double, true, true><<<blocks, kThreads, 0, s>>>(a);
+      thElemKernel64<<<eblocks, 128, 0, s>>>(a, map->jac_pos_rows);
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
