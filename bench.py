@@ -413,7 +413,7 @@ def main():
             "roofline_fp64_plain": {"bound": "fp64", "achieved": flop_th * e / t_kern64 / 1e12,
                                     "peak": fp64, "unit": "TFLOP/s",
                                     "frac": flop_th * e / t_kern64 / 1e12 / fp64,
-                                    "kernel": "thKernel<double,true>",
+                                    "kernel": "thElemKernel64 (thread per element)",
                                     "launch_ms": t_kern64 * 1e3,
                                     "peak_source": "measured by gbfem_probe_fp64_fma"},
             "fp64_fma_peak_tflops_measured": fp64,
