@@ -62,6 +62,16 @@ class CsrTransposeView(C.Structure):
     ]
 
 
+class MeshView(C.Structure):
+    _fields_ = [
+        ("dim", C.c_int), ("num_nodes", C.c_int), ("num_elems", C.c_int),
+        ("nodes_per_elem", C.c_int), ("num_facets", C.c_int), ("nodes_per_facet", C.c_int),
+        ("coords", C.c_void_p), ("conn", C.c_void_p), ("elem_etag", C.c_void_p),
+        ("elem_ptag", C.c_void_p), ("facet_conn", C.c_void_p), ("facet_etag", C.c_void_p),
+        ("facet_ptag", C.c_void_p),
+    ]
+
+
 class BatchInstance(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("map", C.c_void_p), ("num_nodes", C.c_int),
@@ -100,6 +110,10 @@ SIGNATURES = {
     "gbfem_spmv": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp]),
     "gbfem_spmv_t": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _d, _d, _vp]),
     "gbfem_csr_transpose_create": (_i, [_i, _i, _vp, _vp, _vp, _vp]),
+    "gbfem_mesh_read_gmsh": (_i, [C.c_char_p, _vp]),
+    "gbfem_mesh_get_view": (_i, [_vp, _vp]),
+    "gbfem_mesh_physical_name": (_i, [_vp, _i, _i, C.c_char_p, _i]),
+    "gbfem_mesh_destroy": (None, [_vp]),
     "gbfem_csr_transpose_get_view": (_i, [_vp, _vp]),
     "gbfem_csr_transpose_apply": (_i, [_vp, _vp, _vp, _vp]),
     "gbfem_csr_transpose_destroy": (None, [_vp]),

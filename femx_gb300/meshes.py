@@ -262,3 +262,77 @@ def cavity_state(coords_p2: np.ndarray, num_vertices: int, seed: int):
     vel = stream_velocity(coords_p2, seed)
     p = np.random.default_rng(seed).standard_normal(num_vertices)
     return np.concatenate([vel.reshape(-1), p])
+
+
+def boundary_edges(coords: np.ndarray, conn: np.ndarray, tol: float = 1e-12):
+    """Edges of a unit-square triangulation that lie on its boundary, with the
+    side they lie on (1 bottom, 2 right, 3 top, 4 left)."""
+    out = []
+    x, y = coords[:, 0], coords[:, 1]
+    for e in range(conn.shape[0]):
+        for a, b in ((0, 1), (1, 2), (2, 0)):
+            i, j = int(conn[e, a]), int(conn[e, b])
+            for side, on in ((1, lambda k: abs(y[k]) < tol), (2, lambda k: abs(x[k] - 1) < tol),
+                             (3, lambda k: abs(y[k] - 1) < tol), (4, lambda k: abs(x[k]) < tol)):
+                if on(i) and on(j):
+                    out.append((side, i, j))
+    return out
+
+
+def write_gmsh(path: str, coords: np.ndarray, conn: np.ndarray, version: int = 4,
+               tag_offset: int = 100, seed: int = 0):
+    """Write a unit-square triangle mesh as an ASCII Gmsh file (2.2 or 4.1)
+    with physical groups wall_bottom/right/top/left (1-4, the boundary
+    segments) and fluid (5, the triangles). Node tags are a seeded
+    permutation shifted by tag_offset, so readers must map tags; a point
+    element and a $Comments section are included to be skipped."""
+    rng = np.random.default_rng(seed)
+    n = coords.shape[0]
+    tags = rng.permutation(n) + tag_offset
+    edges = boundary_edges(coords, conn)
+    names = {1: "wall_bottom", 2: "wall_right", 3: "wall_top", 4: "wall_left"}
+    lines = ["$MeshFormat", "2.2 0 8" if version == 2 else "4.1 0 8", "$EndMeshFormat",
+             "$Comments", "written by femx_gb300.meshes.write_gmsh $EndComments-not-a-marker",
+             "$EndComments", "$PhysicalNames", "5"]
+    lines += [f'1 {k} "{v}"' for k, v in names.items()] + ['2 5 "fluid"', "$EndPhysicalNames"]
+    if version == 2:
+        lines += ["$Nodes", str(n)]
+        lines += [f"{tags[i]} {float(coords[i, 0])!r} {float(coords[i, 1])!r} 0" for i in range(n)]
+        lines += ["$EndNodes", "$Elements", str(1 + len(edges) + conn.shape[0])]
+        k = 1
+        lines.append(f"{k} 15 2 0 1 {tags[0]}")
+        for side, i, j in edges:
+            k += 1
+            lines.append(f"{k} 1 2 {side} {side} {tags[i]} {tags[j]}")
+        for e in range(conn.shape[0]):
+            k += 1
+            a, b, c = (int(v) for v in conn[e])
+            lines.append(f"{k} 2 2 5 1 {tags[a]} {tags[b]} {tags[c]}")
+        lines.append("$EndElements")
+    else:
+        lines += ["$Entities", "0 4 1 0"]
+        for side in range(1, 5):
+            lines.append(f"{side} 0 0 0 1 1 0 1 {side} 0")
+        lines.append("1 0 0 0 1 1 0 1 5 4 1 2 3 4")
+        lines.append("$EndEntities")
+        lines += ["$Nodes", f"1 {n} {tags.min()} {tags.max()}", f"2 1 0 {n}"]
+        lines += [str(tags[i]) for i in range(n)]
+        lines += [f"{float(coords[i, 0])!r} {float(coords[i, 1])!r} 0" for i in range(n)]
+        lines.append("$EndNodes")
+        by_side = {s: [(i, j) for (s2, i, j) in edges if s2 == s] for s in range(1, 5)}
+        nelem = len(edges) + conn.shape[0]
+        lines += ["$Elements", f"5 {nelem} 1 {nelem}"]
+        k = 0
+        for side in range(1, 5):
+            lines.append(f"1 {side} 1 {len(by_side[side])}")
+            for i, j in by_side[side]:
+                k += 1
+                lines.append(f"{k} {tags[i]} {tags[j]}")
+        lines.append(f"2 1 2 {conn.shape[0]}")
+        for e in range(conn.shape[0]):
+            k += 1
+            a, b, c = (int(v) for v in conn[e])
+            lines.append(f"{k} {tags[a]} {tags[b]} {tags[c]}")
+        lines.append("$EndElements")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")

@@ -174,6 +174,34 @@ GBFEM_API int gbfem_spmv_t(int rows, int cols, const int* row_ptr, const int* co
                  double beta, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Mesh ingestion — replaces femx::fem::GmshReader::read (GmshReader.cpp:
+ * 446-548; ASCII Gmsh 2.x/4.x) with flat arrays for the device path:
+ * coordinates [num_nodes][3] (nodes in file order), connectivity of the
+ * elements of the mesh dimension [num_elems][nodes_per_elem] and of the
+ * boundary facets one dimension lower, each with its entity tag and its
+ * physical tag (from the element, else the first of its entity's). femx's
+ * errors and messages; a mesh mixing element shapes is rejected (the
+ * kernels take one node count per element). Host memory owned by the
+ * handle.
+ * ------------------------------------------------------------------------ */
+typedef struct gbfem_mesh gbfem_mesh;
+
+typedef struct
+{
+  int           dim, num_nodes, num_elems, nodes_per_elem, num_facets, nodes_per_facet;
+  const double* coords;
+  const int *   conn, *elem_etag, *elem_ptag;
+  const int *   facet_conn, *facet_etag, *facet_ptag;
+} gbfem_mesh_view;
+
+GBFEM_API int  gbfem_mesh_read_gmsh(const char* path, gbfem_mesh** out);
+GBFEM_API int  gbfem_mesh_get_view(const gbfem_mesh* mesh, gbfem_mesh_view* view);
+/* The physical name of (dim, tag), "" when the file names none. */
+GBFEM_API int  gbfem_mesh_physical_name(const gbfem_mesh* mesh, int dim, int tag, char* buf,
+                                        int buf_len);
+GBFEM_API void gbfem_mesh_destroy(gbfem_mesh* mesh);
+
+/* ---------------------------------------------------------------------------
  * Explicit CSR transpose — replaces MatrixHandler::transpose(src, dst)
  * (femx/linalg/handler/MatrixHandler.cpp:140-155, MatrixHandler.cu:401-512).
  * _create builds, once per source layout, the transposed pattern (rows =

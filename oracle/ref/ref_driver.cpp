@@ -13,7 +13,9 @@
 // (femx/model/ns/Components.hpp:397-577) unchanged, with femx's
 // makeNavierData on a P1 triangle mesh and femx's mixed-space DOF layout.
 //
-// Usage: ref_driver <kind> <case_dir>, kind in {kat, p1, th, inverse, navier}.
+// kind "gmsh" runs femx's GmshReader on case_dir/mesh.msh.
+//
+// Usage: ref_driver <kind> <case_dir>, kind in {kat, p1, th, inverse, navier, gmsh}.
 // Inputs and outputs are raw little-endian arrays named <name>.bin in
 // case_dir; scalar parameters are read from params.txt ("key value" lines).
 
@@ -36,6 +38,7 @@
 #include <femx/fem/ElementQuadratureData.hpp>
 #include <femx/fem/FESpace.hpp>
 #include <femx/fem/GaussQuadrature.hpp>
+#include <femx/fem/GmshReader.hpp>
 #include <femx/fem/Geometry.hpp>
 #include <femx/fem/Mesh.hpp>
 #include <femx/fem/elements/LagrangeTriangleP1.hpp>
@@ -827,11 +830,60 @@ void runNavier()
   writeBin("num_dofs", &nd, 1);
 }
 
+// femx's GmshReader on case_dir/mesh.msh: nodes, elements and boundary
+// facets with their entity and physical tags, and the physical names.
+void runGmsh()
+{
+  const fem::Mesh     mesh = fem::GmshReader::read(g_dir + "/mesh.msh");
+  std::vector<double> xyz;
+  for (Index i = 0; i < mesh.numNodes(); ++i)
+  {
+    for (int d = 0; d < 3; ++d)
+    {
+      xyz.push_back(mesh.node(i)[d]);
+    }
+  }
+  std::vector<int> conn, etag, ptag, fconn, fetag, fptag;
+  for (Index ie = 0; ie < mesh.numElems(); ++ie)
+  {
+    const auto& el = mesh.elem(ie);
+    for (Index k = 0; k < el.numNodes(); ++k)
+    {
+      conn.push_back(el.nodeIds()[k]);
+    }
+    etag.push_back(el.entityTag());
+    ptag.push_back(el.physicalTag());
+  }
+  for (const auto& f : mesh.boundaryFacets())
+  {
+    for (Index k = 0; k < f.nids.size(); ++k)
+    {
+      fconn.push_back(f.nids[k]);
+    }
+    fetag.push_back(f.etag);
+    fptag.push_back(f.ptag);
+  }
+  const int dim = static_cast<int>(mesh.dim());
+  writeBin("dim", &dim, 1);
+  writeBin("coords", xyz.data(), xyz.size());
+  writeBin("conn", conn.data(), conn.size());
+  writeBin("etag", etag.data(), etag.size());
+  writeBin("ptag", ptag.data(), ptag.size());
+  writeBin("fconn", fconn.data(), fconn.size());
+  writeBin("fetag", fetag.data(), fetag.size());
+  writeBin("fptag", fptag.data(), fptag.size());
+  std::ofstream names(g_dir + "/names.txt");
+  for (const auto& pn : mesh.physicalNames())
+  {
+    names << pn.first.first << " " << pn.first.second << " " << pn.second << "\n";
+  }
+}
+
 int main(int argc, char** argv)
 {
   if (argc != 3)
   {
-    std::cerr << "usage: ref_driver <kat|p1|th|inverse|navier> <case_dir>\n";
+    std::cerr << "usage: ref_driver <kat|p1|th|inverse|navier|gmsh> <case_dir>\n";
     return 2;
   }
   const std::string kind = argv[1];
@@ -857,6 +909,10 @@ int main(int argc, char** argv)
     else if (kind == "navier")
     {
       runNavier();
+    }
+    else if (kind == "gmsh")
+    {
+      runGmsh();
     }
     else
     {

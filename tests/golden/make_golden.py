@@ -17,6 +17,11 @@ Cases
   th_jit3      3x3 jittered, permuted Taylor-Hood mesh, nu = 1e-3
   inverse_12   12x12 Poisson inverse: femx ReducedFunctional gradient with
                DenseLinearSolver, misfit 0.5|u - d|^2, kappa = exp(m)
+  gmsh_v2, gmsh_v4
+               femx's GmshReader on ASCII Gmsh 2.2 / 4.1 files written by
+               meshes.write_gmsh (6x6 jittered mesh, permuted node tags,
+               boundary segments with physical groups); the file text is
+               stored with the reader's output
   ns_gls_*     femx's own equal-order GLS Navier-Stokes time operator
                (NavierOperator, CN + AB2) on P1 triangles through femx's time
                assemble: 5x5 jittered permuted mesh at step 0 (no AB2) and
@@ -24,6 +29,7 @@ Cases
                history: the elemLength fallback direction)
 
     python tests/golden/make_golden.py --only ns_gls   # one family of cases
+    python tests/golden/make_golden.py --only gmsh
 """
 from __future__ import annotations
 
@@ -187,18 +193,44 @@ def navier_cases(tmp):
                         **case_navier(tmp, "ns_still", c2, k2, 1.0, 1e-3, 0.1, 2, 43, still=True))
 
 
+def case_gmsh(tmp, name, version):
+    d = os.path.join(tmp, name)
+    os.makedirs(d, exist_ok=True)
+    coords, conn = meshes.jittered_tri(6, seed=61)
+    path = os.path.join(d, "mesh.msh")
+    meshes.write_gmsh(path, coords, conn, version=version, seed=62)
+    run("gmsh", d)
+    out = {"msh": np.frombuffer(open(path, "rb").read(), dtype=np.uint8)}
+    out["dim"] = read(d, "dim", np.int32)
+    out["coords"] = read(d, "coords", np.float64)
+    for k in ("conn", "etag", "ptag", "fconn", "fetag", "fptag"):
+        out[k] = read(d, k, np.int32)
+    out["names"] = np.frombuffer(open(os.path.join(d, "names.txt"), "rb").read(), dtype=np.uint8)
+    return out
+
+
+def gmsh_cases(tmp):
+    for v in (2, 4):
+        np.savez_compressed(os.path.join(HERE, f"gmsh_v{v}.npz"), **case_gmsh(tmp, f"g{v}", v))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default="", help="generate one family: ns_gls")
+    ap.add_argument("--only", default="", help="generate one family: ns_gls, gmsh")
     args = ap.parse_args()
     build(args.ref)
     if args.only == "ns_gls":
         with tempfile.TemporaryDirectory() as tmp:
             navier_cases(tmp)
         return
+    if args.only == "gmsh":
+        with tempfile.TemporaryDirectory() as tmp:
+            gmsh_cases(tmp)
+        return
     with tempfile.TemporaryDirectory() as tmp:
         navier_cases(tmp)
+        gmsh_cases(tmp)
         np.savez_compressed(os.path.join(HERE, "kat.npz"), **case_kat(tmp))
 
         coords, conn = meshes.structured_tri(32)

@@ -477,3 +477,47 @@ def test_taylor_hood_state_vjp_matches_oracle(precision, tol):
     _, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-2, state)
     ref = orc.matvec_t(om.row_ptr, om.col_ind, rvals, lam, nd)
     assert rel_inf(host(g), ref) <= tol
+
+
+@pytest.mark.parametrize("precision,det", [("fp64", False), ("fp32_quad", False), ("mixed", False),
+                                           ("fp32_quad", True)])
+def test_taylor_hood_degenerate_element_is_reported(precision, det):
+    """A zero-area element is reported through the map's status word (femx
+    throws "Singular 2D Jacobian." from ElementValues::invJacobian) and adds
+    nothing; the other elements are assembled."""
+    c3, k3 = meshes.structured_tri(4)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    cp2 = cp2.copy()
+    a, b = conn6[5][0], conn6[5][1]
+    cp2[b] = cp2[a]  # collapse an edge of element 5 (and of its neighbours)
+    state = meshes.cavity_state(cp2, nv, seed=2)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), res, jac,
+                         precision=precision, deterministic=det)
+    with pytest.raises(A.GbfemError, match="Singular 2D Jacobian"):
+        m.check()
+    m.check()
+    assert torch.isfinite(res).all() and torch.isfinite(jac.vals).all()
+
+
+def test_navier_degenerate_element_is_reported():
+    coords, conn = meshes.structured_tri(4)
+    coords = coords.copy()
+    coords[conn[3][1]] = coords[conn[3][0]]
+    n = coords.shape[0]
+    offs, dofs, nd = meshes.navier_elem_dofs(conn, n)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    z = torch.zeros(2 * nd, dtype=torch.float64, device="cuda")
+    A.assembleNavier(m, dev(coords), dev(conn, torch.int32), 1.0, 1e-2, 0.1, 1, z,
+                     z[:nd].clone(), res)
+    with pytest.raises(A.GbfemError, match="Singular 2D Jacobian"):
+        m.check()
+    out = torch.zeros(2 * nd, dtype=torch.float64, device="cuda")
+    A.vjpNavierHist(m, dev(coords), dev(conn, torch.int32), 1.0, 1e-2, 0.1, 1, z, z[:nd].clone(),
+                    z[:nd].clone(), out)
+    with pytest.raises(A.GbfemError, match="Singular 2D Jacobian"):
+        m.check()
