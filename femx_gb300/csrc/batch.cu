@@ -82,18 +82,47 @@ __global__ void zeroSegments(const ZeroSeg* __restrict__ segs,
   }
 }
 
-__device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th_chunk)
-{
-  const int c = d.kind == GBFEM_BATCH_P1_KAPPA ? p1_chunk : th_chunk;
-  return (d.num_elems + c - 1) / c;
-}
-
 // kMode: 0 = FP64, 1 = FP32 quadrature, 2 = MIXED (Jacobian from FP32
 // quadrature; residual and the P1 gradients from FP64 element math; the
 // Taylor-Hood state VJP J^T lam uses the FP32 Jacobian it transposes).
 constexpr int kModeFp64  = 0;
 constexpr int kModeFp32  = 1;
 constexpr int kModeMixed = 2;
+
+__device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th_chunk)
+{
+  const int c = d.kind == GBFEM_BATCH_P1_KAPPA ? p1_chunk : th_chunk;
+  return (d.num_elems + c - 1) / c;
+}
+
+// MIXED: the Taylor-Hood FP64 residuals of every instance in one flat launch
+// after the persistent kernel, one thread per element (FP64 issue is the
+// bound, so every lane works; inside the persistent kernel its registers
+// would cut the occupancy of the other work items).
+__global__ void __launch_bounds__(kBatchThreads)
+    thResidualBatchKernel(const BatchDesc* __restrict__ descs, const int* __restrict__ th_idx,
+                          const long long* __restrict__ th_prefix, int nth)
+{
+  const long long g = blockIdx.x * static_cast<long long>(kBatchThreads) + threadIdx.x;
+  if (g >= th_prefix[nth])
+  {
+    return;
+  }
+  int lo = 0, hi = nth;
+  while (hi - lo > 1)
+  {
+    const int mid = (lo + hi) >> 1;
+    if (th_prefix[mid] <= g)
+    {
+      lo = mid;
+    }
+    else
+    {
+      hi = mid;
+    }
+  }
+  thResidual64Elem(descs[th_idx[lo]].th, static_cast<int>(g - th_prefix[lo]));
+}
 
 template <int kMode, bool kSep, bool kLoad, bool kVjp>
 __device__ __forceinline__ void p1Chunk(const P1Args& a, int e0, int e1)
@@ -148,7 +177,7 @@ struct BatchSmem<kModeFp32>
 template <>
 struct BatchSmem<kModeMixed>
 {
-  using type = ThSmemMixed<float>;
+  using type = ThSmem<float>;
 };
 
 template <int kMode>
@@ -225,8 +254,8 @@ __global__ void __launch_bounds__(kBatchThreads)
         }
         else
         {
-          vjp ? thBlock<float, true, false, true, true>(d.th, eb, sm)
-              : thBlock<float, true, false, false, true>(d.th, eb, sm);
+          vjp ? thBlock<float, true, false, true>(d.th, eb, sm)
+              : thBlock<float, true, false, false>(d.th, eb, sm);
         }
       }
     }
@@ -248,9 +277,15 @@ struct gbfem_batch
   int*                 d_ticket      = nullptr;
   gbfem::DeviceStatus* d_status      = nullptr;
   long long            total_elems   = 0;
+  int                  nth           = 0;       // Taylor-Hood instances
+  long long            th_elems      = 0;
+  int*                 d_th_idx      = nullptr; // their descriptor indices
+  long long*           d_th_prefix   = nullptr; // [nth + 1] element offsets
 
   ~gbfem_batch()
   {
+    gbfem::deviceFree(d_th_idx);
+    gbfem::deviceFree(d_th_prefix);
     gbfem::deviceFree(d_descs);
     gbfem::deviceFree(d_segs);
     gbfem::deviceFree(d_block_prefix);
@@ -373,6 +408,30 @@ extern "C" int gbfem_batch_create(int n, const gbfem_batch_instance* inst, void*
           acc += (z.n + kZeroTile - 1) / kZeroTile;
         }
       }
+      std::vector<int>       th_idx;
+      std::vector<long long> th_prefix{0};
+      for (int i = 0; i < n; ++i)
+      {
+        if (descs[i].kind == GBFEM_BATCH_TH_NS)
+        {
+          th_idx.push_back(i);
+          th_prefix.push_back(th_prefix.back() + descs[i].num_elems);
+        }
+      }
+      b->nth         = static_cast<int>(th_idx.size());
+      b->th_elems    = th_prefix.back();
+      b->d_th_idx    = deviceAlloc<int>(b->nth);
+      b->d_th_prefix = deviceAlloc<long long>(b->nth + 1LL);
+      if (b->nth > 0)
+      {
+        cudaCheck(cudaMemcpyAsync(b->d_th_idx, th_idx.data(), sizeof(int) * b->nth,
+                                  cudaMemcpyHostToDevice, s),
+                  "batch upload");
+      }
+      cudaCheck(cudaMemcpyAsync(b->d_th_prefix, th_prefix.data(),
+                                sizeof(long long) * (b->nth + 1), cudaMemcpyHostToDevice, s),
+                "batch upload");
+      cudaCheck(cudaStreamSynchronize(s), "batch upload");
       b->nseg        = static_cast<int>(nonempty.size());
       b->zero_blocks = acc;
       b->d_descs     = deviceAlloc<BatchDesc>(n);
@@ -440,6 +499,14 @@ extern "C" int gbfem_batch_run(gbfem_batch* b, int precision, int p1_chunk, int 
     {
       batchKernel<kModeMixed><<<grid, kBatchThreads, 0, s>>>(
           b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
+      if (b->th_elems > 0)
+      {
+        cudaCheck(cudaGetLastError(), "batch launch");
+        thResidualBatchKernel<<<static_cast<unsigned>((b->th_elems + kBatchThreads - 1)
+                                                      / kBatchThreads),
+                                kBatchThreads, 0, s>>>(b->d_descs, b->d_th_idx,
+                                                       b->d_th_prefix, b->nth);
+      }
     }
     cudaCheck(cudaGetLastError(), "batch launch");
   });

@@ -33,113 +33,9 @@
 namespace
 {
 
-// Reference tables in constant memory: the thread-per-element kernel below
-// reads every entry with the same address across the warp (broadcast).
-__constant__ ThRef<double> kRefC = makeRef();
-
-// FP64 residual, one thread per element, by direct quadrature:
-//   R_(a,c) = sum_q [Ft_c(q) . dN^_a(q) + src_c(q) N^_a(q)],
-//   Ft_c = J^-1 W (nu grad u_c - p e_c),  src_c = W u . grad u_c,
-//   R_p(b)  = -sum_q psi^_b(q) W div u(q),   W = w_q |det|.
-// All 32 lanes work (FP64 issue, not lanes, is the bound on GB300); used for
-// the residual-only FP64 path and, next to the FP32-quadrature Jacobian
-// kernel, for the MIXED Newton scheme.
 __global__ void __launch_bounds__(128) thResidual64Kernel(ThArgs a)
 {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= a.ne)
-  {
-    return;
-  }
-  int nodes[3];
-  for (int k = 0; k < 6; ++k)
-  {
-    const int nk = a.conn6[6 * e + k];
-    if (static_cast<unsigned>(nk) >= static_cast<unsigned>(a.num_nodes))
-    {
-      gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
-      return;
-    }
-    if (k < 3)
-    {
-      nodes[k] = nk;
-    }
-  }
-  const double2 x0 = a.coords[nodes[0]], x1 = a.coords[nodes[1]], x2 = a.coords[nodes[2]];
-  const double  j00 = x1.x - x0.x, j01 = x2.x - x0.x;
-  const double  j10 = x1.y - x0.y, j11 = x2.y - x0.y;
-  const double  det = j00 * j11 - j01 * j10;
-  if (!(fabs(det) >= 1.0e-30))
-  {
-    gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
-    return;
-  }
-  const double inv   = 1.0 / det;
-  const double iJ[4] = {j11 * inv, -j01 * inv, -j10 * inv, j00 * inv};
-  const double ad    = fabs(det);
-  double       st[15], r[15];
-  int          dofs[15];
-#pragma unroll
-  for (int l = 0; l < 15; ++l)
-  {
-    dofs[l] = a.dofs[15 * e + l];
-    st[l]   = a.state[dofs[l]];
-    r[l]    = 0.0;
-  }
-  const ThRef<double>& rd = kRefC;
-  const double         nu = a.nu;
-#pragma unroll
-  for (int q = 0; q < kNq; ++q)
-  {
-    double u0 = 0, u1 = 0, r00 = 0, r01 = 0, r10 = 0, r11 = 0;
-#pragma unroll
-    for (int s2 = 0; s2 < 6; ++s2)
-    {
-      const double v0 = st[2 * s2], v1 = st[2 * s2 + 1];
-      const double n = rd.N[q][s2], g0 = rd.dNr[q][s2][0], g1 = rd.dNr[q][s2][1];
-      u0 += n * v0;
-      u1 += n * v1;
-      r00 += g0 * v0;
-      r01 += g1 * v0;
-      r10 += g0 * v1;
-      r11 += g1 * v1;
-    }
-    const double G00 = r00 * iJ[0] + r01 * iJ[2], G01 = r00 * iJ[1] + r01 * iJ[3];
-    const double G10 = r10 * iJ[0] + r11 * iJ[2], G11 = r10 * iJ[1] + r11 * iJ[3];
-    double       pq  = 0;
-#pragma unroll
-    for (int b = 0; b < 3; ++b)
-    {
-      pq += rd.P[q][b] * st[12 + b];
-    }
-    const double W   = rd.w[q] * ad;
-    const double F00 = W * (nu * G00 - pq), F01 = W * nu * G01;
-    const double F10 = W * nu * G10, F11 = W * (nu * G11 - pq);
-    const double Ft[2][2] = {{iJ[0] * F00 + iJ[1] * F01, iJ[2] * F00 + iJ[3] * F01},
-                             {iJ[0] * F10 + iJ[1] * F11, iJ[2] * F10 + iJ[3] * F11}};
-    const double src[2]   = {W * (u0 * G00 + u1 * G01), W * (u0 * G10 + u1 * G11)};
-    const double dq       = W * (G00 + G11);
-#pragma unroll
-    for (int sa = 0; sa < 6; ++sa)
-    {
-#pragma unroll
-      for (int c = 0; c < 2; ++c)
-      {
-        r[2 * sa + c] += Ft[c][0] * rd.dNr[q][sa][0] + Ft[c][1] * rd.dNr[q][sa][1]
-                         + src[c] * rd.N[q][sa];
-      }
-    }
-#pragma unroll
-    for (int b = 0; b < 3; ++b)
-    {
-      r[12 + b] -= rd.P[q][b] * dq;
-    }
-  }
-#pragma unroll
-  for (int l = 0; l < 15; ++l)
-  {
-    gbfem::redAdd(a.res + dofs[l], r[l]);
-  }
+  thResidual64Elem(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Plain FP64 Jacobian + residual, one thread per element. The same
