@@ -403,7 +403,8 @@ def main():
                                              "element order, no atomics"},
             "mixed_newton": {"value": world * e / t_mixed, "unit": "elements/s",
                              "ms_per_step": t_mixed * 1e3,
-                             "precision": "Jacobian fp32 quadrature, residual fp64",
+                             "precision": "Jacobian fp32 quadrature, residual to fp64 "
+                                          "accuracy (double-float arithmetic on the FP32 pipe)",
                              "rel_err_vs_fp64": {"jacobian": err_jm, "residual": err_rm}},
             "roofline": {"bound": "hbm", "achieved": b_th / t_kern / 1e9, "peak": hbm,
                          "unit": "GB/s", "frac": b_th / t_kern / 1e9 / hbm,
@@ -730,7 +731,8 @@ def main():
                                     "mixed": tuned.pop("mixed_err")},
             "gate": 1e-6,
             "precision_modes": {"fp32_quad": "all element quadrature fp32, fp64 accumulation",
-                                "mixed": "Jacobian fp32 quadrature; residual and P1 "
+                                "mixed": "Jacobian fp32 quadrature; residual to fp64 accuracy "
+                                         "(Taylor-Hood: double-float, P1: fp64) and P1 "
                                          "gradients fp64; Taylor-Hood J^T lam from the fp32 J"},
             "autotuned": tuned,
         }

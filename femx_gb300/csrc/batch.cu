@@ -95,10 +95,10 @@ __device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th
   return (d.num_elems + c - 1) / c;
 }
 
-// MIXED: the Taylor-Hood FP64 residuals of every instance in one flat launch
-// after the persistent kernel, one thread per element (FP64 issue is the
-// bound, so every lane works; inside the persistent kernel its registers
-// would cut the occupancy of the other work items).
+// MIXED: the Taylor-Hood residuals of every instance (double-float on the
+// FP32 pipe) in one flat launch after the persistent kernel, one thread per
+// element (inside the persistent kernel its registers would cut the
+// occupancy of the other work items).
 __global__ void __launch_bounds__(kBatchThreads)
     thResidualBatchKernel(const BatchDesc* __restrict__ descs, const int* __restrict__ th_idx,
                           const long long* __restrict__ th_prefix, int nth)
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kBatchThreads)
       hi = mid;
     }
   }
-  thResidual64Elem(descs[th_idx[lo]].th, static_cast<int>(g - th_prefix[lo]));
+  thResidualDFElem(descs[th_idx[lo]].th, static_cast<int>(g - th_prefix[lo]));
 }
 
 template <int kMode, bool kSep, bool kLoad, bool kVjp>

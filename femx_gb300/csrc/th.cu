@@ -38,6 +38,11 @@ __global__ void __launch_bounds__(128) thResidual64Kernel(ThArgs a)
   thResidual64Elem(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+__global__ void __launch_bounds__(128) thResidualDFKernel(ThArgs a)
+{
+  thResidualDFElem(a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // Plain FP64 Jacobian + residual, one thread per element. The same
 // factorised element as thBlock (diffusion from the reference tensors S,
 // convection from the quadrature transforms, reaction from the vertex
@@ -374,13 +379,17 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     }
     else
     {
-      // FP64 residual (residual-only FP64 calls; MIXED: next to the
-      // FP32-quadrature Jacobian)
       if (jac)
       {
+        // MIXED: FP32-quadrature Jacobian, residual in double-float
         thKernel<float, true, false><<<blocks, kThreads, 0, s>>>(a);
+        thResidualDFKernel<<<eblocks, 128, 0, s>>>(a);
       }
-      thResidual64Kernel<<<eblocks, 128, 0, s>>>(a);
+      else
+      {
+        // residual-only calls of the FP64 and MIXED modes: FP64
+        thResidual64Kernel<<<eblocks, 128, 0, s>>>(a);
+      }
     }
     cudaCheck(cudaGetLastError(), "Taylor-Hood assembly launch");
   });

@@ -5,6 +5,7 @@
 
 #include <type_traits>
 
+#include "dfloat.cuh"
 #include "maps.cuh"
 
 namespace
@@ -134,49 +135,60 @@ constexpr ThRef<double> makeRef()
 }
 
 template <class R>
+constexpr R refCast(double d)
+{
+  return static_cast<R>(d);
+}
+template <>
+constexpr gbfem::DF refCast<gbfem::DF>(double d)
+{
+  return gbfem::dfConst(d);
+}
+
+template <class R>
 constexpr ThRef<R> castRef()
 {
   const ThRef<double> d = makeRef();
   ThRef<R>            r{};
   for (int q = 0; q < kNq; ++q)
   {
-    r.w[q] = static_cast<R>(d.w[q]);
+    r.w[q] = refCast<R>(d.w[q]);
     for (int b = 0; b < 3; ++b)
     {
-      r.P[q][b] = static_cast<R>(d.P[q][b]);
+      r.P[q][b] = refCast<R>(d.P[q][b]);
     }
     for (int a = 0; a < 6; ++a)
     {
-      r.N[q][a]      = static_cast<R>(d.N[q][a]);
-      r.wN[q][a]     = static_cast<R>(d.wN[q][a]);
-      r.dNr[q][a][0] = static_cast<R>(d.dNr[q][a][0]);
-      r.dNr[q][a][1] = static_cast<R>(d.dNr[q][a][1]);
+      r.N[q][a]      = refCast<R>(d.N[q][a]);
+      r.wN[q][a]     = refCast<R>(d.wN[q][a]);
+      r.dNr[q][a][0] = refCast<R>(d.dNr[q][a][0]);
+      r.dNr[q][a][1] = refCast<R>(d.dNr[q][a][1]);
     }
   }
   for (int a = 0; a < 6; ++a)
   {
     for (int b = 0; b < 6; ++b)
     {
-      r.S00[a][b] = static_cast<R>(d.S00[a][b]);
-      r.S11[a][b] = static_cast<R>(d.S11[a][b]);
-      r.S01[a][b] = static_cast<R>(d.S01[a][b]);
+      r.S00[a][b] = refCast<R>(d.S00[a][b]);
+      r.S11[a][b] = refCast<R>(d.S11[a][b]);
+      r.S01[a][b] = refCast<R>(d.S01[a][b]);
       for (int v = 0; v < 3; ++v)
       {
-        r.T[v][a][b] = static_cast<R>(d.T[v][a][b]);
+        r.T[v][a][b] = refCast<R>(d.T[v][a][b]);
       }
     }
     for (int b = 0; b < 3; ++b)
     {
-      r.C[0][a][b] = static_cast<R>(d.C[0][a][b]);
-      r.C[1][a][b] = static_cast<R>(d.C[1][a][b]);
+      r.C[0][a][b] = refCast<R>(d.C[0][a][b]);
+      r.C[1][a][b] = refCast<R>(d.C[1][a][b]);
     }
   }
   for (int v = 0; v < 3; ++v)
   {
     for (int s2 = 0; s2 < 6; ++s2)
     {
-      r.dNv[v][s2][0] = static_cast<R>(d.dNv[v][s2][0]);
-      r.dNv[v][s2][1] = static_cast<R>(d.dNv[v][s2][1]);
+      r.dNv[v][s2][0] = refCast<R>(d.dNv[v][s2][0]);
+      r.dNv[v][s2][1] = refCast<R>(d.dNv[v][s2][1]);
     }
   }
   return r;
@@ -750,7 +762,48 @@ __constant__ ThRef<double> kRefC = makeRef();
 // All 32 lanes work (FP64 issue, not lanes, is the bound on GB300); used for
 // the residual-only FP64 path and, next to the FP32-quadrature Jacobian
 // kernel, for the MIXED Newton scheme.
-__device__ __forceinline__ void thResidual64Elem(const ThArgs& a, int e)
+// Scalar adapters: the residual below is written once over S = double (the
+// FP64 path) and S = DF (double-float on the FP32 pipe, the MIXED path).
+template <class S>
+__device__ __forceinline__ S sFromF64(double d);
+template <>
+__device__ __forceinline__ double sFromF64<double>(double d)
+{
+  return d;
+}
+template <>
+__device__ __forceinline__ gbfem::DF sFromF64<gbfem::DF>(double d)
+{
+  return gbfem::dfFromF64(d);
+}
+// acc + x*y, and the end of an accumulation
+__device__ __forceinline__ double sFma(double x, double y, double acc)
+{
+  return acc + x * y;
+}
+__device__ __forceinline__ gbfem::DF sFma(gbfem::DF x, gbfem::DF y, gbfem::DF acc)
+{
+  return gbfem::dfFma(x, y, acc);
+}
+__device__ __forceinline__ double sNorm(double x)
+{
+  return x;
+}
+__device__ __forceinline__ gbfem::DF sNorm(gbfem::DF x)
+{
+  return gbfem::dfNorm(x);
+}
+__device__ __forceinline__ double sToF64(double x)
+{
+  return x;
+}
+__device__ __forceinline__ double sToF64(gbfem::DF x)
+{
+  return gbfem::dfToF64(x);
+}
+
+template <class S>
+__device__ __forceinline__ void thResidualElem(const ThArgs& a, int e, const ThRef<S>& rd)
 {
   if (e >= a.ne)
   {
@@ -770,6 +823,7 @@ __device__ __forceinline__ void thResidual64Elem(const ThArgs& a, int e)
       nodes[k] = nk;
     }
   }
+  // geometry in FP64 (a few operations per element)
   const double2 x0 = a.coords[nodes[0]], x1 = a.coords[nodes[1]], x2 = a.coords[nodes[2]];
   const double  j00 = x1.x - x0.x, j01 = x2.x - x0.x;
   const double  j10 = x1.y - x0.y, j11 = x2.y - x0.y;
@@ -780,71 +834,100 @@ __device__ __forceinline__ void thResidual64Elem(const ThArgs& a, int e)
     return;
   }
   const double inv   = 1.0 / det;
-  const double iJ[4] = {j11 * inv, -j01 * inv, -j10 * inv, j00 * inv};
-  const double ad    = fabs(det);
-  double       st[15], r[15];
+  const S      iJ[4] = {sFromF64<S>(j11 * inv), sFromF64<S>(-j01 * inv),
+                        sFromF64<S>(-j10 * inv), sFromF64<S>(j00 * inv)};
+  const S      ad    = sFromF64<S>(fabs(det));
+  const S      zero  = sFromF64<S>(0.0);
+  S            st[15], r[15];
   int          dofs[15];
 #pragma unroll
   for (int l = 0; l < 15; ++l)
   {
     dofs[l] = a.dofs[15 * e + l];
-    st[l]   = a.state[dofs[l]];
-    r[l]    = 0.0;
+    st[l]   = sFromF64<S>(a.state[dofs[l]]);
+    r[l]    = zero;
   }
-  const ThRef<double>& rd = kRefC;
-  const double         nu = a.nu;
-#pragma unroll
+  const S nu = sFromF64<S>(a.nu);
+  // double-float code is ~10x longer per operation: fully unrolled over the
+  // points it overflows the instruction cache, so it keeps the point loop
+  constexpr int kUnrollQ = std::is_same<S, double>::value ? kNq : 1;
+#pragma unroll kUnrollQ
   for (int q = 0; q < kNq; ++q)
   {
-    double u0 = 0, u1 = 0, r00 = 0, r01 = 0, r10 = 0, r11 = 0;
+    S u0 = zero, u1 = zero, r00 = zero, r01 = zero, r10 = zero, r11 = zero;
 #pragma unroll
     for (int s2 = 0; s2 < 6; ++s2)
     {
-      const double v0 = st[2 * s2], v1 = st[2 * s2 + 1];
-      const double n = rd.N[q][s2], g0 = rd.dNr[q][s2][0], g1 = rd.dNr[q][s2][1];
-      u0 += n * v0;
-      u1 += n * v1;
-      r00 += g0 * v0;
-      r01 += g1 * v0;
-      r10 += g0 * v1;
-      r11 += g1 * v1;
+      const S v0 = st[2 * s2], v1 = st[2 * s2 + 1];
+      const S n = rd.N[q][s2], g0 = rd.dNr[q][s2][0], g1 = rd.dNr[q][s2][1];
+      u0  = sFma(n, v0, u0);
+      u1  = sFma(n, v1, u1);
+      r00 = sFma(g0, v0, r00);
+      r01 = sFma(g1, v0, r01);
+      r10 = sFma(g0, v1, r10);
+      r11 = sFma(g1, v1, r11);
     }
-    const double G00 = r00 * iJ[0] + r01 * iJ[2], G01 = r00 * iJ[1] + r01 * iJ[3];
-    const double G10 = r10 * iJ[0] + r11 * iJ[2], G11 = r10 * iJ[1] + r11 * iJ[3];
-    double       pq  = 0;
+    u0  = sNorm(u0);
+    u1  = sNorm(u1);
+    r00 = sNorm(r00);
+    r01 = sNorm(r01);
+    r10 = sNorm(r10);
+    r11 = sNorm(r11);
+    const S G00 = sNorm(sFma(r01, iJ[2], r00 * iJ[0]));
+    const S G01 = sNorm(sFma(r01, iJ[3], r00 * iJ[1]));
+    const S G10 = sNorm(sFma(r11, iJ[2], r10 * iJ[0]));
+    const S G11 = sNorm(sFma(r11, iJ[3], r10 * iJ[1]));
+    S       pq  = zero;
 #pragma unroll
     for (int b = 0; b < 3; ++b)
     {
-      pq += rd.P[q][b] * st[12 + b];
+      pq = sFma(rd.P[q][b], st[12 + b], pq);
     }
-    const double W   = rd.w[q] * ad;
-    const double F00 = W * (nu * G00 - pq), F01 = W * nu * G01;
-    const double F10 = W * nu * G10, F11 = W * (nu * G11 - pq);
-    const double Ft[2][2] = {{iJ[0] * F00 + iJ[1] * F01, iJ[2] * F00 + iJ[3] * F01},
-                             {iJ[0] * F10 + iJ[1] * F11, iJ[2] * F10 + iJ[3] * F11}};
-    const double src[2]   = {W * (u0 * G00 + u1 * G01), W * (u0 * G10 + u1 * G11)};
-    const double dq       = W * (G00 + G11);
+    pq          = sNorm(pq);
+    const S W   = rd.w[q] * ad;
+    const S F00 = W * (nu * G00 - pq), F01 = W * (nu * G01);
+    const S F10 = W * (nu * G10), F11 = W * (nu * G11 - pq);
+    const S Ft[2][2] = {{sNorm(sFma(iJ[1], F01, iJ[0] * F00)), sNorm(sFma(iJ[3], F01, iJ[2] * F00))},
+                        {sNorm(sFma(iJ[1], F11, iJ[0] * F10)), sNorm(sFma(iJ[3], F11, iJ[2] * F10))}};
+    const S src[2]   = {W * sNorm(sFma(u1, G01, u0 * G00)), W * sNorm(sFma(u1, G11, u0 * G10))};
+    const S dq       = W * (G00 + G11);
 #pragma unroll
     for (int sa = 0; sa < 6; ++sa)
     {
 #pragma unroll
       for (int c = 0; c < 2; ++c)
       {
-        r[2 * sa + c] += Ft[c][0] * rd.dNr[q][sa][0] + Ft[c][1] * rd.dNr[q][sa][1]
-                         + src[c] * rd.N[q][sa];
+        S t = sFma(Ft[c][0], rd.dNr[q][sa][0], r[2 * sa + c]);
+        t   = sFma(Ft[c][1], rd.dNr[q][sa][1], t);
+        r[2 * sa + c] = sNorm(sFma(src[c], rd.N[q][sa], t));
       }
     }
 #pragma unroll
     for (int b = 0; b < 3; ++b)
     {
-      r[12 + b] -= rd.P[q][b] * dq;
+      r[12 + b] = sNorm(sFma(-rd.P[q][b], dq, r[12 + b]));
     }
   }
 #pragma unroll
   for (int l = 0; l < 15; ++l)
   {
-    gbfem::redAdd(a.res + dofs[l], r[l]);
+    gbfem::redAdd(a.res + dofs[l], sToF64(r[l]));
   }
+}
+
+// Reference tables in constant memory (warp-uniform operands).
+__constant__ ThRef<gbfem::DF> kRefDF = castRef<gbfem::DF>();
+
+__device__ __forceinline__ void thResidual64Elem(const ThArgs& a, int e)
+{
+  thResidualElem<double>(a, e, kRefC);
+}
+
+// MIXED residual: double-float arithmetic (~44 significant bits) on the
+// FP32 pipe; error against the FP64 residual ~1e-14 relative.
+__device__ __forceinline__ void thResidualDFElem(const ThArgs& a, int e)
+{
+  thResidualElem<gbfem::DF>(a, e, kRefDF);
 }
 
 // Row-gather variants: the element pass writes records, no atomics.

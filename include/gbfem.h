@@ -37,8 +37,10 @@ extern "C" {
 /* Arithmetic of the element kernels. FP64: plain double everywhere (the
  * drop-in). FP32_QUAD: element quadrature in float (Jacobian and residual
  * contributions); accumulation, scatter and all global vectors in double.
- * MIXED: the Newton scheme — Jacobian from FP32 quadrature, residual from
- * FP64 element math; accumulation in double. */
+ * MIXED: the Newton scheme — Jacobian from FP32 quadrature, residual to
+ * FP64 accuracy (Taylor-Hood: double-float arithmetic on the FP32 pipe,
+ * about 1e-14 from the FP64 residual; P1: FP64); accumulation in double.
+ * Residual-only calls in MIXED use the FP64 kernels. */
 #define GBFEM_PREC_FP64 0
 #define GBFEM_PREC_FP32_QUAD 1
 #define GBFEM_PREC_MIXED 2
