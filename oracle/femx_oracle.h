@@ -1,11 +1,12 @@
 /*
  * femx_oracle.h — CPU oracle for the femx assembly hot path.
  *
- * TEST INFRASTRUCTURE ONLY. This library restates, in plain serial C++, the
- * reference algorithms of femx (v0.4.0) that the GB300 kernels replace. It is
- * the checker: only the test-suite, the smoke check and the CPU-baseline leg
- * of the benchmark may load it. The product library (libgbfem) never links
- * or calls it, and has no CPU fallback.
+ * TEST INFRASTRUCTURE ONLY. This library restates, in plain C++, the
+ * reference algorithms of femx (v0.4.0) that the GB300 kernels replace, to
+ * check them against: only the test-suite, the smoke check and the CPU legs
+ * of the benchmark (its CPU baseline and its reference arm) may load it. The
+ * product library (libgbfem) never links or calls it, and has no CPU
+ * fallback.
  *
  * Parity is pinned in two ways (tests/test_oracle_golden.py):
  *   - against the known-answer vectors held by the reference's own unit tests

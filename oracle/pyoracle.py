@@ -1,7 +1,8 @@
 """ctypes wrapper of the CPU oracle (oracle/femx_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by the smoke check and by the
-benchmark's CPU-baseline leg, never by the product package. See
+benchmark's CPU legs (CPU baseline, reference arm), never by the product
+package. See
 oracle/femx_oracle.h for what each function restates and how the oracle is
 pinned to the reference.
 """
