@@ -208,13 +208,19 @@ def host_cores():
 # ------------------------------------------------------------------ GPU arm
 
 class Timer:
-    def __init__(self, torch, stream, flush):
-        self.torch, self.stream, self.flush = torch, stream, flush
+    """Per-step CUDA-event timing on the launch stream, L2 flushed before
+    every step (outside the events); the timed region is bracketed by a
+    barrier + synchronize on both sides (replicas: every rank)."""
+
+    def __init__(self, torch, stream, flush, rep):
+        self.torch, self.stream, self.flush, self.rep = torch, stream, flush, rep
 
     def run(self, fn, steps, warmup):
         torch = self.torch
         for _ in range(warmup):
             fn()
+        torch.cuda.synchronize()
+        self.rep.barrier()
         torch.cuda.synchronize()
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
                for _ in range(steps)]
@@ -223,6 +229,8 @@ class Timer:
             a.record(self.stream)
             fn()
             b.record(self.stream)
+        torch.cuda.synchronize()
+        self.rep.barrier()
         torch.cuda.synchronize()
         return sum(a.elapsed_time(b) for a, b in evs) / steps * 1e-3
 
@@ -279,7 +287,9 @@ def main():
         dist.init_process_group("nccl")
     stream = torch.cuda.current_stream()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    timer = Timer(torch, stream, flush)
+    from femx_gb300.replicas import Replicas
+    rep = Replicas(dist)
+    timer = Timer(torch, stream, flush, rep)
     hbm, peak_kind = peaks()
     traffic = traffic_table()
 
@@ -288,11 +298,7 @@ def main():
         return (t if dtype is None else t.to(dtype)).cuda()
 
     def maxrank(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return rep.max_time(x)
 
     only = args.only
     line = {}
