@@ -359,9 +359,24 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   {
     R64 = &static_cast<ThSmemMixed<T>&>(sm).r64[le];
   }
+  // Every global load whose address is known up front is issued here, so
+  // that the row-pointer and position loads (which depend on the dof load)
+  // overlap the geometry and quadrature work instead of following it.
+  int   hd    = 0;
+  int   h_rs  = 0;
+  uint4 h_pos = make_uint4(0, 0, 0, 0);
   if (has && l < 15)
   {
-    const double sv = a.state[a.dofs[15 * e + l]];
+    hd = a.dofs[15 * e + l];
+    if (kJac && !kGather && a.vals != nullptr)
+    {
+      h_rs = a.row_ptr[hd];
+      if (a.jac_pos != nullptr)
+      {
+        h_pos = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
+      }
+    }
+    const double sv = a.state[hd];
     S.st[l]         = gbfem::fromF64<T>(sv);
     if (kRes64)
     {
@@ -630,14 +645,13 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   }
   if (!kGather && row_lane)
   {
-    const int row_dof = a.dofs[15 * e + l];
     if (kRes)
     {
-      gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
+      gbfem::redAdd(a.res + hd, gbfem::toF64(r));
     }
     if constexpr (kRes64)
     {
-      gbfem::redAdd(a.res + row_dof, rowRes64(*R64, l));
+      gbfem::redAdd(a.res + hd, rowRes64(*R64, l));
     }
     if (kJac)
     {
@@ -668,7 +682,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
         // the pressure-pressure block is structurally present and zero:
         // nothing is added to it
       }
-      sm.rs[le][l] = a.row_ptr[row_dof];
+      sm.rs[le][l] = h_rs;
     }
   }
   if (kJac && !kGather)
@@ -684,8 +698,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
         unsigned char pos[16];
         if (a.jac_pos != nullptr)
         {
-          const uint4 w4 = *reinterpret_cast<const uint4*>(a.jac_pos + (15LL * e + l) * 16);
-          const unsigned wd[4] = {w4.x, w4.y, w4.z, w4.w};
+          const unsigned wd[4] = {h_pos.x, h_pos.y, h_pos.z, h_pos.w};
 #pragma unroll
           for (int i = 0; i < 16; ++i)
           {
@@ -715,7 +728,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
             acc += sm.outv[le][row][l] * sm.lam[le][row];
           }
         }
-        gbfem::redAdd(a.g_state + a.dofs[15 * e + l], gbfem::toF64(acc));
+        gbfem::redAdd(a.g_state + hd, gbfem::toF64(acc));
       }
     }
   }
@@ -723,7 +736,10 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 }
 
 template <class T, bool kJac, bool kRes>
-__global__ void __launch_bounds__(kThreads) thKernel(ThArgs a)
+// 12 resident blocks per SM (at most 40 registers): the kernel waits mostly
+// on its dependent gathers (dofs -> state and row pointers, connectivity ->
+// coordinates), and more resident elements hide more of that latency.
+__global__ void __launch_bounds__(kThreads, 12) thKernel(ThArgs a)
 {
   __shared__ ThSmem<T> sm;
   thStageRef(sm);
