@@ -362,13 +362,12 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   // Every global load whose address is known up front is issued here, so
   // that the row-pointer and position loads (which depend on the dof load)
   // overlap the geometry and quadrature work instead of following it.
-  int   hd    = 0;
   int   h_rs  = 0;
   uint4 h_pos = make_uint4(0, 0, 0, 0);
   if (has && l < 15)
   {
-    hd = a.dofs[15 * e + l];
-    if (kJac && !kGather && a.vals != nullptr)
+    const int hd = a.dofs[15 * e + l];
+    if (kJac && !kGather)
     {
       h_rs = a.row_ptr[hd];
       if (a.jac_pos != nullptr)
@@ -645,13 +644,15 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   }
   if (!kGather && row_lane)
   {
+    // reloaded (an L1 hit) rather than kept live through the element math
+    const int row_dof = a.dofs[15 * e + l];
     if (kRes)
     {
-      gbfem::redAdd(a.res + hd, gbfem::toF64(r));
+      gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
     }
     if constexpr (kRes64)
     {
-      gbfem::redAdd(a.res + hd, rowRes64(*R64, l));
+      gbfem::redAdd(a.res + row_dof, rowRes64(*R64, l));
     }
     if (kJac)
     {
@@ -728,7 +729,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
             acc += sm.outv[le][row][l] * sm.lam[le][row];
           }
         }
-        gbfem::redAdd(a.g_state + hd, gbfem::toF64(acc));
+        gbfem::redAdd(a.g_state + a.dofs[15 * e + l], gbfem::toF64(acc));
       }
     }
   }
