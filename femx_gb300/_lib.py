@@ -133,6 +133,7 @@ SIGNATURES = {
     "gbfem_batch_num_elems": (C.c_longlong, [_vp]),
     "gbfem_batch_destroy": (None, [_vp]),
     "gbfem_probe_convert": (_i, [_i, _vp, _vp, _vp, _vp]),
+    "gbfem_probe_convert_ftz": (_i, [_i, _vp, _vp, _vp]),
 }
 
 _lib = None

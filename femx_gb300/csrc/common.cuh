@@ -181,6 +181,22 @@ __device__ __forceinline__ double f32ToF64(float f)
   return __longlong_as_double(static_cast<long long>(bits));
 }
 
+// Branch-free float -> double for the Jacobian scatter loops: exact for
+// zeros, normal numbers, infinities and NaNs; a subnormal float (magnitude
+// below 2^-126, only reachable by underflow in the FP32 element math) becomes
+// a zero of the same sign. Seven integer operations and no call, against the
+// two branches and the out-of-line fallback of f32ToF64.
+__device__ __forceinline__ double f32ToF64Ftz(float f)
+{
+  const unsigned u    = __float_as_uint(f);
+  const unsigned m    = u & 0x7fffffffu;
+  const unsigned bias = m >= 0x7f800000u ? 0x70000000u : 0x38000000u; // exponent 896 or 2047
+  const bool     norm = m >= 0x00800000u;
+  const unsigned hi   = (norm ? (m >> 3) + bias : 0u) | (u & 0x80000000u);
+  const unsigned lo   = norm ? (u << 29) : 0u;
+  return __hiloint2double(static_cast<int>(hi), static_cast<int>(lo));
+}
+
 // double -> float with round-to-nearest-even, from the IEEE-754 fields on
 // the integer pipe (same reason as above). Values whose float result is
 // normal take the integer path; zeros are exact; anything that would be
@@ -227,6 +243,14 @@ __device__ __forceinline__ double toF64(double d)
 __device__ __forceinline__ double toF64(float f)
 {
   return f32ToF64(f);
+}
+__device__ __forceinline__ double toF64Ftz(double d)
+{
+  return d;
+}
+__device__ __forceinline__ double toF64Ftz(float f)
+{
+  return f32ToF64Ftz(f);
 }
 
 // FP64 reduction-add at L2 without a return value.

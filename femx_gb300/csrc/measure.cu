@@ -40,7 +40,28 @@ __global__ void convertProbe(int n, const double* in, float* out_f, double* out_
     out_d[i]      = gbfem::f32ToF64(f);
   }
 }
+__global__ void convertFtzProbe(int n, const float* in, double* out)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    out[i] = gbfem::f32ToF64Ftz(in[i]);
+  }
+}
 } // namespace
+
+extern "C" int gbfem_probe_convert_ftz(int n, const float* in, double* out, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(n >= 0 && (n == 0 || (in && out)), "probe arguments are invalid");
+    if (n > 0)
+    {
+      convertFtzProbe<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, in, out);
+      cudaCheck(cudaGetLastError(), "convert probe launch");
+    }
+  });
+}
 
 extern "C" int gbfem_probe_convert(int n, const double* in, float* out_f,
                                    double* out_d, void* stream)

@@ -713,7 +713,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
           {
             const int slot = a.jac_pos != nullptr ? sm.rs[le][row] + pos[row]
                                                   : a.jac_map[225LL * e + 15 * row + l];
-            gbfem::redAdd(a.vals + slot, gbfem::toF64(sm.outv[le][row][l]));
+            gbfem::redAdd(a.vals + slot, gbfem::toF64Ftz(sm.outv[le][row][l]));
           }
         }
       }

@@ -26,6 +26,11 @@ GBFEM_API int gbfem_probe_fp64_fma(int blocks, int threads, int iters,
 GBFEM_API int gbfem_probe_convert(int n, const double* in, float* out_f,
                                   double* out_d, void* stream);
 
+/* Test hook for the branch-free float->double conversion of the FP32
+ * Jacobian scatter: out[i] = in[i] widened exactly, except that subnormal
+ * floats become zeros of the same sign. */
+GBFEM_API int gbfem_probe_convert_ftz(int n, const float* in, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -56,3 +56,29 @@ def test_conversions_match_ieee_round_to_nearest_even():
 def test_nan_stays_nan():
     _, f, d = run_probe(np.array([np.nan, -np.nan]))
     assert torch.isnan(f).all() and torch.isnan(d).all()
+
+
+def test_scatter_conversion_is_exact_except_subnormals():
+    from femx_gb300 import _lib
+    rng = np.random.default_rng(1)
+    specials = np.array([0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan,
+                         3.4028234663852886e38, -3.4028234663852886e38,
+                         1.1754943508222875e-38, -1.1754943508222875e-38,   # smallest normals
+                         1.1754942106924411e-38, 1.401298464324817e-45,     # subnormals
+                         -1.401298464324817e-45], dtype=np.float32)
+    bits = rng.integers(0, 1 << 32, size=1 << 20, dtype=np.uint64).astype(np.uint32)
+    vals = np.concatenate([specials, bits.view(np.float32),
+                           rng.standard_normal(1 << 18).astype(np.float32)])
+    x = torch.from_numpy(vals).cuda()
+    out = torch.empty(x.numel(), dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().gbfem_probe_convert_ftz(
+        x.numel(), C.c_void_p(x.data_ptr()), C.c_void_p(out.data_ptr()),
+        C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    ref = x.to(torch.float64)
+    sub = (x != 0) & (x.abs() < 1.1754943508222875e-38)
+    ref = torch.where(sub, torch.copysign(torch.zeros_like(ref), ref), ref)
+    nan = torch.isnan(ref)
+    assert torch.equal(torch.isnan(out), nan)
+    assert torch.equal(out[~nan].view(torch.int64), ref[~nan].view(torch.int64))
+    assert int(sub.sum()) > 0
