@@ -133,6 +133,41 @@ __device__ inline void devFail(DeviceStatus* st, int code, int index)
 
 const char* deviceErrorMessage(int code);
 
+// Programmatic dependent launch (sm_90+). zeroForNext() clears the output
+// arrays of the assembly that follows it on the stream, in a kernel that
+// lets that assembly launch at once (griddepcontrol.launch_dependents); the
+// assembly, launched by launchDependent(), loads and computes its first
+// elements while the zeros are written and calls awaitPrerequisites()
+// (griddepcontrol.wait: returns once the zero kernel has completed and its
+// stores are visible) before its first global reduction. In a kernel that
+// was not launched as a dependent, the wait returns at once. The zero kernel
+// itself waits for all earlier work on the stream, as any launch does.
+__device__ __forceinline__ void awaitPrerequisites()
+{
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// a[0..na) = 0 and b[0..nb) = 0 (either may be empty), as a dependent-launch
+// primary.
+void zeroForNext(double* a, long long na, double* b, long long nb, cudaStream_t s);
+
+template <class... P, class... A>
+void launchDependent(void (*kernel)(P...), unsigned grid, unsigned block, cudaStream_t s,
+                     A&&... args)
+{
+  cudaLaunchConfig_t  cfg{};
+  cudaLaunchAttribute attr[1];
+  attr[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.gridDim                                        = dim3(grid);
+  cfg.blockDim                                       = dim3(block);
+  cfg.dynamicSmemBytes                               = 0;
+  cfg.stream                                         = s;
+  cfg.attrs                                          = attr;
+  cfg.numAttrs                                       = 1;
+  cudaCheck(cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...), "dependent launch");
+}
+
 // Checks the device status word after a synchronize; throws on failure.
 void checkDeviceStatus(DeviceStatus* d_status, cudaStream_t stream);
 

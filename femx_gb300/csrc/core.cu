@@ -1,5 +1,7 @@
 // core.cu — error plumbing, device status checks and the setup-time scan.
+#include <algorithm>
 #include <climits>
+#include <cstdint>
 #include <string>
 #include <vector>
 
@@ -191,7 +193,73 @@ long long scanTo32(const T* in, int* out, long long n, cudaStream_t s)
   return total_h;
 }
 
+__device__ void zeroRange(double* p, long long n, long long tid, long long nt)
+{
+  if (n <= 0)
+  {
+    return;
+  }
+  // one leading double when p is not 16-byte aligned, then pairs, then a tail
+  const long long head = (reinterpret_cast<std::uintptr_t>(p) & 15u) != 0 ? 1 : 0;
+  const long long m    = n - head;
+  if (tid == 0)
+  {
+    if (head != 0)
+    {
+      p[0] = 0.0;
+    }
+    if ((m & 1) != 0)
+    {
+      p[n - 1] = 0.0;
+    }
+  }
+  double2* q = reinterpret_cast<double2*>(p + head);
+  for (long long i = tid; i < m / 2; i += nt)
+  {
+    q[i] = make_double2(0.0, 0.0);
+  }
+}
+
+__global__ void __launch_bounds__(256) zeroForNextKernel(double* a, long long na, double* b,
+                                                          long long nb)
+{
+  asm volatile("griddepcontrol.launch_dependents;");
+  const long long tid = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
+  const long long nt  = static_cast<long long>(gridDim.x) * blockDim.x;
+  zeroRange(a, na, tid, nt);
+  zeroRange(b, nb, tid, nt);
+}
+
+int smCount()
+{
+  thread_local int dev = -1, count = 0;
+  int              d   = 0;
+  cudaCheck(cudaGetDevice(&d), "cudaGetDevice");
+  if (d != dev)
+  {
+    cudaCheck(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, d),
+              "SM count");
+    dev = d;
+  }
+  return count;
+}
+
 } // namespace
+
+void zeroForNext(double* a, long long na, double* b, long long nb, cudaStream_t s)
+{
+  if (na <= 0 && nb <= 0)
+  {
+    return;
+  }
+  // two 256-thread blocks per SM: all resident at once, so that every block
+  // has signalled the dependent launch early, and room is left on each SM
+  // for the dependent assembly's blocks
+  const long long pairs = (std::max(na, 0LL) + std::max(nb, 0LL)) / 2 + 1;
+  const unsigned  grid  = std::min<unsigned>(2u * smCount(), blocksFor(pairs, 256));
+  zeroForNextKernel<<<grid, 256, 0, s>>>(a, na > 0 ? na : 0, b, nb > 0 ? nb : 0);
+  cudaCheck(cudaGetLastError(), "zero-fill launch");
+}
 
 void setLastError(const std::string& msg)
 {

@@ -302,13 +302,9 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     const bool   gather = det && map->num_elems > 0;
     if (!gather)
     {
-      cudaCheck(cudaMemsetAsync(res, 0, sizeof(double) * map->num_res, s),
-                "residual zero");
-      if (vals != nullptr && map->nnz > 0)
-      {
-        cudaCheck(cudaMemsetAsync(vals, 0, sizeof(double) * map->nnz, s),
-                  "matrix zero");
-      }
+      // the FP32-quadrature element kernel is launched as a dependent of
+      // this zero fill and overlaps it up to its first reduction
+      zeroForNext(vals, vals != nullptr ? map->nnz : 0, res, map->num_res, s);
     }
     if (map->num_elems == 0)
     {
@@ -374,15 +370,15 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
-      jac ? thKernel<float, true, true><<<blocks, kThreads, 0, s>>>(a)
-          : thKernel<float, false, true><<<blocks, kThreads, 0, s>>>(a);
+      jac ? launchDependent(thKernel<float, true, true>, blocks, kThreads, s, a)
+          : launchDependent(thKernel<float, false, true>, blocks, kThreads, s, a);
     }
     else
     {
       if (jac)
       {
         // MIXED: FP32-quadrature Jacobian, residual in double-float
-        thKernel<float, true, false><<<blocks, kThreads, 0, s>>>(a);
+        launchDependent(thKernel<float, true, false>, blocks, kThreads, s, a);
         thResidualDFKernel<<<eblocks, 128, 0, s>>>(a);
       }
       else

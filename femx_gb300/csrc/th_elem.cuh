@@ -642,6 +642,10 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       storeRecord(static_cast<T*>(a.geb) + 16LL * k, z);
     }
   }
+  // Every global reduction below adds into arrays that the previous kernel
+  // on the stream zero-fills; a kernel launched as its dependent may have
+  // started before that fill completed (no-op otherwise).
+  gbfem::awaitPrerequisites();
   if (!kGather && row_lane)
   {
     // reloaded (an L1 hit) rather than kept live through the element math
