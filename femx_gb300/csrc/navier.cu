@@ -267,6 +267,8 @@ __global__ void __launch_bounds__(kThreads) nsAssembleKernel(NsArgs a)
     }
   }
   // velocity rows (i, c)
+  // the outputs are zero-filled by the kernel this one may overlap
+  gbfem::awaitPrerequisites();
   for (int i = 0; i < 3; ++i)
   {
     double kvv[3], kvp[2][3];
@@ -524,11 +526,7 @@ extern "C" int gbfem_assemble_navier(const gbfem_assembly_map* map, int num_node
                 && (vals == nullptr || res != vals),
             "Time assembly outputs must not alias inputs or each other");
     cudaStream_t s = asStream(stream);
-    cudaCheck(cudaMemsetAsync(res, 0, sizeof(double) * map->num_res, s), "residual zero");
-    if (vals != nullptr && map->nnz > 0)
-    {
-      cudaCheck(cudaMemsetAsync(vals, 0, sizeof(double) * map->nnz, s), "matrix zero");
-    }
+    zeroForNext(vals, vals != nullptr ? map->nnz : 0, res, map->num_res, s);
     if (map->num_elems == 0)
     {
       return;
@@ -539,8 +537,8 @@ extern "C" int gbfem_assemble_navier(const gbfem_assembly_map* map, int num_node
     // VJPs, Components.hpp:412-435): a history block is the zero matrix
     a.vals   = wrt_hist_lag < 0 ? vals : nullptr;
     const unsigned blocks = blocksFor(a.ne, kThreads);
-    a.vals != nullptr ? nsAssembleKernel<true><<<blocks, kThreads, 0, s>>>(a)
-                      : nsAssembleKernel<false><<<blocks, kThreads, 0, s>>>(a);
+    a.vals != nullptr ? launchDependent(nsAssembleKernel<true>, blocks, kThreads, s, a)
+                      : launchDependent(nsAssembleKernel<false>, blocks, kThreads, s, a);
     cudaCheck(cudaGetLastError(), "Navier assembly launch");
   });
 }

@@ -41,21 +41,23 @@ template <bool kF32, bool kSep>
 void launchAssemble(const P1Args& a, bool load, bool jac, cudaStream_t s)
 {
   const unsigned blocks = gbfem::blocksFor(a.ne, 256);
+  // dependent launches: each overlaps the zero fill (or the kernel) before
+  // it on the stream up to its first reduction
   if (load && jac)
   {
-    p1AssembleKernel<kF32, kSep, true, true><<<blocks, 256, 0, s>>>(a);
+    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, true, true>, blocks, 256, s, a);
   }
   else if (load)
   {
-    p1AssembleKernel<kF32, kSep, true, false><<<blocks, 256, 0, s>>>(a);
+    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, true, false>, blocks, 256, s, a);
   }
   else if (jac)
   {
-    p1AssembleKernel<kF32, kSep, false, true><<<blocks, 256, 0, s>>>(a);
+    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, false, true>, blocks, 256, s, a);
   }
   else
   {
-    p1AssembleKernel<kF32, kSep, false, false><<<blocks, 256, 0, s>>>(a);
+    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, false, false>, blocks, 256, s, a);
   }
 }
 
@@ -114,13 +116,7 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     a.f            = f_nodal;
     a.res          = res;
     a.vals         = vals;
-    cudaCheck(cudaMemsetAsync(res, 0, sizeof(double) * map->num_res, s),
-              "residual zero");
-    if (vals != nullptr && map->nnz > 0)
-    {
-      cudaCheck(cudaMemsetAsync(vals, 0, sizeof(double) * map->nnz, s),
-                "matrix zero");
-    }
+    zeroForNext(vals, vals != nullptr ? map->nnz : 0, res, map->num_res, s);
     if (a.ne == 0)
     {
       return;
@@ -143,11 +139,11 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
       const unsigned blocks = blocksFor(a.ne, 256);
       if (sep)
       {
-        p1AssembleKernel<true, true, false, true, false><<<blocks, 256, 0, s>>>(a);
+        launchDependent(p1AssembleKernel<true, true, false, true, false>, blocks, 256, s, a);
       }
       else
       {
-        p1AssembleKernel<true, false, false, true, false><<<blocks, 256, 0, s>>>(a);
+        launchDependent(p1AssembleKernel<true, false, false, true, false>, blocks, 256, s, a);
       }
       sep ? launchAssemble<false, true>(a, load, false, s)
           : launchAssemble<false, false>(a, load, false, s);

@@ -110,6 +110,8 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
     r1 -= c * (f1 + fs);
     r2 -= c * (f2 + fs);
   }
+  // the outputs are zero-filled by the kernel this one may overlap
+  gbfem::awaitPrerequisites();
   if (kRes)
   {
     gbfem::redAdd(a.res + d0, gbfem::toF64(r0));

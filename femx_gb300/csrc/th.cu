@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(128) thElemKernel64(ThArgs a, const unsigned c
     }
   };
   auto stage = [&](int l, int rs, const uint4& pw, const double (&v)[15], double r) {
+    gbfem::awaitPrerequisites(); // the outputs' zero fill may still be running
     if (live)
     {
       gbfem::redAdd(a.res + a.dofs[15 * e + l], r);
@@ -366,7 +367,7 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     const unsigned eblocks = blocksFor(a.ne, 128);
     if (precision == GBFEM_PREC_FP64 && jac)
     {
-      thElemKernel64<<<eblocks, 128, 0, s>>>(a, map->jac_pos_rows);
+      launchDependent(thElemKernel64, eblocks, 128, s, a, map->jac_pos_rows);
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
