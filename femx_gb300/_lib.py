@@ -121,6 +121,8 @@ SIGNATURES = {
     "gbfem_assemble_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_vjp_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
+    "gbfem_newton_system_th_ns_host": (_i, [_vp, _vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _vp, _vp,
+                                            _d, _vp, _i, _vp]),
     "gbfem_vjp_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_navier": (_i, [_vp, _i, _vp, _vp, _d, _d, _d, _i, _i, _i, _vp, _vp, _vp,
                                    _vp, _vp]),

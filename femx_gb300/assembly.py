@@ -345,6 +345,41 @@ def assembleTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, res, jac=Non
          float(nu), _ptr(state), _ptr(res), _jac_ptr(amap, jac), mode, _stream())
 
 
+def _check_host_vec(v, n, name):
+    if not isinstance(v, torch.Tensor) or v.device.type != "cpu" or v.dtype != torch.float64 \
+            or not v.is_contiguous() or v.numel() != n:
+        raise GbfemError(_lib.GBFEM_EINVAL,
+                         f"{name} must be a contiguous float64 host tensor of size {n}")
+    return v
+
+
+def newtonSystemTaylorHoodHost(amap: AssemblyMap, bc: BoundaryMap, coords, conn6, nu,
+                               state_host, state, bc_vals, res, jac, res_host,
+                               diag: float = 1.0, precision: str = "fp32_quad",
+                               deterministic: bool = False):
+    """One Newton system from a host-resident state: state_host -> state
+    (device), residual + Jacobian (jac may be None) with Dirichlet rows
+    (replaceRes with bc_vals, replaceRows with diag), final residual ->
+    res_host. The copies overlap the device work (pin the host tensors for
+    that); everything is ordered on the current stream."""
+    coords = _dev(coords, torch.float64, "coords")
+    conn6 = _dev(conn6, torch.int32, "conn6")
+    state = _check_vec(state, amap.numStates(), "state")
+    res = _check_vec(res, amap.numRes(), "residual")
+    bc_vals = _check_vec(bc_vals, bc.numBcs(), "prescribed values")
+    state_host = _check_host_vec(state_host, amap.numStates(), "host state")
+    res_host = _check_host_vec(res_host, amap.numRes(), "host residual")
+    if jac is not None:
+        _check_layout(bc, jac)
+    mode = PRECISIONS[precision]
+    if deterministic:
+        amap.enableDeterministic()
+        mode |= _lib.DETERMINISTIC
+    call("gbfem_newton_system_th_ns_host", amap.handle, bc.handle, coords.shape[0],
+         _ptr(coords), _ptr(conn6), float(nu), _ptr(state_host), _ptr(state), _ptr(bc_vals),
+         _ptr(res), _jac_ptr(amap, jac), float(diag), _ptr(res_host), mode, _stream())
+
+
 def vjpTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, lam, g_state,
                   precision: str = "fp64"):
     """g_state = J(state)^T lam of the Taylor-Hood residual, without forming J."""

@@ -151,9 +151,10 @@ __device__ __forceinline__ void awaitPrerequisites()
 // primary.
 void zeroForNext(double* a, long long na, double* b, long long nb, cudaStream_t s);
 
+// A launch as a dependent (dependent = true) or an ordinary one.
 template <class... P, class... A>
-void launchDependent(void (*kernel)(P...), unsigned grid, unsigned block, cudaStream_t s,
-                     A&&... args)
+void launchMaybeDependent(bool dependent, void (*kernel)(P...), unsigned grid, unsigned block,
+                          cudaStream_t s, A&&... args)
 {
   cudaLaunchConfig_t  cfg{};
   cudaLaunchAttribute attr[1];
@@ -164,8 +165,15 @@ void launchDependent(void (*kernel)(P...), unsigned grid, unsigned block, cudaSt
   cfg.dynamicSmemBytes                               = 0;
   cfg.stream                                         = s;
   cfg.attrs                                          = attr;
-  cfg.numAttrs                                       = 1;
-  cudaCheck(cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...), "dependent launch");
+  cfg.numAttrs                                       = dependent ? 1 : 0;
+  cudaCheck(cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...), "kernel launch");
+}
+
+template <class... P, class... A>
+void launchDependent(void (*kernel)(P...), unsigned grid, unsigned block, cudaStream_t s,
+                     A&&... args)
+{
+  launchMaybeDependent(true, kernel, grid, block, s, static_cast<A&&>(args)...);
 }
 
 // Checks the device status word after a synchronize; throws on failure.

@@ -270,14 +270,18 @@ __global__ void __launch_bounds__(128) thElemKernel64(ThArgs a, const unsigned c
 
 } // namespace
 
-extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
-                                    int num_p2_nodes, const double* coords,
-                                    const int* conn6, double nu,
-                                    const double* state, double* res,
-                                    double* vals, int precision, void* stream)
+namespace gbfem
 {
-  using namespace gbfem;
-  return guarded([&] {
+
+// The Taylor-Hood assembly behind gbfem_assemble_th_ns. zero = true: the
+// outputs are zero-filled here and the element kernels launch as dependents
+// of that fill; zero = false: the caller has zero-filled res and vals on the
+// stream (or on a stream it has joined) and the kernels launch ordinarily.
+void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const double* coords,
+                        const int* conn6, double nu, const double* state, double* res,
+                        double* vals, int precision, cudaStream_t s, bool zero)
+{
+  {
     require(map != nullptr, "AssemblyMap handle is null");
     require(map->num_elems == 0
                 || (map->uniform_res == 15 && map->uniform_state == 15),
@@ -299,9 +303,9 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
             "deterministic assembly needs gbfem_assembly_map_enable_gather on the map");
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
-    cudaStream_t s      = asStream(stream);
-    const bool   gather = det && map->num_elems > 0;
-    if (!gather)
+    const bool gather = det && map->num_elems > 0;
+    const bool dep    = zero;
+    if (!gather && zero)
     {
       // the FP32-quadrature element kernel is launched as a dependent of
       // this zero fill and overlaps it up to its first reduction
@@ -367,19 +371,19 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
     const unsigned eblocks = blocksFor(a.ne, 128);
     if (precision == GBFEM_PREC_FP64 && jac)
     {
-      launchDependent(thElemKernel64, eblocks, 128, s, a, map->jac_pos_rows);
+      launchMaybeDependent(dep, thElemKernel64, eblocks, 128, s, a, map->jac_pos_rows);
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
-      jac ? launchDependent(thKernel<float, true, true>, blocks, kThreads, s, a)
-          : launchDependent(thKernel<float, false, true>, blocks, kThreads, s, a);
+      jac ? launchMaybeDependent(dep, thKernel<float, true, true>, blocks, kThreads, s, a)
+          : launchMaybeDependent(dep, thKernel<float, false, true>, blocks, kThreads, s, a);
     }
     else
     {
       if (jac)
       {
         // MIXED: FP32-quadrature Jacobian, residual in double-float
-        launchDependent(thKernel<float, true, false>, blocks, kThreads, s, a);
+        launchMaybeDependent(dep, thKernel<float, true, false>, blocks, kThreads, s, a);
         thResidualDFKernel<<<eblocks, 128, 0, s>>>(a);
       }
       else
@@ -389,6 +393,21 @@ extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
       }
     }
     cudaCheck(cudaGetLastError(), "Taylor-Hood assembly launch");
+  }
+}
+
+} // namespace gbfem
+
+extern "C" int gbfem_assemble_th_ns(const gbfem_assembly_map* map,
+                                    int num_p2_nodes, const double* coords,
+                                    const int* conn6, double nu,
+                                    const double* state, double* res,
+                                    double* vals, int precision, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    assembleTaylorHood(map, num_p2_nodes, coords, conn6, nu, state, res, vals, precision,
+                       asStream(stream), true);
   });
 }
 

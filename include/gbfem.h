@@ -275,6 +275,20 @@ GBFEM_API int gbfem_assemble_th_ns(const gbfem_assembly_map* map, int num_p2_nod
                          const double* coords, const int* conn6, double nu,
                          const double* state, double* res, double* vals,
                          int precision, void* stream);
+/* One Newton system per call for a host-resident state (femx's Newton
+ * iteration, femx/solver/Newton.hpp, with host vectors): uploads state_host
+ * into `state` (device, num_states), assembles res and vals as
+ * gbfem_assemble_th_ns does, applies replaceRes (bc_vals) and, when vals is
+ * not NULL, replaceRows (diag), and downloads the final residual into
+ * res_host (num_res). The upload overlaps the zero fill and the download
+ * overlaps replaceRows, on a side stream owned by the calling host thread
+ * (created on its first call); all of it is ordered on `stream`. Host
+ * buffers should be page-locked for the copies to be asynchronous. */
+GBFEM_API int gbfem_newton_system_th_ns_host(
+    const gbfem_assembly_map* map, const gbfem_boundary_map* bc, int num_p2_nodes,
+    const double* coords, const int* conn6, double nu, const double* state_host, double* state,
+    const double* bc_vals, double* res, double* vals, double diag, double* res_host,
+    int precision, void* stream);
 /* State VJP of the Taylor-Hood residual: g_state = J(state)^T lam, computed
  * element by element without forming J (the transpose action behind
  * Residual::applyJacT / adjoint solves, femx/state/Residual.hpp:42-59,
