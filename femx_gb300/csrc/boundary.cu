@@ -248,7 +248,11 @@ __global__ void replaceRowsKernel(int nb, const int* __restrict__ row_begin,
   {
     return;
   }
-  for (int k = row_begin[ib]; k < row_end[ib]; ++k)
+  // launched as a dependent of the assembly: the row extents are the map's
+  // own (immutable) data; the values are the assembly's output
+  const int kb = row_begin[ib], ke = row_end[ib];
+  gbfem::awaitPrerequisites();
+  for (int k = kb; k < ke; ++k)
   {
     vals[k] = 0.0;
   }
@@ -264,7 +268,8 @@ __global__ void replaceResKernel(int nb, const int* __restrict__ bc_rows,
   if (ib < nb)
   {
     const int r = bc_rows[ib];
-    res[r]      = state[r] - g[ib];
+    gbfem::awaitPrerequisites(); // state, values and residual come from earlier work
+    res[r] = state[r] - g[ib];
   }
 }
 
@@ -535,8 +540,10 @@ extern "C" int gbfem_replace_rows(const gbfem_boundary_map* b, double* vals,
       return;
     }
     require(vals != nullptr, "BoundaryMap matrix values are null");
-    replaceRowsKernel<<<blocksFor(b->num_bcs, 256), 256, 0, asStream(stream)>>>(
-        b->num_bcs, b->row_begin, b->row_end, b->diag, vals, d);
+    // dependent launches: start while the kernel before them drains
+    launchDependent(replaceRowsKernel, blocksFor(b->num_bcs, 256), 256, asStream(stream),
+                    b->num_bcs, static_cast<const int*>(b->row_begin),
+                    static_cast<const int*>(b->row_end), static_cast<const int*>(b->diag), vals, d);
     cudaCheck(cudaGetLastError(), "replaceRows launch");
   });
 }
@@ -554,8 +561,8 @@ extern "C" int gbfem_replace_res(const gbfem_boundary_map* b,
     {
       return;
     }
-    replaceResKernel<<<blocksFor(b->num_bcs, 256), 256, 0, asStream(stream)>>>(
-        b->num_bcs, b->bc_rows, state, g, res);
+    launchDependent(replaceResKernel, blocksFor(b->num_bcs, 256), 256, asStream(stream),
+                    b->num_bcs, static_cast<const int*>(b->bc_rows), state, g, res);
     cudaCheck(cudaGetLastError(), "replaceRes launch");
   });
 }
