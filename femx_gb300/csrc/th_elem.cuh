@@ -241,7 +241,12 @@ struct ElemShared
   T   vq[kNq][6]; // |det| dN^_b(q) . ut_q
   T   Gv[3][4];   // |det| grad u at the vertices, [v][c*2+e]
   int ok;
+  // pads the record to 16 words mod 32, so that the two elements of a warp
+  // (lanes 0-15 and 16-31) write lane-consecutive fields into disjoint banks
+  int pad[sizeof(T) == 4 ? 24 : 1];
 };
+static_assert(sizeof(ElemShared<float>) % 128 == 64 && sizeof(ElemShared<double>) % 128 == 64,
+              "element record stride must be 16 words mod 32");
 
 // FP64 residual by direct quadrature (MIXED mode): state, geometry and the
 // per-quadrature-point reference-coordinate fluxes Ft[q][c][k], sources
@@ -533,18 +538,27 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   const bool row_lane = live && l < 15;
 
   // Row l: velocity (sa, c) for l < 12, pressure b = l - 12 otherwise.
-  // jcc[b] -> column (b, c), jco[b] -> (b, 1-c), jp[b] -> pressure b;
-  // for pressure rows jcc/jco hold the columns (b, 0) and (b, 1).
-  T   jcc[6], jco[6], jp[3] = {0, 0, 0};
+  // FP32 (kCompOrder): je[b] -> column (b, 0), jo[b] -> column (b, 1) on
+  // every row, so that all lanes store column 2b, then 2b + 1: with the row
+  // stride of 17 words those stores hit distinct banks for the two elements
+  // of a warp. FP64 keeps the own/other-component order on velocity rows
+  // (je -> (b, c), jo -> (b, 1 - c)), which needs fewer registers there.
+  // jp[b] -> pressure column b.
+  constexpr bool kCompOrder = sizeof(T) == 4;
+  T              je[6], jo[6], jp[3] = {0, 0, 0};
   T   r = 0;
   int c = 0;
   if (row_lane && l < 12)
   {
     const int sa = l >> 1;
     c            = l & 1;
-    const int oc = c ^ 1;
-    const T   Gcc[3] = {S.Gv[0][c * 2 + c], S.Gv[1][c * 2 + c], S.Gv[2][c * 2 + c]};
-    const T   Gco[3] = {S.Gv[0][c * 2 + oc], S.Gv[1][c * 2 + oc], S.Gv[2][c * 2 + oc]};
+    // kCompOrder: G0/G1 = grad u_c at the vertices, components 0 and 1, and
+    // the scalar block da sits on the diagonal component (w0 = 1 for c = 0,
+    // w1 = 1 for c = 1). Otherwise G0/G1 = own/other component.
+    const int k0 = kCompOrder ? 0 : c, k1 = kCompOrder ? 1 : c ^ 1;
+    const T   G0[3] = {S.Gv[0][c * 2 + k0], S.Gv[1][c * 2 + k0], S.Gv[2][c * 2 + k0]};
+    const T   G1[3] = {S.Gv[0][c * 2 + k1], S.Gv[1][c * 2 + k1], S.Gv[2][c * 2 + k1]};
+    const T   w0    = c == 0 ? T(1) : T(0), w1 = T(1) - w0;
 #pragma unroll
     for (int b = 0; b < 6; ++b)
     {
@@ -554,12 +568,18 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       {
         da += ref.wN[q][sa] * S.vq[q][b];
       }
-      const T mcc = ref.T[0][sa][b] * Gcc[0] + ref.T[1][sa][b] * Gcc[1]
-                    + ref.T[2][sa][b] * Gcc[2];
-      const T mco = ref.T[0][sa][b] * Gco[0] + ref.T[1][sa][b] * Gco[1]
-                    + ref.T[2][sa][b] * Gco[2];
-      jcc[b] = da + mcc;
-      jco[b] = mco;
+      const T m0 = ref.T[0][sa][b] * G0[0] + ref.T[1][sa][b] * G0[1] + ref.T[2][sa][b] * G0[2];
+      const T m1 = ref.T[0][sa][b] * G1[0] + ref.T[1][sa][b] * G1[1] + ref.T[2][sa][b] * G1[2];
+      if constexpr (kCompOrder)
+      {
+        je[b] = da * w0 + m0;
+        jo[b] = da * w1 + m1;
+      }
+      else
+      {
+        je[b] = da + m0;
+        jo[b] = m1;
+      }
       r += da * S.st[2 * b + c];
     }
     const T ic0 = S.aInvJ[0 * 2 + c], ic1 = S.aInvJ[1 * 2 + c];
@@ -577,9 +597,9 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     for (int sa = 0; sa < 6; ++sa)
     {
       const T c0 = ref.C[0][sa][b], c1 = ref.C[1][sa][b];
-      jcc[sa]    = -(S.aInvJ[0] * c0 + S.aInvJ[2] * c1);
-      jco[sa]    = -(S.aInvJ[1] * c0 + S.aInvJ[3] * c1);
-      r += jcc[sa] * S.st[2 * sa] + jco[sa] * S.st[2 * sa + 1];
+      je[sa]     = -(S.aInvJ[0] * c0 + S.aInvJ[2] * c1);
+      jo[sa]     = -(S.aInvJ[1] * c0 + S.aInvJ[3] * c1);
+      r += je[sa] * S.st[2 * sa] + jo[sa] * S.st[2 * sa + 1];
     }
   }
   if (kGather && row_lane)
@@ -597,30 +617,18 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     }
     if (kJac)
     {
-      T v[16];
-      if (l < 12)
+      T          v[16];
+      const bool swap = !kCompOrder && l < 12 && c == 1;
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
       {
-#pragma unroll
-        for (int b = 0; b < 6; ++b)
-        {
-          v[2 * b]     = c ? jco[b] : jcc[b];
-          v[2 * b + 1] = c ? jcc[b] : jco[b];
-        }
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-        {
-          v[12 + b] = jp[b];
-        }
+        v[2 * b]     = swap ? jo[b] : je[b];
+        v[2 * b + 1] = swap ? je[b] : jo[b];
       }
-      else
-      {
 #pragma unroll
-        for (int sa = 0; sa < 6; ++sa)
-        {
-          v[2 * sa]     = jcc[sa];
-          v[2 * sa + 1] = jco[sa];
-        }
-        v[12] = v[13] = v[14] = T(0);
+      for (int b = 0; b < 3; ++b)
+      {
+        v[12 + b] = jp[b]; // zero on pressure rows
       }
       v[15] = T(0);
       storeRecord(static_cast<T*>(a.geb) + 16LL * k, v);
@@ -660,32 +668,33 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     }
     if (kJac)
     {
+      // one store sequence for velocity and pressure rows (no divergence):
+      // local columns 2b (component 0), 2b + 1 (component 1), then the
+      // pressure columns, zero on pressure rows (the pressure-pressure block
+      // is structurally present and zero: the scatter adds nothing to it)
       T* ov = sm.outv[le][l];
-      if (l < 12)
+      if (kCompOrder || l >= 12)
       {
 #pragma unroll
         for (int b = 0; b < 6; ++b)
         {
-          // local columns 2b (component 0) and 2b + 1 (component 1)
-          ov[2 * b + c]       = jcc[b];
-          ov[2 * b + (c ^ 1)] = jco[b];
-        }
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-        {
-          ov[12 + b] = jp[b];
+          ov[2 * b]     = je[b];
+          ov[2 * b + 1] = jo[b];
         }
       }
       else
       {
 #pragma unroll
-        for (int sa = 0; sa < 6; ++sa)
+        for (int b = 0; b < 6; ++b)
         {
-          ov[2 * sa]     = jcc[sa];
-          ov[2 * sa + 1] = jco[sa];
+          ov[2 * b + c]       = je[b];
+          ov[2 * b + (c ^ 1)] = jo[b];
         }
-        // the pressure-pressure block is structurally present and zero:
-        // nothing is added to it
+      }
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+      {
+        ov[12 + b] = jp[b];
       }
       sm.rs[le][l] = h_rs;
     }
