@@ -103,3 +103,73 @@ def test_host_newton_system_rejects_device_host_buffers(cavity):
         A.newtonSystemTaylorHoodHost(t["amap"], t["bc"], t["coords"], t["c6"], 1e-2,
                                      d, d.clone(), t["bvals"], d.clone(), None,
                                      torch.zeros(nd, dtype=torch.float64))
+
+
+def test_dependent_launches_capture_into_a_cuda_graph(cavity):
+    """The zero fill, the element kernel launched as its dependent and the
+    Dirichlet kernels launched as dependents replay from a CUDA graph with
+    the eager results (FP64: the reductions' order may differ, within 1e-13)."""
+    t = cavity
+    nd = t["nd"]
+    state = dev(meshes.cavity_state(t["cp2"], t["nv"], seed=7))
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(t["amap"].pattern())
+    r_ref, v_ref = reference(t, state, "fp32_quad", False)
+
+    def step():
+        A.assembleTaylorHood(t["amap"], t["coords"], t["c6"], 1e-2, state, res, jac,
+                             precision="fp32_quad")
+        A.replaceRes(t["bc"], state, t["bvals"], res)
+        A.replaceRows(t["bc"], jac, 1.0)
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        step()                      # warm-up outside the capture
+    torch.cuda.current_stream().wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+    res.fill_(3.0)
+    jac.vals.fill_(3.0)
+    for _ in range(2):
+        g.replay()
+    torch.cuda.synchronize()
+    assert rel(res, r_ref) <= 1e-13 and rel(jac.vals, v_ref) <= 1e-13
+    t["amap"].check()
+
+
+def test_host_newton_system_captures_into_a_cuda_graph(cavity):
+    """The host-state entry forks its side stream from the capturing stream
+    and joins it back, so the whole call (copies included) replays from a
+    graph; the host residual follows the pinned host state on replay."""
+    t = cavity
+    nd = t["nd"]
+    state_np = meshes.cavity_state(t["cp2"], t["nv"], seed=8)
+    state_host = torch.from_numpy(state_np).pin_memory()
+    res_host = torch.empty(nd, dtype=torch.float64).pin_memory()
+    state_d = torch.empty(nd, dtype=torch.float64, device="cuda")
+    res = torch.empty(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(t["amap"].pattern())
+
+    def call():
+        A.newtonSystemTaylorHoodHost(t["amap"], t["bc"], t["coords"], t["c6"], 1e-2,
+                                     state_host, state_d, t["bvals"], res, jac, res_host,
+                                     precision="fp64")
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        call()
+    torch.cuda.current_stream().wait_stream(side)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        call()
+    state2 = meshes.cavity_state(t["cp2"], t["nv"], seed=9)
+    state_host.copy_(torch.from_numpy(state2))
+    res_host.fill_(0.0)
+    g.replay()
+    torch.cuda.synchronize()
+    r_ref, v_ref = reference(t, dev(state2), "fp64", False)
+    assert rel(res_host.cuda(), r_ref) <= 1e-13 and rel(jac.vals, v_ref) <= 1e-13
