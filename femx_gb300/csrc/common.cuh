@@ -267,6 +267,28 @@ __device__ __forceinline__ float f64ToF32(double d)
   return __uint_as_float(r);
 }
 
+// 1/x in FP64 by Newton-Raphson refinement of a single-precision seed: each
+// step r <- r + r (1 - x r) squares the relative error, so the seed's 2^-22
+// becomes 2^-44 and then falls below double rounding; the result is within
+// two ulps of the correctly rounded reciprocal. Four FP64 FMAs replace the
+// division sequence (GB300's FP64 pipe is the scarce one). |x| outside
+// [2^-120, 2^120] (the seed would leave the float range) takes the division.
+__device__ __forceinline__ double rcpF64(double x)
+{
+  const unsigned e = (static_cast<unsigned>(__double2hiint(x)) >> 20) & 0x7ffu;
+  if (e - (1023u - 120u) > 240u)
+  {
+    return 1.0 / x;
+  }
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(f64ToF32(x)));
+  double r = f32ToF64(r0);
+  double d = fma(-x, r, 1.0);
+  r        = fma(r, d, r);
+  d        = fma(-x, r, 1.0);
+  return fma(r, d, r);
+}
+
 template <class T>
 __device__ __forceinline__ T fromF64(double d);
 template <>

@@ -55,7 +55,15 @@ __device__ __forceinline__ bool elementK(double2 x0, double2 x1, double2 x2,
   }
   // h1 = (by, -bx), h2 = (-ay, ax), h0 = -(h1 + h2) = (ay - by, bx - ax)
   const T h0x = ay - by, h0y = bx - ax;
-  const T s   = gbfem::fromF64<T>(kappa) * T(0.5) / adet;
+  T s;
+  if constexpr (std::is_same<T, double>::value)
+  {
+    s = kappa * 0.5 * gbfem::rcpF64(adet);
+  }
+  else
+  {
+    s = gbfem::fromF64<T>(kappa) * T(0.5) / adet;
+  }
   K.k01       = s * (h0x * by - h0y * bx);
   K.k02       = s * (-h0x * ay + h0y * ax);
   K.k12       = s * (-by * ay - bx * ax);
