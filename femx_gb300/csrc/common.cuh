@@ -289,6 +289,29 @@ __device__ __forceinline__ double rcpF64(double x)
   return fma(r, d, r);
 }
 
+// 1/sqrt(x) in FP64 by the same scheme: a single-precision seed and two
+// Newton-Raphson steps y <- y + (y/2)(1 - x y^2) (quadratic convergence),
+// within two ulps of the correctly rounded value. x outside [2^-120, 2^120]
+// (including 0) takes 1 / sqrt(x).
+__device__ __forceinline__ double rsqrtF64(double x)
+{
+  const unsigned e = (static_cast<unsigned>(__double2hiint(x)) >> 20) & 0x7ffu;
+  if (e - (1023u - 120u) > 240u || __double2hiint(x) < 0)
+  {
+    return 1.0 / sqrt(x);
+  }
+  float y0;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(f64ToF32(x)));
+  double y = f32ToF64(y0);
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+  {
+    const double d = fma(-x * y, y, 1.0);
+    y              = fma(0.5 * y, d, y);
+  }
+  return y;
+}
+
 template <class T>
 __device__ __forceinline__ T fromF64(double d);
 template <>

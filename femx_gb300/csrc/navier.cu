@@ -58,6 +58,9 @@ struct NsArgs
   const int*           conn;  // [ne][3]
   const double2*       coords;
   double               rho, mu, dt;
+  // host-side constants, so that no kernel divides by them: 1/dt, 2/dt,
+  // (2/dt)^2, rho/dt, 1/rho, nu = mu/rho
+  double               inv_dt, two_dt, time2, rho_dt, inv_rho, nu;
   int                  step, num_hist;
   const double*        hist;  // [num_hist][num_states]
   const double*        nxt;
@@ -106,7 +109,7 @@ __device__ bool loadElement(const NsArgs& a, int e, NsElem& E)
     gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
     return false;
   }
-  const double inv = 1.0 / det;
+  const double inv = gbfem::rcpF64(det);
   const double i0 = J3 * inv, i1 = -J1 * inv, i2 = -J2 * inv, i3 = J0 * inv;
   // dN/dx_d = sum_b dN^/dr_b invJ[b][d], dN^/dr = (-1,-1), (1,0), (0,1)
   E.g[0][0] = -i0 - i2;
@@ -143,6 +146,7 @@ __device__ bool loadElement(const NsArgs& a, int e, NsElem& E)
 struct NsQp
 {
   double N[3], u[2], adv[2], ag[2], tau, speed, h, sum, dir[2];
+  double inv_speed, inv_h; // 1/|u| (when not fallback), 1/h = sum/2 (when h > 0)
   bool   fallback;
 };
 
@@ -161,32 +165,42 @@ __device__ __forceinline__ void pointState(const NsArgs& a, const NsElem& E, int
   {
     P.ag[c] = E.grad[c][0] * P.adv[0] + E.grad[c][1] * P.adv[1];
   }
-  const double speed = sqrt(P.u[0] * P.u[0] + P.u[1] * P.u[1]);
+  // The same quantities as femx's evalQp/elemLength with the divisions and
+  // square roots recast: |u| = s2 / sqrt(s2) from one reciprocal square root,
+  // u/|u| as a product, h = 2/sum enters only as (2|u|/h) = |u| sum and
+  // (4 nu/h^2) = nu sum^2; tau = 1/sqrt(...) from rsqrtF64 (the FP64 pipe
+  // is GB300's scarce resource; results agree with the divided forms to a
+  // few ulps).
+  const double s2  = P.u[0] * P.u[0] + P.u[1] * P.u[1];
+  const double is  = s2 > 0.0 ? gbfem::rsqrtF64(s2) : 0.0;
+  const double speed = s2 * is;
   P.fallback         = !(speed > 1.0e-10);
+  P.inv_speed        = is;
   if (!P.fallback)
   {
-    P.dir[0] = P.u[0] / speed;
-    P.dir[1] = P.u[1] / speed;
+    P.dir[0] = P.u[0] * is;
+    P.dir[1] = P.u[1] * is;
   }
   else
   {
-    P.dir[0] = P.dir[1] = 1.0 / sqrt(2.0);
+    P.dir[0] = P.dir[1] = 0.70710678118654752440; // 1/sqrt(2)
   }
   double sum = 0.0;
   for (int i = 0; i < 3; ++i)
   {
     sum += fabs(P.dir[0] * E.g[i][0] + P.dir[1] * E.g[i][1]);
   }
-  const double h    = sum > 1.0e-14 ? 2.0 / sum : 0.0;
-  const double nu   = a.mu / a.rho;
-  const double time = (2.0 / a.dt) * (2.0 / a.dt);
-  double       flow = 0.0, diff = 0.0;
-  if (h > 0.0)
+  double h = 0.0, flow = 0.0, diff = 0.0;
+  P.inv_h  = 0.0;
+  if (sum > 1.0e-14)
   {
-    flow = (2.0 * speed / h) * (2.0 * speed / h);
-    diff = (4.0 * nu / (h * h)) * (4.0 * nu / (h * h));
+    h          = 2.0 * gbfem::rcpF64(sum);
+    P.inv_h    = 0.5 * sum;
+    const double fs = speed * sum, ds = a.nu * sum * sum;
+    flow       = fs * fs;
+    diff       = ds * ds;
   }
-  P.tau   = 1.0 / sqrt(time + flow + diff);
+  P.tau   = gbfem::rsqrtF64(a.time2 + flow + diff);
   P.speed = speed;
   P.h     = h;
   P.sum   = sum;
@@ -216,7 +230,7 @@ __global__ void __launch_bounds__(kThreads) nsAssembleKernel(NsArgs a)
   {
     return; // reported through the status word; the element adds nothing
   }
-  const double rho = a.rho, mu = a.mu, dt = a.dt;
+  const double rho = a.rho, mu = a.mu;
   double       Ss[3][3] = {}, T[3] = {}, Pj[3] = {}, Fv[3][2] = {}, V[2] = {}, Tt = 0.0;
   double       Nsum[3] = {};
   for (int q = 0; q < kQ; ++q)
@@ -228,10 +242,10 @@ __global__ void __launch_bounds__(kThreads) nsAssembleKernel(NsArgs a)
     {
       dv[i]  = E.g[i][0] * P.adv[0] + E.g[i][1] * P.adv[1];
       s[i]   = P.N[i] + P.tau * dv[i];
-      phi[i] = (2.0 / dt) * P.N[i] + dv[i];
+      phi[i] = a.two_dt * P.N[i] + dv[i];
       Nsum[i] += P.N[i];
     }
-    const double w[2] = {P.u[0] / dt - 0.5 * P.ag[0], P.u[1] / dt - 0.5 * P.ag[1]};
+    const double w[2] = {P.u[0] * a.inv_dt - 0.5 * P.ag[0], P.u[1] * a.inv_dt - 0.5 * P.ag[1]};
     for (int i = 0; i < 3; ++i)
     {
       for (int j = 0; j < 3; ++j)
@@ -310,7 +324,7 @@ __global__ void __launch_bounds__(kThreads) nsAssembleKernel(NsArgs a)
     for (int j = 0; j < 3; ++j)
     {
       const double gd  = E.g[i][0] * E.g[j][0] + E.g[i][1] * E.g[j][1];
-      const double kpp = gd * Jw * Tt / rho;
+      const double kpp = gd * Jw * Tt * a.inv_rho;
       r += kpp * x[6 + j];
       for (int dd = 0; dd < 2; ++dd)
       {
@@ -354,7 +368,8 @@ __global__ void __launch_bounds__(kThreads, 1) nsHistVjpKernel(NsArgs a)
   {
     return;
   }
-  const double rho = a.rho, mu = a.mu, dt = a.dt, nu = mu / rho;
+  const double rho = a.rho, mu = a.mu, nu = a.nu;
+  const double idt = a.inv_dt, rdt = a.rho_dt, irho = a.inv_rho;
   double       x[kDofs], ad[kDofs];
   for (int k = 0; k < kDofs; ++k)
   {
@@ -399,11 +414,11 @@ __global__ void __launch_bounds__(kThreads, 1) nsHistVjpKernel(NsArgs a)
     for (int c = 0; c < 2; ++c)
     {
       const double xm = X[c] - P.u[c], dg = Dv[c] + P.ag[c];
-      Ptau += rho / dt * Av[c] * xm + 0.5 * rho * Av[c] * dg + Av[c] * Gp[c];
-      Ptau += GAP[c] * (X[c] / dt + 0.5 * Dv[c] + Gp[c] / rho - P.u[c] / dt + 0.5 * P.ag[c]);
+      Ptau += rdt * Av[c] * xm + 0.5 * rho * Av[c] * dg + Av[c] * Gp[c];
+      Ptau += GAP[c] * (X[c] * idt + 0.5 * Dv[c] + Gp[c] * irho - P.u[c] * idt + 0.5 * P.ag[c]);
       W[c]   = 0.5 * rho * A[c] + 0.5 * tau * rho * Av[c] + 0.5 * tau * GAP[c];
-      PAv[c] = tau * rho / dt * xm + 0.5 * tau * rho * dg + tau * Gp[c];
-      du[c]  = -rho / dt * A[c] - tau * rho / dt * Av[c] - tau / dt * GAP[c];
+      PAv[c] = tau * rdt * xm + 0.5 * tau * rho * dg + tau * Gp[c];
+      du[c]  = -rdt * A[c] - tau * rdt * Av[c] - tau * idt * GAP[c];
     }
     // tau(u) through |u| and h(u/|u|): dtau = -tau^3/2 d(flow + diff)
     if (P.h > 0.0)
@@ -418,15 +433,16 @@ __global__ void __launch_bounds__(kThreads, 1) nsHistVjpKernel(NsArgs a)
           dh[0] += sg * (E.g[i][0] - gr * P.dir[0]);
           dh[1] += sg * (E.g[i][1] - gr * P.dir[1]);
         }
-        const double f = -2.0 / (P.sum * P.sum * P.speed);
+        const double f = -0.5 * (P.h * P.h) * P.inv_speed; // -2/(sum^2 |u|), 1/sum = h/2
         dh[0] *= f;
         dh[1] *= f;
       }
       const double h = P.h, t3 = tau * tau * tau;
+      const double ih = P.inv_h, ih3 = ih * ih * ih, ih5 = ih3 * ih * ih;
       for (int c = 0; c < 2; ++c)
       {
-        const double dflow = 8.0 * (P.u[c] * h - P.speed * P.speed * dh[c]) / (h * h * h);
-        const double ddiff = -64.0 * nu * nu * dh[c] / (h * h * h * h * h);
+        const double dflow = 8.0 * (P.u[c] * h - P.speed * P.speed * dh[c]) * ih3;
+        const double ddiff = -64.0 * nu * nu * dh[c] * ih5;
         du[c] += Ptau * (-0.5 * t3 * (dflow + ddiff));
       }
     }
@@ -480,6 +496,12 @@ NsArgs makeArgs(const gbfem_assembly_map* map, int num_nodes, const double* coor
   a.rho        = rho;
   a.mu         = mu;
   a.dt         = dt;
+  a.inv_dt     = 1.0 / dt;
+  a.two_dt     = 2.0 / dt;
+  a.time2      = (2.0 / dt) * (2.0 / dt);
+  a.rho_dt     = rho / dt;
+  a.inv_rho    = 1.0 / rho;
+  a.nu         = mu / rho;
   a.step       = step;
   a.num_hist   = num_hist;
   a.hist       = hist;
