@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     const double  ad  = det < 0.0 ? -det : det;
     if (ad >= 1.0e-30)
     {
-      const double inv = 1.0 / det;
+      const double inv = gbfem::rcpF64(det);
       const double i00 = j11 * inv, i01 = -j01 * inv, i10 = -j10 * inv, i11 = j00 * inv;
       aInvJ[0]         = ad * i00;
       aInvJ[1]         = ad * i01;

@@ -417,7 +417,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       if (kRes64)
       {
         const double ddet = dj00 * dj11 - dj01 * dj10;
-        const double dinv = 1.0 / ddet;
+        const double dinv = gbfem::rcpF64(ddet);
         R64->invJ[0]       = dj11 * dinv;
         R64->invJ[1]       = -dj01 * dinv;
         R64->invJ[2]       = -dj10 * dinv;
@@ -431,7 +431,15 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       if (ad >= T(1.0e-30))
       {
         S.ok        = 1;
-        const T inv = T(1) / det;
+        T inv;
+        if constexpr (std::is_same<T, double>::value)
+        {
+          inv = gbfem::rcpF64(det);
+        }
+        else
+        {
+          inv = T(1) / det;
+        }
         const T i00 = j11 * inv, i01 = -j01 * inv;
         const T i10 = -j10 * inv, i11 = j00 * inv;
         S.invJ[0]   = i00;
@@ -863,7 +871,7 @@ __device__ __forceinline__ void thResidualElem(const ThArgs& a, int e, const ThR
     gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
     return;
   }
-  const double inv   = 1.0 / det;
+  const double inv   = gbfem::rcpF64(det);
   const S      iJ[4] = {sFromF64<S>(j11 * inv), sFromF64<S>(-j01 * inv),
                         sFromF64<S>(-j10 * inv), sFromF64<S>(j00 * inv)};
   const S      ad    = sFromF64<S>(fabs(det));
