@@ -151,6 +151,23 @@ __device__ __forceinline__ void awaitPrerequisites()
 // primary.
 void zeroForNext(double* a, long long na, double* b, long long nb, cudaStream_t s);
 
+// A second stream owned by the calling host thread, with its own events,
+// for work that runs beside the caller's stream inside one library call
+// (fork: event on the caller's stream, side stream waits; join: the
+// reverse). Created on the thread's first use (setup); later calls
+// allocate nothing. Fork/join through events is CUDA-graph capturable.
+struct SideStream
+{
+  static constexpr int kEvents = 8;
+  int                  dev     = -1;
+  cudaStream_t         s       = nullptr;
+  cudaEvent_t          ev[kEvents]{};
+  void                 release();
+  void                 ensure();
+  ~SideStream() { release(); }
+};
+SideStream& sideStream(); // this thread's, ensured for the current device
+
 // A launch as a dependent (dependent = true) or an ordinary one.
 template <class... P, class... A>
 void launchMaybeDependent(bool dependent, void (*kernel)(P...), unsigned grid, unsigned block,

@@ -246,6 +246,48 @@ int smCount()
 
 } // namespace
 
+void SideStream::release()
+{
+  for (cudaEvent_t& e : ev)
+  {
+    if (e != nullptr)
+    {
+      cudaEventDestroy(e);
+      e = nullptr;
+    }
+  }
+  if (s != nullptr)
+  {
+    cudaStreamDestroy(s);
+    s = nullptr;
+  }
+  dev = -1;
+}
+
+void SideStream::ensure()
+{
+  int d = 0;
+  cudaCheck(cudaGetDevice(&d), "cudaGetDevice");
+  if (d == dev)
+  {
+    return;
+  }
+  release();
+  cudaCheck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "side stream");
+  for (cudaEvent_t& e : ev)
+  {
+    cudaCheck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "side event");
+  }
+  dev = d;
+}
+
+SideStream& sideStream()
+{
+  thread_local SideStream side;
+  side.ensure();
+  return side;
+}
+
 void zeroForNext(double* a, long long na, double* b, long long nb, cudaStream_t s)
 {
   if (na <= 0 && nb <= 0)

@@ -8,8 +8,7 @@
 //   side stream : zero fill of res/J ─┘                       └─ D2H residual ┘
 // so the call costs max(H2D, zero fill) + assembly + replaceRes +
 // max(D2H, replaceRows) instead of their sum. The side stream and its
-// events belong to the calling host thread and are created on its first
-// call (setup); later calls allocate nothing.
+// events belong to the calling host thread (gbfem::sideStream).
 #include <string>
 
 #include "common.cuh"
@@ -24,51 +23,6 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
 
 namespace
 {
-
-struct SideStream
-{
-  int          dev = -1;
-  cudaStream_t s   = nullptr;
-  cudaEvent_t  ev[4]{};
-
-  void release()
-  {
-    for (cudaEvent_t& e : ev)
-    {
-      if (e != nullptr)
-      {
-        cudaEventDestroy(e);
-        e = nullptr;
-      }
-    }
-    if (s != nullptr)
-    {
-      cudaStreamDestroy(s);
-      s = nullptr;
-    }
-    dev = -1;
-  }
-  ~SideStream() { release(); }
-
-  void ensure()
-  {
-    int d = 0;
-    gbfem::cudaCheck(cudaGetDevice(&d), "cudaGetDevice");
-    if (d == dev)
-    {
-      return;
-    }
-    release();
-    gbfem::cudaCheck(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "side stream");
-    for (cudaEvent_t& e : ev)
-    {
-      gbfem::cudaCheck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "side event");
-    }
-    dev = d;
-  }
-};
-
-thread_local SideStream g_side;
 
 void checkCode(int code)
 {
@@ -97,8 +51,8 @@ extern "C" int gbfem_newton_system_th_ns_host(
     require(vals == nullptr || bc->layout_id == map->layout_id,
             "BoundaryMap was built for another CSR pattern");
     cudaStream_t s = asStream(stream);
-    g_side.ensure();
-    cudaStream_t s2 = g_side.s;
+    SideStream&  g_side = sideStream();
+    cudaStream_t s2     = g_side.s;
     // fork after the work already queued on the user stream
     cudaCheck(cudaEventRecord(g_side.ev[0], s), "fork");
     cudaCheck(cudaStreamWaitEvent(s2, g_side.ev[0], 0), "fork");

@@ -946,6 +946,7 @@ __device__ __forceinline__ void thResidualElem(const ThArgs& a, int e, const ThR
       r[12 + b] = sNorm(sFma(-rd.P[q][b], dq, r[12 + b]));
     }
   }
+  gbfem::awaitPrerequisites(); // the residual's zero fill may still be running
 #pragma unroll
   for (int l = 0; l < 15; ++l)
   {
