@@ -136,7 +136,7 @@ SIGNATURES = {
     "gbfem_batch_destroy": (None, [_vp]),
     "gbfem_probe_convert": (_i, [_i, _vp, _vp, _vp, _vp]),
     "gbfem_probe_convert_ftz": (_i, [_i, _vp, _vp, _vp]),
-    "gbfem_probe_rcp": (_i, [_i, _vp, _vp, _vp]),
+    "gbfem_probe_rcp": (_i, [_i, _vp, _vp, _i, _vp]),
 }
 
 _lib = None

@@ -48,24 +48,24 @@ __global__ void convertFtzProbe(int n, const float* in, double* out)
     out[i] = gbfem::f32ToF64Ftz(in[i]);
   }
 }
-__global__ void rcpProbe(int n, const double* in, double* out)
+__global__ void rcpProbe(int n, const double* in, double* out, int rsqrt)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n)
   {
-    out[i] = gbfem::rcpF64(in[i]);
+    out[i] = rsqrt ? gbfem::rsqrtF64(in[i]) : gbfem::rcpF64(in[i]);
   }
 }
 } // namespace
 
-extern "C" int gbfem_probe_rcp(int n, const double* in, double* out, void* stream)
+extern "C" int gbfem_probe_rcp(int n, const double* in, double* out, int rsqrt, void* stream)
 {
   using namespace gbfem;
   return guarded([&] {
     require(n >= 0 && (n == 0 || (in && out)), "probe arguments are invalid");
     if (n > 0)
     {
-      rcpProbe<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, in, out);
+      rcpProbe<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, in, out, rsqrt);
       cudaCheck(cudaGetLastError(), "reciprocal probe launch");
     }
   });

@@ -31,9 +31,10 @@ GBFEM_API int gbfem_probe_convert(int n, const double* in, float* out_f,
  * floats become zeros of the same sign. */
 GBFEM_API int gbfem_probe_convert_ftz(int n, const float* in, double* out, void* stream);
 
-/* Test hook for the FP64 reciprocal of the plain-FP64 P1 element (a float
- * seed refined by two Newton-Raphson steps): out[i] = 1 / in[i]. */
-GBFEM_API int gbfem_probe_rcp(int n, const double* in, double* out, void* stream);
+/* Test hook for the FP64 reciprocal and reciprocal square root of the FP64
+ * kernels (a float seed refined by two Newton-Raphson steps):
+ * out[i] = 1 / in[i] (rsqrt == 0) or 1 / sqrt(in[i]) (rsqrt != 0). */
+GBFEM_API int gbfem_probe_rcp(int n, const double* in, double* out, int rsqrt, void* stream);
 
 #ifdef __cplusplus
 }

@@ -93,7 +93,7 @@ def test_newton_reciprocal_is_within_two_ulps():
     xd = torch.from_numpy(x).cuda()
     out = torch.empty_like(xd)
     _lib.check(_lib.lib().gbfem_probe_rcp(xd.numel(), C.c_void_p(xd.data_ptr()),
-                                          C.c_void_p(out.data_ptr()),
+                                          C.c_void_p(out.data_ptr()), 0,
                                           C.c_void_p(torch.cuda.current_stream().cuda_stream)))
     torch.cuda.synchronize()
     got = out.cpu().numpy()
@@ -103,3 +103,24 @@ def test_newton_reciprocal_is_within_two_ulps():
     ulp = np.abs(got[fin] - ref[fin]) / np.spacing(np.abs(ref[fin]))
     assert ulp.max() <= 2.0
     assert np.array_equal(got[~fin], ref[~fin])
+
+
+def test_newton_reciprocal_square_root_is_within_two_ulps():
+    from femx_gb300 import _lib
+    rng = np.random.default_rng(5)
+    x = np.concatenate([np.abs(rng.standard_normal(1 << 18)) * 10.0 ** rng.integers(-35, 35, size=1 << 18),
+                        np.array([1.0, 4.0, 2.0, 1e-30, 1e30, 2.0 ** -120, 2.0 ** 120,
+                                  2.0 ** -121, 2.0 ** 122, 1e-300, 1e300, 0.0, -1.0])])
+    xd = torch.from_numpy(x).cuda()
+    out = torch.empty_like(xd)
+    _lib.check(_lib.lib().gbfem_probe_rcp(xd.numel(), C.c_void_p(xd.data_ptr()),
+                                          C.c_void_p(out.data_ptr()), 1,
+                                          C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ref = 1.0 / np.sqrt(x)
+    fin = np.isfinite(ref) & (ref != 0)
+    ulp = np.abs(got[fin] - ref[fin]) / np.spacing(np.abs(ref[fin]))
+    assert ulp.max() <= 2.0
+    assert np.isinf(got[x == 0.0]).all() and np.isnan(got[x < 0]).all()
