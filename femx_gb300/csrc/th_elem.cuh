@@ -391,15 +391,41 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       sm.lam[le][l] = gbfem::fromF64<T>(a.lam[a.dofs[15 * e + l]]);
     }
   }
+  // Geometry, spread over the element's lanes: lanes 0-5 check one
+  // connectivity entry each, lanes 0-2 load their vertex, lanes 1 and 2 form
+  // the FP64 edge vectors x_v - x_0 (they carry the mesh scale) and convert
+  // them; lane 15 forms the inverse Jacobian from the shuffled edges and
+  // stores it. Every lane runs the shuffles (the warp is converged here).
+  constexpr unsigned kAll = 0xffffffffu;
+  int                node = 0;
+  bool               bad  = false;
+  if (has && l < 6)
+  {
+    node = a.conn6[6 * e + l];
+    bad  = static_cast<unsigned>(node) >= static_cast<unsigned>(a.num_nodes);
+  }
+  const bool nodes_ok = ((__ballot_sync(kAll, bad) >> (threadIdx.x & 16)) & 0x3fu) == 0u;
+  double2    xv       = make_double2(0.0, 0.0);
+  if (has && nodes_ok && l < 3)
+  {
+    xv = a.coords[node];
+  }
+  const double dex = xv.x - __shfl_sync(kAll, xv.x, 0, kLanes);
+  const double dey = xv.y - __shfl_sync(kAll, xv.y, 0, kLanes);
+  const T      ex = gbfem::fromF64<T>(dex), ey = gbfem::fromF64<T>(dey);
+  // J[a][b] = d x_a / d r_b of the affine map (vertex nodes)
+  const T j00 = __shfl_sync(kAll, ex, 1, kLanes), j10 = __shfl_sync(kAll, ey, 1, kLanes);
+  const T j01 = __shfl_sync(kAll, ex, 2, kLanes), j11 = __shfl_sync(kAll, ey, 2, kLanes);
+  double  dj[4] = {0.0, 0.0, 0.0, 0.0}; // FP64 edges, for the FP64 residual only
+  if constexpr (kRes64)
+  {
+    dj[0] = __shfl_sync(kAll, dex, 1, kLanes);
+    dj[1] = __shfl_sync(kAll, dex, 2, kLanes);
+    dj[2] = __shfl_sync(kAll, dey, 1, kLanes);
+    dj[3] = __shfl_sync(kAll, dey, 2, kLanes);
+  }
   if (has && l == 15)
   {
-    bool nodes_ok = true;
-    for (int k = 0; k < 6; ++k)
-    {
-      nodes_ok = nodes_ok
-                 && static_cast<unsigned>(a.conn6[6 * e + k])
-                        < static_cast<unsigned>(a.num_nodes);
-    }
     S.ok = 0;
     if (!nodes_ok)
     {
@@ -407,25 +433,16 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     }
     else
     {
-      const double2 x0 = a.coords[a.conn6[6 * e + 0]];
-      const double2 x1 = a.coords[a.conn6[6 * e + 1]];
-      const double2 x2 = a.coords[a.conn6[6 * e + 2]];
-      // J[a][b] = d x_a / d r_b of the affine map (vertex nodes); the edge
-      // vectors carry the mesh scale and are formed in FP64, the rest in T.
-      const double dj00 = x1.x - x0.x, dj01 = x2.x - x0.x;
-      const double dj10 = x1.y - x0.y, dj11 = x2.y - x0.y;
-      if (kRes64)
+      if constexpr (kRes64)
       {
-        const double ddet = dj00 * dj11 - dj01 * dj10;
+        const double ddet = dj[0] * dj[3] - dj[1] * dj[2];
         const double dinv = gbfem::rcpF64(ddet);
-        R64->invJ[0]       = dj11 * dinv;
-        R64->invJ[1]       = -dj01 * dinv;
-        R64->invJ[2]       = -dj10 * dinv;
-        R64->invJ[3]       = dj00 * dinv;
+        R64->invJ[0]       = dj[3] * dinv;
+        R64->invJ[1]       = -dj[1] * dinv;
+        R64->invJ[2]       = -dj[2] * dinv;
+        R64->invJ[3]       = dj[0] * dinv;
         R64->ad            = fabs(ddet);
       }
-      const T j00 = gbfem::fromF64<T>(dj00), j01 = gbfem::fromF64<T>(dj01);
-      const T j10 = gbfem::fromF64<T>(dj10), j11 = gbfem::fromF64<T>(dj11);
       const T det = j00 * j11 - j01 * j10;
       const T ad  = det < T(0) ? -det : det;
       if (ad >= T(1.0e-30))
