@@ -521,3 +521,60 @@ def test_navier_degenerate_element_is_reported():
                     z[:nd].clone(), out)
     with pytest.raises(A.GbfemError, match="Singular 2D Jacobian"):
         m.check()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_quad", "mixed"])
+def test_taylor_hood_odd_element_count_matches_oracle(precision):
+    """An element count that fills neither the 8-element blocks nor the two
+    element halves of the last warp (the lanes of the missing element still
+    take part in the warp-wide shuffles of the geometry stage)."""
+    c3, k3 = meshes.jittered_tri(7, seed=4)
+    k3 = k3[:-3]                                   # 95 triangles
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    assert conn6.shape[0] % 2 == 1
+    state = meshes.cavity_state(cp2, nv, seed=6)
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-2, state)
+    tol_j, tol_r = {"fp64": (TOL64, TOL64), "fp32_quad": (TOL32, TOL32),
+                    "mixed": (TOL32, TOL64)}[precision]
+    _, res, vals = th_gpu(cp2, conn6, dofs, nd, 1e-2, state, precision)
+    assert rel_inf(res, rres) <= tol_r
+    assert rel_inf(vals, rvals) <= tol_j
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_quad"])
+def test_taylor_hood_connectivity_out_of_range_is_reported(precision):
+    """A P2 node index past the coordinate array is reported through the
+    status word (no coordinate is read for that element) and the element
+    adds nothing; the others are assembled."""
+    c3, k3 = meshes.structured_tri(4)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    bad = conn6.copy()
+    bad[9][4] = cp2.shape[0] + 5                   # an edge node of element 9
+    state = meshes.cavity_state(cp2, nv, seed=1)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleTaylorHood(m, dev(cp2), dev(bad, torch.int32), 1e-2, dev(state), res, jac,
+                         precision=precision)
+    with pytest.raises(A.GbfemError, match="connectivity is out of range"):
+        m.check()
+    # the oracle: the whole mesh minus element 9 alone (scattered into the
+    # whole mesh's pattern, which element 9 still shapes)
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-2, state)
+    d9 = dofs[15 * 9:15 * 10].copy()
+    o9 = np.array([0, 15], dtype=np.int32)
+    om9 = orc.AssemblyMap(nd, nd, o9, d9, o9, d9)
+    r9, v9 = orc.assemble_th_ns(om9, cp2, conn6[9:10], 1e-2, state)
+    rres = rres - r9
+    for r in np.unique(d9):
+        full = {int(c): k for k, c in enumerate(om.col_ind[om.row_ptr[r]:om.row_ptr[r + 1]],
+                                                  start=int(om.row_ptr[r]))}
+        for k in range(om9.row_ptr[r], om9.row_ptr[r + 1]):
+            rvals[full[int(om9.col_ind[k])]] -= v9[k]
+    tol = TOL64 if precision == "fp64" else TOL32
+    assert rel_inf(host(res), rres) <= tol
+    assert rel_inf(host(jac.vals), rvals) <= tol
