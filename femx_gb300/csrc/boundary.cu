@@ -238,25 +238,29 @@ __global__ void flagPositive(int n, const int* __restrict__ in,
 
 // ---- hot-path kernels ------------------------------------------------------
 
+// Sixteen lanes per constrained row: the row's entries are zeroed (and its
+// diagonal set) by coalesced stores, instead of one thread walking the row.
+constexpr int kRowLanes = 16;
+
 __global__ void replaceRowsKernel(int nb, const int* __restrict__ row_begin,
                                   const int* __restrict__ row_end,
                                   const int* __restrict__ diag,
                                   double* __restrict__ vals, double d)
 {
-  const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t  = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ib = t / kRowLanes, j = t % kRowLanes;
   if (ib >= nb)
   {
     return;
   }
   // launched as a dependent of the assembly: the row extents are the map's
   // own (immutable) data; the values are the assembly's output
-  const int kb = row_begin[ib], ke = row_end[ib];
+  const int kb = row_begin[ib], ke = row_end[ib], kd = diag[ib];
   gbfem::awaitPrerequisites();
-  for (int k = kb; k < ke; ++k)
+  for (int k = kb + j; k < ke; k += kRowLanes)
   {
-    vals[k] = 0.0;
+    vals[k] = k == kd ? d : 0.0;
   }
-  vals[diag[ib]] = d;
 }
 
 __global__ void replaceResKernel(int nb, const int* __restrict__ bc_rows,
@@ -541,7 +545,8 @@ extern "C" int gbfem_replace_rows(const gbfem_boundary_map* b, double* vals,
     }
     require(vals != nullptr, "BoundaryMap matrix values are null");
     // dependent launches: start while the kernel before them drains
-    launchDependent(replaceRowsKernel, blocksFor(b->num_bcs, 256), 256, asStream(stream),
+    launchDependent(replaceRowsKernel, blocksFor(static_cast<long long>(b->num_bcs) * kRowLanes, 256),
+                    256, asStream(stream),
                     b->num_bcs, static_cast<const int*>(b->row_begin),
                     static_cast<const int*>(b->row_end), static_cast<const int*>(b->diag), vals, d);
     cudaCheck(cudaGetLastError(), "replaceRows launch");
