@@ -30,6 +30,12 @@ Cases
 
     python tests/golden/make_golden.py --only ns_gls   # one family of cases
     python tests/golden/make_golden.py --only gmsh
+    python tests/golden/make_golden.py --only real
+
+  real_sq_*    femx's GmshReader on the reference's data/meshes/
+               2d_square_res_very_low.msh (parsed arrays only, the file is not
+               copied) and, on that mesh moved onto the unit square, the
+               p1 / ns_gls / th cases above
 """
 from __future__ import annotations
 
@@ -214,10 +220,48 @@ def gmsh_cases(tmp):
         np.savez_compressed(os.path.join(HERE, f"gmsh_v{v}.npz"), **case_gmsh(tmp, f"g{v}", v))
 
 
+# A real unstructured mesh of the reference's own data (data/meshes), read by
+# femx's GmshReader here; the file itself is not copied: the fixtures hold
+# femx's parsed arrays and femx's assembly outputs on that mesh.
+REAL_MESHES = {"real_sq": "2d_square_res_very_low.msh"}
+
+
+def real_cases(tmp, ref):
+    import shutil
+    for name, fn in REAL_MESHES.items():
+        d = os.path.join(tmp, name + "_gmsh")
+        os.makedirs(d, exist_ok=True)
+        shutil.copyfile(os.path.join(ref, "data", "meshes", fn), os.path.join(d, "mesh.msh"))
+        run("gmsh", d)
+        mesh = {"source": np.frombuffer(fn.encode(), dtype=np.uint8),
+                "dim": read(d, "dim", np.int32), "coords": read(d, "coords", np.float64)}
+        for k in ("conn", "etag", "ptag", "fconn", "fetag", "fptag"):
+            mesh[k] = read(d, k, np.int32)
+        mesh["names"] = np.frombuffer(open(os.path.join(d, "names.txt"), "rb").read(),
+                                      dtype=np.uint8)
+        np.savez_compressed(os.path.join(HERE, name + "_mesh.npz"), **mesh)
+        # the square [-0.5, 0.5]^2 moved onto the unit square, whose edges the
+        # reference driver's Dirichlet set selects
+        coords = mesh["coords"].reshape(-1, 3)[:, :2] + 0.5  # stored as (x, y, z)
+        conn = mesh["conn"].reshape(-1, 3)
+        n, e = coords.shape[0], conn.shape[0]
+        rng = np.random.default_rng(81)
+        np.savez_compressed(os.path.join(HERE, name + "_p1.npz"), **case_p1(
+            tmp, name + "_p1", coords, conn, np.exp(rng.standard_normal(e)),
+            meshes.fourier_source(coords, 5), rng.standard_normal(n), rng.standard_normal(n),
+            rng.standard_normal(n), (0.25, -1.0, 0.5)))
+        np.savez_compressed(os.path.join(HERE, name + "_ns.npz"),
+                            **case_navier(tmp, name + "_ns", coords, conn, 1.0, 2e-3, 0.01, 3, 82))
+        th = case_th(tmp, name + "_th", coords, conn, 1e-3, 83)
+        for k in ("jac_offsets", "jac_map"):  # the test checks row_ptr/col_ind and values
+            th.pop(k)
+        np.savez_compressed(os.path.join(HERE, name + "_th.npz"), **th)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref", default="/root/reference")
-    ap.add_argument("--only", default="", help="generate one family: ns_gls, gmsh")
+    ap.add_argument("--only", default="", help="generate one family: ns_gls, gmsh, real")
     args = ap.parse_args()
     build(args.ref)
     if args.only == "ns_gls":
@@ -228,9 +272,14 @@ def main():
         with tempfile.TemporaryDirectory() as tmp:
             gmsh_cases(tmp)
         return
+    if args.only == "real":
+        with tempfile.TemporaryDirectory() as tmp:
+            real_cases(tmp, args.ref)
+        return
     with tempfile.TemporaryDirectory() as tmp:
         navier_cases(tmp)
         gmsh_cases(tmp)
+        real_cases(tmp, args.ref)
         np.savez_compressed(os.path.join(HERE, "kat.npz"), **case_kat(tmp))
 
         coords, conn = meshes.structured_tri(32)

@@ -39,6 +39,25 @@ def test_reader_matches_femx_gmsh_reader(case, tmp_path):
     assert m.names == names
 
 
+def test_reader_matches_femx_on_a_reference_data_mesh():
+    """A real unstructured mesh of the reference's own data (data/meshes,
+    Gmsh 4.1 with entities and physical groups) read by our reader against
+    femx's GmshReader output stored in the fixture real_sq_mesh. Needs the
+    reference tree, named by FEMX_REFERENCE (skipped where it is absent)."""
+    root = os.environ.get("FEMX_REFERENCE")
+    g = load_golden("real_sq_mesh")
+    path = os.path.join(root or "", "data", "meshes", bytes(g["source"]).decode())
+    if not root or not os.path.exists(path):
+        pytest.skip("the reference tree is not available (set FEMX_REFERENCE)")
+    m = mesh_io.read_gmsh(path)
+    assert m.dim == int(g["dim"][0])
+    assert np.array_equal(m.coords.reshape(-1), g["coords"])
+    assert np.array_equal(m.conn.reshape(-1), g["conn"])
+    assert np.array_equal(m.elem_etag, g["etag"]) and np.array_equal(m.elem_ptag, g["ptag"])
+    assert np.array_equal(m.facet_conn.reshape(-1), g["fconn"])
+    assert np.array_equal(m.facet_etag, g["fetag"]) and np.array_equal(m.facet_ptag, g["fptag"])
+
+
 @pytest.mark.parametrize("text,msg", [
     ("$MeshFormat\n4.1 1 8\n$EndMeshFormat\n", "only ASCII"),
     ("$MeshFormat\n3.0 0 8\n$EndMeshFormat\n", "Gmsh 2.x and 4.x"),

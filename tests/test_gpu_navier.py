@@ -19,7 +19,7 @@ from femx_gb300 import assembly as A  # noqa: E402
 from femx_gb300 import meshes  # noqa: E402
 from oracle import pyoracle as orc  # noqa: E402
 
-CASES = ["ns_gls_jit5_s0", "ns_gls_jit5_s3", "ns_gls_still4"]
+CASES = ["ns_gls_jit5_s0", "ns_gls_jit5_s3", "ns_gls_still4", "real_sq_ns"]
 
 
 @pytest.fixture(scope="module", autouse=True)
