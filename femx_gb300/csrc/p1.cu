@@ -172,8 +172,8 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     a.g_m          = g_m;
     if (g_u != nullptr)
     {
-      cudaCheck(cudaMemsetAsync(g_u, 0, sizeof(double) * map->num_states, s),
-                "VJP state zero");
+      // the VJP kernel is launched as a dependent of this zero fill
+      zeroForNext(g_u, map->num_states, nullptr, 0, s);
     }
     if (a.ne == 0 || (g_u == nullptr && g_m == nullptr))
     {
@@ -181,15 +181,16 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     }
     const unsigned blocks = blocksFor(a.ne, 256);
     const bool     sep    = conn != nullptr;
+    const bool dep = g_u != nullptr;
     if (precision != GBFEM_PREC_FP32_QUAD)
     {
-      sep ? p1VjpKernel<false, true><<<blocks, 256, 0, s>>>(a)
-          : p1VjpKernel<false, false><<<blocks, 256, 0, s>>>(a);
+      sep ? launchMaybeDependent(dep, p1VjpKernel<false, true>, blocks, 256, s, a)
+          : launchMaybeDependent(dep, p1VjpKernel<false, false>, blocks, 256, s, a);
     }
     else
     {
-      sep ? p1VjpKernel<true, true><<<blocks, 256, 0, s>>>(a)
-          : p1VjpKernel<true, false><<<blocks, 256, 0, s>>>(a);
+      sep ? launchMaybeDependent(dep, p1VjpKernel<true, true>, blocks, 256, s, a)
+          : launchMaybeDependent(dep, p1VjpKernel<true, false>, blocks, 256, s, a);
     }
     cudaCheck(cudaGetLastError(), "P1 VJP launch");
   });

@@ -159,6 +159,7 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
   }
   if (kVjp)
   {
+    gbfem::awaitPrerequisites(); // g_u's zero fill may still be running
     const T l0 = gbfem::fromF64<T>(a.lam[d0]), l1 = gbfem::fromF64<T>(a.lam[d1]);
     const T l2 = gbfem::fromF64<T>(a.lam[d2]);
     // K is symmetric: K^T lam = K lam.
