@@ -466,6 +466,7 @@ __global__ void __launch_bounds__(kThreads, 1) nsHistVjpKernel(NsArgs a)
   }
   const double Jw  = E.jxw;
   const double al0 = E.ab2 ? 1.5 : 1.0;
+  gbfem::awaitPrerequisites(); // the output's zero fill may still be running
   for (int i = 0; i < 3; ++i)
   {
     for (int c = 0; c < 2; ++c)
@@ -581,8 +582,8 @@ extern "C" int gbfem_vjp_navier_hist(const gbfem_assembly_map* map, int num_node
     require(out != nullptr, "VJP output is null");
     require(out != hist && out != nxt && out != adj, "VJP output must not alias its inputs");
     cudaStream_t s = asStream(stream);
-    cudaCheck(cudaMemsetAsync(out, 0, sizeof(double) * num_hist * static_cast<size_t>(map->num_states), s),
-              "VJP zero");
+    // the VJP kernel is launched as a dependent of this zero fill
+    zeroForNext(out, num_hist * static_cast<long long>(map->num_states), nullptr, 0, s);
     if (map->num_elems == 0)
     {
       return;
@@ -590,7 +591,7 @@ extern "C" int gbfem_vjp_navier_hist(const gbfem_assembly_map* map, int num_node
     NsArgs a = makeArgs(map, num_nodes, coords, conn, rho, mu, dt, step, num_hist, hist, nxt);
     a.adj    = adj;
     a.out    = out;
-    nsHistVjpKernel<<<blocksFor(a.ne, kThreads), kThreads, 0, s>>>(a);
+    launchDependent(nsHistVjpKernel, blocksFor(a.ne, kThreads), kThreads, s, a);
     cudaCheck(cudaGetLastError(), "Navier history VJP launch");
   });
 }

@@ -441,7 +441,8 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
     cudaStream_t s = asStream(stream);
-    cudaCheck(cudaMemsetAsync(g_state, 0, sizeof(double) * map->num_states, s), "VJP zero");
+    // the VJP kernel is launched as a dependent of this zero fill
+    zeroForNext(g_state, map->num_states, nullptr, 0, s);
     if (map->num_elems == 0)
     {
       return;
@@ -461,8 +462,9 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
     a.status    = map->status;
     const unsigned blocks = blocksFor(a.ne, kElemsPerBlock);
     // MIXED keeps the Jacobian (and so J^T lam) in FP32 quadrature
-    precision == GBFEM_PREC_FP64 ? thVjpKernel<double, false><<<blocks, kThreads, 0, s>>>(a)
-                                 : thVjpKernel<float, false><<<blocks, kThreads, 0, s>>>(a);
+    precision == GBFEM_PREC_FP64
+        ? launchDependent(thVjpKernel<double, false>, blocks, kThreads, s, a)
+        : launchDependent(thVjpKernel<float, false>, blocks, kThreads, s, a);
     cudaCheck(cudaGetLastError(), "Taylor-Hood VJP launch");
   });
 }
