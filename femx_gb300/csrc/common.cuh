@@ -121,6 +121,7 @@ enum DeviceErr : int
   kDevRowOverflow       = 9,
   kDevPatternInvalid    = 10,
   kDevNodeRange         = 11,
+  kDevStageTimeout      = 12,
 };
 
 __device__ inline void devFail(DeviceStatus* st, int code, int index)
@@ -132,6 +133,46 @@ __device__ inline void devFail(DeviceStatus* st, int code, int index)
 }
 
 const char* deviceErrorMessage(int code);
+
+// One-dimensional bulk copy global -> shared memory by the tensor memory
+// accelerator (cp.async.bulk), its completion counted in bytes on an
+// mbarrier. Call from every thread of the block: thread 0 initialises the
+// barrier and issues the copy; all threads wait for the barrier's phase 0.
+// dst and src 16-byte aligned, bytes a multiple of 16. The wait is bounded
+// (try_wait suspends for a hardware time slice per attempt); it returns
+// false if the copy has not landed after kStageSpin attempts, and the
+// caller reports that through its status word.
+constexpr int kStageSpin = 1 << 20;
+
+__device__ __forceinline__ bool bulkStage(void* dst, const void* src, unsigned bytes,
+                                          unsigned long long* bar)
+{
+  const unsigned b = static_cast<unsigned>(__cvta_generic_to_shared(bar));
+  const unsigned d = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  if (threadIdx.x == 0)
+  {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+                 "%2, [%3];" ::"r"(d),
+                 "l"(src), "r"(bytes), "r"(b)
+                 : "memory");
+  }
+  __syncthreads();
+  unsigned done = 0;
+  for (int it = 0; it < kStageSpin && done == 0; ++it)
+  {
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(b)
+                 : "memory");
+  }
+  return done != 0;
+}
 
 // Programmatic dependent launch (sm_90+). zeroForNext() clears the output
 // arrays of the assembly that follows it on the stream, in a kernel that

@@ -334,6 +334,8 @@ const char* deviceErrorMessage(int code)
     return "CSR pattern row pointers or column indices are invalid";
   case kDevNodeRange:
     return "Geometry element connectivity is out of range";
+  case kDevStageTimeout:
+    return "Staging the reference tables in shared memory timed out";
   default:
     return "unknown device error";
   }

@@ -17,8 +17,10 @@ constexpr int kElemsPerBlock = 8;
 constexpr int kThreads       = kLanes * kElemsPerBlock;
 constexpr int kNq            = 6;
 
+// 16-byte aligned with a size that is a multiple of 16 bytes (456 values),
+// so that one bulk copy stages a table in shared memory.
 template <class R>
-struct ThRef
+struct alignas(16) ThRef
 {
   R N[kNq][6];       // P2 values at the quadrature points
   R wN[kNq][6];      // w_q N^_a(q)
@@ -263,9 +265,10 @@ struct Res64
 
 // Shared memory of one 128-thread block working on up to 8 elements.
 template <class T>
-struct ThSmem
+struct alignas(16) ThSmem
 {
   ThRef<T>      ref;
+  unsigned long long bar; // completion of the reference tables' bulk copy
   ElemShared<T> sh[kElemsPerBlock];
   // Each element's 15x15 block staged row by row (row stride 17, element
   // stride 272 = 16 mod 32 words) so that both the row-wise writes and the
@@ -283,9 +286,23 @@ struct ThSmemMixed : ThSmem<T>
   Res64 r64[kElemsPerBlock];
 };
 
+// Stages the reference tables in shared memory: one bulk copy by the tensor
+// memory accelerator when status is given (the standalone kernels), a
+// block-wide copy loop otherwise (the batched kernel). Follow with
+// __syncthreads before thBlock.
 template <class T>
-__device__ __forceinline__ void thStageRef(ThSmem<T>& sm)
+__device__ __forceinline__ void thStageRef(ThSmem<T>& sm, DeviceStatus* status = nullptr)
 {
+  static_assert(sizeof(ThRef<T>) % 16 == 0, "bulk copies move multiples of 16 bytes");
+  if (status != nullptr)
+  {
+    if (!gbfem::bulkStage(&sm.ref, refTables(T()), sizeof(ThRef<T>), &sm.bar)
+        && threadIdx.x == 0)
+    {
+      gbfem::devFail(status, gbfem::kDevStageTimeout, blockIdx.x);
+    }
+    return;
+  }
   const T* src = reinterpret_cast<const T*>(refTables(T()));
   T*       dst = reinterpret_cast<T*>(&sm.ref);
   for (int i = threadIdx.x; i < int(sizeof(ThRef<T>) / sizeof(T)); i += kThreads)
@@ -781,7 +798,7 @@ template <class T, bool kJac, bool kRes>
 __global__ void __launch_bounds__(kThreads, 12) thKernel(ThArgs a)
 {
   __shared__ ThSmem<T> sm;
-  thStageRef(sm);
+  thStageRef(sm, a.status);
   __syncthreads();
   thBlock<T, kJac, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
 }
@@ -790,7 +807,7 @@ __global__ void __launch_bounds__(kThreads, 12) thKernel(ThArgs a)
 __global__ void __launch_bounds__(kThreads) thKernelMixed(ThArgs a)
 {
   __shared__ ThSmemMixed<float> sm;
-  thStageRef(sm);
+  thStageRef(sm, a.status);
   __syncthreads();
   thBlock<float, true, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
@@ -801,7 +818,7 @@ template <class T, bool kRes>
 __global__ void __launch_bounds__(kThreads) thVjpKernel(ThArgs a)
 {
   __shared__ ThSmem<T> sm;
-  thStageRef(sm);
+  thStageRef(sm, a.status);
   __syncthreads();
   thBlock<T, true, kRes, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
@@ -991,7 +1008,7 @@ template <class T, bool kJac, bool kRes>
 __global__ void __launch_bounds__(kThreads) thKernelGather(ThArgs a)
 {
   __shared__ ThSmem<T> sm;
-  thStageRef(sm);
+  thStageRef(sm, a.status);
   __syncthreads();
   thBlock<T, kJac, kRes, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
@@ -999,7 +1016,7 @@ __global__ void __launch_bounds__(kThreads) thKernelGather(ThArgs a)
 __global__ void __launch_bounds__(kThreads) thKernelMixedGather(ThArgs a)
 {
   __shared__ ThSmemMixed<float> sm;
-  thStageRef(sm);
+  thStageRef(sm, a.status);
   __syncthreads();
   thBlock<float, true, false, false, true, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
