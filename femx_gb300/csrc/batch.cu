@@ -188,7 +188,11 @@ __global__ void __launch_bounds__(kBatchThreads)
   __shared__ typename BatchSmem<kMode>::type sm;
   __shared__ int                             prefix[kMaxInstances + 1];
   __shared__ int                             item;
-  thStageRef(sm);
+  // every instance reports into the batch's one status word
+  DeviceStatus* status = ni > 0 ? (descs[0].kind == GBFEM_BATCH_P1_KAPPA ? descs[0].p1.status
+                                                                          : descs[0].th.status)
+                                : nullptr;
+  thStageRef(sm, status);
   if (threadIdx.x == 0)
   {
     int acc = 0;

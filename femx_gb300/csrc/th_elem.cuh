@@ -287,8 +287,8 @@ struct ThSmemMixed : ThSmem<T>
 };
 
 // Stages the reference tables in shared memory: one bulk copy by the tensor
-// memory accelerator when status is given (the standalone kernels), a
-// block-wide copy loop otherwise (the batched kernel). Follow with
+// memory accelerator when a status word is given (a timed-out wait is
+// reported there), a block-wide copy loop otherwise. Follow with
 // __syncthreads before thBlock.
 template <class T>
 __device__ __forceinline__ void thStageRef(ThSmem<T>& sm, DeviceStatus* status = nullptr)
