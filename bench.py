@@ -590,6 +590,7 @@ def main():
         nnz = pat.nnz
         b_asm = 20 * e + 32 * n + 8 * nnz
         b_spmv = 12 * nnz + 20 * n
+        fp64_p1 = fp64_peak_tflops(torch, L)
         line["poisson"] = {
             "workload": f"poisson_p1_kappa_{POISSON_NX}x{POISSON_NX}_assemble_bc_{NSPMV}spmv",
             "elements_per_s": world * e / t_full, "ms_per_step": t_full * 1e3,
@@ -598,6 +599,16 @@ def main():
                          "unit": "GB/s", "frac": b_asm / t_asm / 1e9 / hbm,
                          "launch_ms": t_asm * 1e3, "traffic": traffic.get("p1_assemble"),
                          "note": "plain FP64: FP64-pipe bound on GB300"},
+            # the bound that applies: 45 FP64 instructions per element (edges 4,
+            # determinant 3, reciprocal 4, scale 2, gradient sums 2, stiffness
+            # 12, residual 9, load 9; counted from the kernel), each the issue
+            # cost of one FMA: expressed as FLOP with FMA = 2
+            "assembly_fp64_pipe": {"bound": "fp64",
+                                   "achieved": 2 * 45 * e / t_asm / 1e12,
+                                   "peak": fp64_p1, "unit": "TFLOP/s",
+                                   "frac": 2 * 45 * e / t_asm / 1e12 / fp64_p1,
+                                   "launch_ms": t_asm * 1e3,
+                                   "peak_source": "measured by gbfem_probe_fp64_fma"},
             "assembly_fp32_quad": {"bound": "hbm", "achieved": b_asm / t_asm32 / 1e9,
                                    "peak": hbm, "unit": "GB/s",
                                    "frac": b_asm / t_asm32 / 1e9 / hbm,
