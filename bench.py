@@ -615,7 +615,11 @@ def main():
                                    "launch_ms": t_asm32 * 1e3},
             "spmv": {"bound": "hbm", "achieved": b_spmv / t_spmv / 1e9, "peak": hbm,
                      "unit": "GB/s", "frac": b_spmv / t_spmv / 1e9 / hbm,
-                     "launch_ms": t_spmv * 1e3, "traffic": traffic.get("spmv")},
+                     "launch_ms": t_spmv * 1e3, "traffic": traffic.get("spmv"),
+                     # the co-bound on GB300: one FP64 FMA per nonzero
+                     "fp64_pipe": {"achieved": 2 * nnz / t_spmv / 1e12, "peak": fp64_p1,
+                                   "unit": "TFLOP/s",
+                                   "frac": 2 * nnz / t_spmv / 1e12 / fp64_p1}},
             "spmv_cusparse": ({"launch_ms": t_lib * 1e3,
                                "achieved": b_spmv / t_lib / 1e9, "unit": "GB/s",
                                "ours_speedup": t_lib / t_spmv,

@@ -7,7 +7,9 @@
 // Taylor-Hood), a warp's rows are contiguous in memory, so the 32 threads
 // together stream a contiguous stretch of vals/col_ind and L1 serves the
 // per-thread walk; each nonzero costs exactly one FP64 FMA, the minimum on a
-// part whose FP64 rate is the scarce resource. x is gathered through L2.
+// part whose FP64 rate is the scarce resource (on GB300 the FMAs alone take
+// about as long as streaming the matrix from HBM). x is gathered through L2.
+// Each lane loads one row pointer; its row end comes from the next lane.
 //
 // Semantics follow cuSPARSE (the reference's device path): y is not read when
 // beta == 0.
@@ -23,13 +25,21 @@ __global__ void __launch_bounds__(256)
              const double* __restrict__ x, double* __restrict__ y,
              double alpha, double beta)
 {
-  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  const int r    = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  // every lane of the warp takes part in the shuffle; row_ptr has rows + 1
+  // entries, so lanes past the last row read the end pointer
+  const int k0 = __ldg(row_ptr + (r < rows ? r : rows));
+  int       k1 = __shfl_down_sync(0xffffffffu, k0, 1);
+  if (lane == 31)
+  {
+    k1 = __ldg(row_ptr + (r + 1 < rows ? r + 1 : rows));
+  }
   if (r >= rows)
   {
     return;
   }
-  const int k0 = row_ptr[r], k1 = row_ptr[r + 1];
-  double    acc = 0.0;
+  double acc = 0.0;
   for (int k = k0; k < k1; ++k)
   {
     acc = fma(__ldg(vals + k), __ldg(x + __ldg(col_ind + k)), acc);
