@@ -482,6 +482,15 @@ def main():
         lt = lam_h.copy()
         lt[p["bdofs"]] = 0.0
         ogu, ogm = orc.vjp_p1_kappa(om, oq, np.exp(m_h), u_h, lt)
+        # the serial oracle VJP timed on one host core (bounded sample)
+        kap_h = np.exp(m_h)
+        n_v, t_v = 0, 0.0
+        while (rank == 0 and world == 1 and not args.no_cpu_baseline
+               and n_v < 20 and (n_v < 1 or t_v < 4.0)):
+            t0 = time.perf_counter()
+            orc.vjp_p1_kappa(om, oq, kap_h, u_h, lt)
+            t_v += time.perf_counter() - t0
+            n_v += 1
         ogu[p["bdofs"]] += lam_h[p["bdofs"]]
         hg["oracle"] = (ogu, ogm)
         direct = {"g_u": float(np.abs(hg["mixed"][0] - ogu).max() / np.abs(ogu).max()),
@@ -526,6 +535,12 @@ def main():
                          "unit": "GB/s", "frac": b_vjp / t32 / 1e9 / hbm,
                          "algorithmic_bytes": b_vjp},
         }
+        if n_v:
+            line["vjp"]["cpu_baseline"] = {
+                "grads_per_s": n_v / t_v, "ms_per_grad": t_v / n_v * 1e3, "cores": 1,
+                "kind": "port",
+                "sample": f"{n_v} state + control VJPs of the same {VJP_NX}x{VJP_NX} "
+                          f"system (serial oracle, FP64)"}
         del bcv
         del amap
 
@@ -626,6 +641,8 @@ def main():
                                "via": "torch.mv on a sparse CSR tensor (cuSPARSE SpMV)"}
                               if t_lib is not None else {"unavailable": lib_err}),
         }
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            line["poisson"].update(poisson_cpu(p, n, A, asm, bcs, rhs, jac, torch))
         del amap, bc, jac
 
     # ---------------- femx's GLS NS time operator (P1/P1, 256x256) ----------
@@ -695,7 +712,7 @@ def main():
         from femx_gb300 import meshes
         from femx_gb300.batch import Batch, P1Instance, THInstance, autotune
         rng = np.random.default_rng(5)
-        insts = []
+        insts, cpu_sample = [], []
         n_p1 = n_th = 0
         for k in range(256):
             if rng.random() < 0.5:
@@ -706,9 +723,12 @@ def main():
                 amap = A.makeAssemblyMap(nn, nn, d(offs), d(dofs), d(offs), d(dofs))
                 kappa = np.exp(meshes.grf_centroids(coords, conn, seed=2000 + k, ell=0.05,
                                                     grid=256))
-                insts.append(P1Instance(amap, d(coords), d(kappa), d(rng.standard_normal(nn)),
-                                        d(meshes.fourier_source(coords, k)),
-                                        d(rng.standard_normal(nn))))
+                u_k, f_k = rng.standard_normal(nn), meshes.fourier_source(coords, k)
+                lam_k = rng.standard_normal(nn)
+                insts.append(P1Instance(amap, d(coords), d(kappa), d(u_k), d(f_k), d(lam_k)))
+                if sum(1 for c in cpu_sample if c[0] == "p1") < 4:
+                    cpu_sample.append(("p1", ne, coords, conn, offs, dofs, kappa, u_k, f_k,
+                                       lam_k))
                 n_p1 += 1
             else:
                 nx = int(rng.integers(32, 129))
@@ -717,9 +737,11 @@ def main():
                 cp2, conn6, nv = meshes.p2_mesh(c3, k3)
                 offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
                 amap = A.makeAssemblyMap(nd, nd, d(offs), d(dofs), d(offs), d(dofs))
-                insts.append(THInstance(amap, d(cp2), d(conn6), 1.0 / re,
-                                        d(meshes.cavity_state(cp2, nv, seed=k)),
-                                        d(rng.standard_normal(nd))))
+                st_k, lam_k = meshes.cavity_state(cp2, nv, seed=k), rng.standard_normal(nd)
+                insts.append(THInstance(amap, d(cp2), d(conn6), 1.0 / re, d(st_k), d(lam_k)))
+                if sum(1 for c in cpu_sample if c[0] == "th") < 4:
+                    cpu_sample.append(("th", conn6.shape[0], cp2, conn6, offs, dofs, nd,
+                                       1.0 / re, st_k, lam_k))
                 n_th += 1
         batch = Batch(insts)
         runs, tuned = {}, {}
@@ -767,6 +789,10 @@ def main():
                                          "gradients fp64; Taylor-Hood J^T lam from the fp32 J"},
             "autotuned": tuned,
         }
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            e_p1 = sum(x.kappa.numel() for x in insts if isinstance(x, P1Instance))
+            line["batch"]["cpu_baseline"] = batch_cpu(cpu_sample, e_p1,
+                                                      batch.num_elems - e_p1)
         del insts, batch
 
     line["gpu_launches"] = launches
@@ -777,6 +803,122 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def batch_cpu(sample, e_p1, e_th):
+    """Serial oracle time of the batch's work (residual + Jacobian + VJP),
+    from a sample of its own instances: per-element rates of each physics,
+    applied to the batch's element counts."""
+    from oracle import pyoracle as orc
+    t = {"p1": 0.0, "th": 0.0}
+    n = {"p1": 0, "th": 0}
+    for rec in sample:
+        if rec[0] == "p1":
+            _, ne, coords, conn, offs, dofs, kappa, u, f, lam = rec
+            nn = coords.shape[0]
+            om = orc.AssemblyMap(nn, nn, offs, dofs, offs, dofs)
+            oq = orc.P1Quad(coords, conn)
+            t0 = time.perf_counter()
+            orc.assemble_p1_kappa(om, oq, kappa, f, u)
+            orc.vjp_p1_kappa(om, oq, kappa, u, lam)
+        else:
+            _, ne, cp2, conn6, offs, dofs, nd, nu, st, lam = rec
+            om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+            th = orc.THQuad(cp2, conn6)
+            res, vals = np.zeros(nd), np.zeros(om.nnz)
+            t0 = time.perf_counter()
+            orc.assemble_th_threads(om, th, nu, st, 1, res, vals)
+            orc.matvec_t(om.row_ptr, om.col_ind, vals, lam, nd)
+        t[rec[0]] += time.perf_counter() - t0
+        n[rec[0]] += ne
+    total = (e_p1 * t["p1"] / max(n["p1"], 1)) + (e_th * t["th"] / max(n["th"], 1))
+    return {"elements_per_s": (e_p1 + e_th) / total, "seconds_per_batch": total, "cores": 1,
+            "kind": "port",
+            "sample": f"serial oracle on {sum(1 for r in sample if r[0] == 'p1')} P1 "
+                      f"({n['p1']} elements) and {sum(1 for r in sample if r[0] == 'th')} "
+                      f"Taylor-Hood ({n['th']} elements) instances of the batch, residual + "
+                      f"Jacobian + VJP (Taylor-Hood VJP as J^T lam), per-element rates "
+                      f"applied to the batch's {e_p1} P1 and {e_th} Taylor-Hood elements"}
+
+
+def poisson_cpu(p, n, A, asm, bcs, rhs, jac, torch):
+    """The same Poisson step on one host core with the oracle (femx's generic
+    assembly has no OpenMP): assembly, prepareForwardSolve and the ten
+    products, timed in place on preallocated arrays; plus the GPU results'
+    errors against it at full size. Each GPU product is checked against the
+    oracle's product of the same input vector: along the chain itself the
+    rounding of every product is amplified by the next (interior rows of the
+    stiffness sum to zero, so each product cancels)."""
+    from oracle import pyoracle as orc
+    om = orc.AssemblyMap(n, n, p["offs"], p["dofs"], p["offs"], p["dofs"])
+    oq = orc.P1Quad(p["coords"], p["conn"])
+    ob = orc.BoundaryMap(p["bdofs"], om.row_ptr, om.col_ind)
+    lib = orc.lib()
+    kap, f = np.ascontiguousarray(p["kappa"]), np.ascontiguousarray(p["f"])
+    u0, g = np.zeros(n), np.zeros(len(p["bdofs"]))
+    r_o, v_o, ya, yb = np.zeros(n), np.zeros(om.nnz), np.zeros(n), np.zeros(n)
+    rp, ci = om.row_ptr, om.col_ind
+
+    f_p = orc._ptr(f)
+
+    def step():
+        orc._check(lib.orc_assemble_p1_kappa(om.h, oq.h, oq.conn, kap, f_p, u0, r_o, v_o))
+        np.negative(r_o, out=r_o)  # rhs = -res at u = 0
+        orc._check(lib.orc_prepare_forward_solve(ob.h, rp, v_o, r_o, g))
+        x, y = r_o, ya
+        for _ in range(NSPMV):
+            lib.orc_matvec(n, rp, ci, v_o, x, y, SPMV_SCALE, 0.0)
+            x, y = y, (yb if y is ya else ya)
+        return x
+
+    step()
+    n_s, tot = 0, 0.0
+    while n_s < 5 and (n_s < 1 or tot < 8.0):
+        t0 = time.perf_counter()
+        step()
+        tot += time.perf_counter() - t0
+        n_s += 1
+    e = p["conn"].shape[0]
+    # the GPU step once more, then its outputs against the oracle's
+    asm()
+    bcs()
+    rhs_g = rhs.cpu().numpy()
+    vals_g = jac.vals.cpu().numpy()
+    r_chk, v_chk = np.zeros(n), np.zeros(om.nnz)
+    orc._check(lib.orc_assemble_p1_kappa(om.h, oq.h, oq.conn, kap, f_p, u0, r_chk, v_chk))
+    np.negative(r_chk, out=r_chk)
+    orc._check(lib.orc_prepare_forward_solve(ob.h, rp, v_chk, r_chk, g))
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / np.abs(b).max())
+
+    # each product against the oracle's product of the same matrix and vector;
+    # also scaled by (|A||x|)_i, the bound of a dot product's rounding
+    x_g, spmv_err, spmv_abs = rhs.clone(), 0.0, 0.0
+    y_ref, y_abs, a_abs = np.zeros(n), np.zeros(n), np.abs(vals_g)
+    for _ in range(NSPMV):
+        y_g = torch.empty_like(x_g)
+        A.matvec(jac, x_g, y_g, alpha=SPMV_SCALE)
+        x_h = x_g.cpu().numpy()
+        lib.orc_matvec(n, rp, ci, vals_g, x_h, y_ref, SPMV_SCALE, 0.0)
+        lib.orc_matvec(n, rp, ci, a_abs, np.abs(x_h), y_abs, SPMV_SCALE, 0.0)
+        d_y = np.abs(y_g.cpu().numpy() - y_ref)
+        spmv_err = max(spmv_err, float(d_y.max() / np.abs(y_ref).max()))
+        spmv_abs = max(spmv_abs, float(d_y.max() / y_abs.max()))
+        x_g = y_g
+    torch.cuda.synchronize()
+
+    return {
+        "cpu_baseline": {"elements_per_s": e * n_s / tot, "ms_per_step": tot / n_s * 1e3,
+                         "cores": 1, "kind": "port",
+                         "sample": f"{n_s} full steps (assembly, prepareForwardSolve, "
+                                   f"{NSPMV} SpMV) of the same 1024x1024 system, serial "
+                                   f"oracle in place"},
+        "rel_err_vs_oracle_full_size": {"csr_vals_after_bc": rel(vals_g, v_chk),
+                                        "rhs_after_lifting": rel(rhs_g, r_chk),
+                                        "spmv_each_product_max": spmv_err,
+                                        "spmv_each_product_max_vs_abs_products": spmv_abs},
+    }
 
 
 def cpu_baseline():
