@@ -590,6 +590,34 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   T              je[6], jo[6], jp[3] = {0, 0, 0};
   T   r = 0;
   int c = 0;
+  // FP32: the scalar block da[sa][b] (diffusion + convection) is the same for
+  // the two component rows 2sa and 2sa + 1, so each lane of the pair forms it
+  // for the columns b = c, c + 2, c + 4 and takes the other three from its
+  // partner. Every lane runs this (the shuffles need the whole warp); lanes of
+  // pressure rows or rejected elements form values that are never used.
+  T dsh[3] = {0, 0, 0}, dpt[3] = {0, 0, 0};
+  if constexpr (kCompOrder)
+  {
+    const int sa = (l < 12 ? l : 0) >> 1, cb = l & 1;
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+    {
+      const int b  = 2 * j + cb;
+      T         da = S.G3[0] * ref.S00[sa][b] + S.G3[1] * ref.S11[sa][b]
+             + S.G3[2] * ref.S01[sa][b];
+#pragma unroll
+      for (int q = 0; q < kNq; ++q)
+      {
+        da += ref.wN[q][sa] * S.vq[q][b];
+      }
+      dsh[j] = da;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+    {
+      dpt[j] = __shfl_xor_sync(kAll, dsh[j], 1);
+    }
+  }
   if (row_lane && l < 12)
   {
     const int sa = l >> 1;
@@ -604,11 +632,19 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
 #pragma unroll
     for (int b = 0; b < 6; ++b)
     {
-      T da = S.G3[0] * ref.S00[sa][b] + S.G3[1] * ref.S11[sa][b] + S.G3[2] * ref.S01[sa][b];
-#pragma unroll
-      for (int q = 0; q < kNq; ++q)
+      T da;
+      if constexpr (kCompOrder)
       {
-        da += ref.wN[q][sa] * S.vq[q][b];
+        da = (b & 1) == c ? dsh[b >> 1] : dpt[b >> 1];
+      }
+      else
+      {
+        da = S.G3[0] * ref.S00[sa][b] + S.G3[1] * ref.S11[sa][b] + S.G3[2] * ref.S01[sa][b];
+#pragma unroll
+        for (int q = 0; q < kNq; ++q)
+        {
+          da += ref.wN[q][sa] * S.vq[q][b];
+        }
       }
       const T m0 = ref.T[0][sa][b] * G0[0] + ref.T[1][sa][b] * G0[1] + ref.T[2][sa][b] * G0[2];
       const T m1 = ref.T[0][sa][b] * G1[0] + ref.T[1][sa][b] * G1[1] + ref.T[2][sa][b] * G1[2];
