@@ -269,6 +269,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only", default="",
                     help="run one workload: th, th64, vjp, poisson, navier, batch")
+    ap.add_argument("--batch-instances", type=int, default=256,
+                    help="instances in the batched workload (smaller only to profile it)")
     ap.add_argument("--soak", type=float, default=1.0,
                     help="seconds of untimed headline steps before timing (clock sampling)")
     args = ap.parse_args()
@@ -721,7 +723,7 @@ def main():
         rng = np.random.default_rng(5)
         insts, cpu_sample = [], []
         n_p1 = n_th = 0
-        for k in range(256):
+        for k in range(args.batch_instances):
             if rng.random() < 0.5:
                 nx = int(rng.integers(32, 513))
                 coords, conn = meshes.jittered_tri(nx, seed=1000 + k)
@@ -777,7 +779,8 @@ def main():
         t_b32, t_b64, t_bmx = runs["fp32_quad"], runs["fp64"], runs["mixed"]
         launches += 6 * args.steps
         line["batch"] = {
-            "workload": "256 uneven instances (P1 Poisson jittered/permuted nx in 32..512, "
+            "workload": f"{args.batch_instances} uneven instances (P1 Poisson "
+                        "jittered/permuted nx in 32..512, "
                         "Taylor-Hood cavity nx in 32..128, Re in 100..1000), residual + "
                         "Jacobian + VJP, one persistent launch replayed from a CUDA graph",
             "instances": {"p1": n_p1, "taylor_hood": n_th}, "elements": batch.num_elems,
