@@ -339,8 +339,9 @@ GBFEM_API int gbfem_vjp_navier_hist(const gbfem_assembly_map* map, int num_nodes
  * P1: g_state = K^T lam, g_control[e] = lam_e^T K_e u_e (gbfem_vjp_p1_kappa);
  * Taylor-Hood: g_state = J^T lam of the assembled Jacobian. femx has no
  * batched entry; this replaces a loop of per-instance calls.
- * gbfem_batch_run enqueues two kernels (zero outputs, persistent assembly),
- * allocates nothing and does not synchronize.
+ * gbfem_batch_run enqueues two kernels (zero outputs, persistent assembly;
+ * MIXED adds a flat launch for the Taylor-Hood residuals), allocates nothing
+ * and does not synchronize.
  * ------------------------------------------------------------------------ */
 #define GBFEM_BATCH_P1_KAPPA 1
 #define GBFEM_BATCH_TH_NS 2
