@@ -21,6 +21,14 @@ Sub-results in the same line:
                  the 256x256 P1 triangulation: residual + next-state
                  Jacobian, and the history VJP, elements/s, with the oracle
                  (femx's operator restated) on every host core beside it
+  batch          256 uneven instances (P1 and Taylor-Hood) in one
+                 persistent launch replayed from a CUDA graph, FP32 / MIXED /
+                 FP64, autotuned, errors against the FP64 batch
+The headline, navier, poisson, vjp and batch entries each carry a CPU
+baseline of the oracle timed on this host (cores stated: every core for the
+Taylor-Hood and GLS NS loops, as femx's OpenMP NS assembly runs; one core
+for the Poisson step, the VJP and the batch, as femx's generic assembly
+runs); poisson also reports its full-size errors against the oracle.
 Inputs are seeded synthetic fields with the configured shapes (no dataset).
 Timing: CUDA events on the launch stream, 512 MB L2 flush before each step
 (outside the events), warm-up steps untimed. e2e: same step through the
