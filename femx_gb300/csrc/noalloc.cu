@@ -37,12 +37,20 @@ constexpr long long kNoAllocScratchWords = kStatusWords + GBFEM_NOALLOC_MAX_ROWS
 static __device__ __align__(256) int g_noalloc_scratch[kNoAllocScratchWords];
 
 // Host code cannot use the array's name as a device address; the address is
-// looked up once per device, with that device current.
+// looked up once per device, with that device current. A device reset
+// (cudaDeviceReset) unloads the module and makes the cached address stale,
+// so the entry point must not be used after one in the same process.
+//
+// g_dirty[dev] is set while a call has constraint slots marked in the array
+// and cleared once the call has enqueued their clearing. If a call throws in
+// between (a failed launch, copy or synchronisation), the next call on that
+// device clears the whole array before it uses it.
 constexpr int kMaxDevices = 64;
 std::mutex    g_addr_mutex;
-int*          g_addr[kMaxDevices] = {};
+int*          g_addr[kMaxDevices]  = {};
+bool          g_dirty[kMaxDevices] = {};
 
-int* scratchAddress()
+int* scratchAddress(int* dev_out)
 {
   int dev = 0;
   gbfem::cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
@@ -55,7 +63,22 @@ int* scratchAddress()
                      "cudaGetSymbolAddress(no-allocation scratch)");
     g_addr[dev] = static_cast<int*>(p);
   }
+  *dev_out = dev;
   return g_addr[dev];
+}
+
+bool takeDirty(int dev)
+{
+  std::lock_guard<std::mutex> lock(g_addr_mutex);
+  const bool d = g_dirty[dev];
+  g_dirty[dev] = false;
+  return d;
+}
+
+void setDirty(int dev, bool d)
+{
+  std::lock_guard<std::mutex> lock(g_addr_mutex);
+  g_dirty[dev] = d;
 }
 
 __global__ void naValidatePattern(int rows, int cols, const int* __restrict__ row_ptr,
@@ -139,6 +162,10 @@ __global__ void naCheckDiag(int nb, int rows, const int* __restrict__ dofs,
 // constrained columns in constraint order with separate multiply and
 // subtract roundings (the CPU loop's order, BoundaryMap.cpp:224-238) and
 // zero those entries; constrained rows become identity rows with rhs = g.
+// The entries are taken in (constraint slot, CSR position) order, so a row
+// that holds the same constrained column twice (femx's CsrPattern does not
+// forbid repeated columns) subtracts and zeroes both, as femx's column list
+// does (BoundaryMap.cpp:113-124 lists every matching entry in row order).
 __global__ void naApply(int rows, const int* __restrict__ row_ptr,
                         const int* __restrict__ col_ind, const int* __restrict__ slot,
                         double* __restrict__ vals, double* __restrict__ rhs,
@@ -160,16 +187,20 @@ __global__ void naApply(int rows, const int* __restrict__ row_ptr,
     rhs[r] = g[own - 1];
     return;
   }
-  double acc  = 0.0;
-  bool   any  = false;
-  int    last = 0; // slots are 1-based; apply in increasing slot order
+  double acc   = 0.0;
+  bool   any   = false;
+  int    last  = 0;  // slots are 1-based; 0 = before the first constraint
+  int    lastk = -1; // CSR position of the entry applied last
   for (;;)
   {
+    // Next entry after (last, lastk) in (slot, k) order. k ascends in the
+    // scan, so the first entry met with the smallest qualifying slot is the
+    // one with the smallest k.
     int best = 0x7fffffff, bk = -1;
     for (int k = k0; k < k1; ++k)
     {
       const int sl = slot[col_ind[k]];
-      if (sl > last && sl < best)
+      if (sl != 0 && (sl > last || (sl == last && k > lastk)) && sl < best)
       {
         best = sl;
         bk   = k;
@@ -187,6 +218,7 @@ __global__ void naApply(int rows, const int* __restrict__ row_ptr,
     acc      = __dsub_rn(acc, __dmul_rn(vals[bk], g[best - 1]));
     vals[bk] = 0.0;
     last     = best;
+    lastk    = bk;
   }
   if (any)
   {
@@ -231,13 +263,22 @@ extern "C" int gbfem_prepare_forward_solve_noalloc(int num_bcs, const int* dofs,
     {
       return;
     }
-    cudaStream_t  s      = asStream(stream);
-    int*          base   = scratchAddress();
-    auto*         status = reinterpret_cast<DeviceStatus*>(base);
-    int*          slot   = base + kStatusWords;
-    const unsigned rb    = blocksFor(rows, 256);
-    const unsigned bb    = blocksFor(num_bcs, 256);
+    cudaStream_t   s = asStream(stream);
+    int            dev    = 0;
+    int*           base   = scratchAddress(&dev);
+    auto*          status = reinterpret_cast<DeviceStatus*>(base);
+    int*           slot   = base + kStatusWords;
+    const unsigned rb     = blocksFor(rows, 256);
+    const unsigned bb     = blocksFor(num_bcs, 256);
 
+    if (takeDirty(dev))
+    {
+      // An earlier call failed with slots marked: start from a zero array.
+      setDirty(dev, true);
+      cudaCheck(cudaMemsetAsync(base, 0, sizeof(int) * kNoAllocScratchWords, s),
+                "scratch reset");
+      setDirty(dev, false);
+    }
     cudaCheck(cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s), "status reset");
     naValidatePattern<<<rb, 256, 0, s>>>(rows, rows, row_ptr, col_ind, status);
     cudaCheck(cudaGetLastError(), "pattern check launch");
@@ -247,11 +288,12 @@ extern "C" int gbfem_prepare_forward_solve_noalloc(int num_bcs, const int* dofs,
     cudaCheck(cudaStreamSynchronize(s), "pattern check");
     if (h.code != kDevOk)
     {
-      cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s);
-      cudaStreamSynchronize(s);
+      cudaCheck(cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s), "status reset");
+      cudaCheck(cudaStreamSynchronize(s), "status reset");
       throw Error(GBFEM_EDATA, deviceErrorMessage(h.code));
     }
 
+    setDirty(dev, true);
     naMark<<<bb, 256, 0, s>>>(num_bcs, rows, dofs, slot, status);
     cudaCheck(cudaGetLastError(), "constraint mark launch");
     naCheckDiag<<<bb, 256, 0, s>>>(num_bcs, rows, dofs, row_ptr, col_ind, status);
@@ -268,6 +310,7 @@ extern "C" int gbfem_prepare_forward_solve_noalloc(int num_bcs, const int* dofs,
     naClear<<<bb, 256, 0, s>>>(num_bcs, dofs, rows, slot);
     cudaCheck(cudaGetLastError(), "scratch clear launch");
     cudaCheck(cudaMemsetAsync(status, 0, sizeof(DeviceStatus), s), "status reset");
+    setDirty(dev, false);
     if (h.code != kDevOk)
     {
       cudaCheck(cudaStreamSynchronize(s), "scratch clear");

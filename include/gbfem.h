@@ -153,8 +153,13 @@ GBFEM_API int gbfem_prepare_forward_solve(const gbfem_boundary_map* bc, double* 
  * address (cudaGetSymbolAddress), so make it before any stream capture. It
  * synchronizes `stream` to report invalid input (out-of-range or repeated
  * DOFs, a missing diagonal, a malformed pattern) before touching vals/rhs.
- * All calls share the array and leave it cleared; calls whose GPU work
- * overlaps (unordered streams) race on it. */
+ * The pattern is square (rows x rows), as femx's makeBoundaryMap requires
+ * (BoundaryMap.cpp:62); a row that repeats a constrained column has every
+ * such entry lifted and zeroed, as in femx. All calls share the array and
+ * leave it cleared (a call that fails midway has the next call clear it
+ * whole); calls whose GPU work overlaps (unordered streams) race on it. The
+ * looked-up address does not survive cudaDeviceReset: do not call this entry
+ * point after a device reset in the same process. */
 #define GBFEM_NOALLOC_MAX_ROWS 2097152
 GBFEM_API int gbfem_prepare_forward_solve_noalloc(int num_bcs, const int* dofs,
                                                   int rows, const int* row_ptr,

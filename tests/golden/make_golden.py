@@ -260,7 +260,9 @@ def real_cases(tmp, ref):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("FEMX_REFERENCE"),
+                    required=os.environ.get("FEMX_REFERENCE") is None,
+                    help="femx source tree (default: $FEMX_REFERENCE)")
     ap.add_argument("--only", default="", help="generate one family: ns_gls, gmsh, real")
     args = ap.parse_args()
     build(args.ref)

@@ -72,13 +72,18 @@ def with_handle(dofs, row_ptr, col_ind, vals, rhs, g):
 
 
 def no_alloc(dofs, row_ptr, col_ind, vals, rhs, g):
-    L = lib()
     v, r = vals.clone(), rhs.clone()
-    rc = L.lib().gbfem_prepare_forward_solve_noalloc(
+    rc = call_no_alloc(dofs, row_ptr, col_ind, v, r, g)
+    return rc, v, r
+
+
+def call_no_alloc(dofs, row_ptr, col_ind, v, r, g):
+    """One C-ABI call on buffers the caller already holds (v, r updated)."""
+    rc = lib().lib().gbfem_prepare_forward_solve_noalloc(
         dofs.numel(), ptr(dofs), row_ptr.numel() - 1, ptr(row_ptr), ptr(col_ind), ptr(v),
         ptr(r), ptr(g), stream())
     torch.cuda.synchronize()
-    return rc, v, r
+    return rc
 
 
 def golden_case():
@@ -104,18 +109,78 @@ def assert_same(a, b):
     assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
 
 
-def test_two_calls_in_a_row_match_the_handle_path():
+def test_two_calls_in_a_row_match_the_handle_path_and_the_reference():
     case = golden_case()
     ref = with_handle(*case)
-    free_before = None
+    gold = load_golden("p1_jit9")
+    dofs, row_ptr, col_ind, vals, rhs, g = case
+    # Buffers are made before the calls so that only the C call runs between
+    # the two memory readings around it.
+    v, r = vals.clone(), rhs.clone()
     for call in range(2):
+        v.copy_(vals)
+        r.copy_(rhs)
+        torch.cuda.synchronize()
+        free0, reserved0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
+        rc = call_no_alloc(dofs, row_ptr, col_ind, v, r, g)
+        free1, reserved1 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
+        assert rc == 0, lib().lib().gbfem_last_error().decode()
+        assert free1 == free0 and reserved1 == reserved0  # the call allocated nothing
+        assert_same((v, r), ref)
+        # femx's own prepareForwardSolve output on this case, bit for bit
+        assert np.array_equal(v.cpu().numpy(), gold["vals_fwd"])
+        assert np.array_equal(r.cpu().numpy(), gold["rhs_fwd"])
+
+
+def test_repeated_constrained_column_is_lifted_every_time():
+    """A row may hold the same constrained column twice (femx's CsrPattern
+    checks ranges and order only); femx lifts and zeroes both entries."""
+    gold = load_golden("p1_jit9")
+    row_ptr, col_ind = gold["row_ptr"].copy(), gold["col_ind"].copy()
+    bc = set(int(d) for d in gold["bc_dofs"])
+    rng = np.random.default_rng(11)
+    vals = rng.standard_normal(len(col_ind))
+    picked = []
+    for r in range(len(row_ptr) - 1):
+        if r in bc:
+            continue
+        ks = [k for k in range(row_ptr[r], row_ptr[r + 1]) if int(col_ind[k]) in bc]
+        if ks:
+            picked.append(ks[0])
+        if len(picked) == 4:
+            break
+    assert picked
+    new_cols, new_vals, new_ptr = [], [], [0]
+    for r in range(len(row_ptr) - 1):
+        for k in range(row_ptr[r], row_ptr[r + 1]):
+            new_cols.append(col_ind[k])
+            new_vals.append(vals[k])
+            if k in picked:  # the same column again, right after
+                new_cols.append(col_ind[k])
+                new_vals.append(0.5 + rng.random())
+        new_ptr.append(len(new_cols))
+    new_ptr = np.asarray(new_ptr, np.int32)
+    new_cols = np.asarray(new_cols, np.int32)
+    new_vals = np.asarray(new_vals)
+    rhs = rng.standard_normal(len(new_ptr) - 1)
+    g = rng.standard_normal(len(gold["bc_dofs"]))
+
+    from oracle import pyoracle as orc
+    ev, er = orc.BoundaryMap(gold["bc_dofs"], new_ptr, new_cols).prepare_forward_solve(
+        new_vals, rhs, g)
+    case = (dev(gold["bc_dofs"]), dev(new_ptr), dev(new_cols), dev(new_vals), dev(rhs), dev(g))
+    ref = with_handle(*case)
+    for _ in range(2):
         rc, v, r = no_alloc(*case)
         assert rc == 0, lib().lib().gbfem_last_error().decode()
         assert_same((v, r), ref)
-        free_now = torch.cuda.mem_get_info()[0]
-        if free_before is not None:
-            assert free_now == free_before  # the call allocated nothing
-        free_before = free_now
+        assert np.array_equal(v.cpu().numpy(), ev) and np.array_equal(r.cpu().numpy(), er)
+    # every entry of an unconstrained row in a constrained column is zero,
+    # the repeated ones included
+    row_of = np.repeat(np.arange(len(new_ptr) - 1), np.diff(new_ptr))
+    bcl = sorted(bc)
+    lifted = np.isin(new_cols, bcl) & ~np.isin(row_of, bcl)
+    assert np.all(v.cpu().numpy()[lifted] == 0.0)
 
 
 def test_alternating_problems_leave_no_state_behind():
