@@ -96,11 +96,27 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
       return;
     }
   }
-  ElemK<T> K;
-  if (!elementK<T>(a.coords[n0], a.coords[n1], a.coords[n2], a.kappa[e], K))
+  // FP32: the element is formed for kappa = 1 (geometry only; exact on a
+  // uniform mesh, whose edge vectors, determinant and h_i . h_j are exact in
+  // FP32), kappa is applied afterwards: in FP32 for the residual and the
+  // Jacobian, in FP64 for the gradients.
+  const double kap = a.kappa[e];
+  ElemK<T>     K;
+  if (!elementK<T>(a.coords[n0], a.coords[n1], a.coords[n2], kF32 ? 1.0 : kap, K))
   {
     gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
     return;
+  }
+  ElemK<T> Kh = K;
+  if constexpr (kF32)
+  {
+    const T kf = gbfem::fromF64<T>(kap);
+    K.k00 *= kf;
+    K.k01 *= kf;
+    K.k02 *= kf;
+    K.k11 *= kf;
+    K.k12 *= kf;
+    K.k22 *= kf;
   }
   // Element residual in T (FP64 on the plain path); accumulation in FP64.
   const T u0 = gbfem::fromF64<T>(a.u[d0]), u1 = gbfem::fromF64<T>(a.u[d1]);
@@ -160,27 +176,50 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
   if (kVjp)
   {
     gbfem::awaitPrerequisites(); // g_u's zero fill may still be running
-    const T l0 = gbfem::fromF64<T>(a.lam[d0]), l1 = gbfem::fromF64<T>(a.lam[d1]);
-    const T l2 = gbfem::fromF64<T>(a.lam[d2]);
-    // K is symmetric: K^T lam = K lam.
-    const T v0 = K.k00 * l0 + K.k01 * l1 + K.k02 * l2;
-    const T v1 = K.k01 * l0 + K.k11 * l1 + K.k12 * l2;
-    const T v2 = K.k02 * l0 + K.k12 * l1 + K.k22 * l2;
-    if (a.g_u != nullptr)
+    if constexpr (kF32)
     {
-      gbfem::redAdd(a.g_u + d0, gbfem::toF64(v0));
-      gbfem::redAdd(a.g_u + d1, gbfem::toF64(v1));
-      gbfem::redAdd(a.g_u + d2, gbfem::toF64(v2));
+      // The gradient reduction in FP64 (the FP32 element's geometry widened
+      // exactly, kappa, adjoint and state in FP64): FP32 rounding here would
+      // put ~1e-7 relative noise on every element's gradient, which
+      // directional derivatives over many elements amplify by cancellation.
+      const double h00 = gbfem::f32ToF64(Kh.k00), h01 = gbfem::f32ToF64(Kh.k01);
+      const double h02 = gbfem::f32ToF64(Kh.k02), h11 = gbfem::f32ToF64(Kh.k11);
+      const double h12 = gbfem::f32ToF64(Kh.k12), h22 = gbfem::f32ToF64(Kh.k22);
+      const double l0 = a.lam[d0], l1 = a.lam[d1], l2 = a.lam[d2];
+      const double v0 = h00 * l0 + h01 * l1 + h02 * l2;
+      const double v1 = h01 * l0 + h11 * l1 + h12 * l2;
+      const double v2 = h02 * l0 + h12 * l1 + h22 * l2;
+      if (a.g_u != nullptr)
+      {
+        gbfem::redAdd(a.g_u + d0, kap * v0);
+        gbfem::redAdd(a.g_u + d1, kap * v1);
+        gbfem::redAdd(a.g_u + d2, kap * v2);
+      }
+      if (a.g_m != nullptr)
+      {
+        a.g_m[e] = kap * (v0 * a.u[d0] + v1 * a.u[d1] + v2 * a.u[d2]);
+      }
     }
-    if (a.g_m != nullptr)
+    else
     {
-      // lam^T K u = (K lam) . u
-      const T w0 = gbfem::fromF64<T>(a.u[d0]), w1 = gbfem::fromF64<T>(a.u[d1]);
-      const T w2 = gbfem::fromF64<T>(a.u[d2]);
-      a.g_m[e]   = gbfem::toF64(v0 * w0 + v1 * w1 + v2 * w2);
+      const T l0 = a.lam[d0], l1 = a.lam[d1], l2 = a.lam[d2];
+      // K is symmetric: K^T lam = K lam.
+      const T v0 = K.k00 * l0 + K.k01 * l1 + K.k02 * l2;
+      const T v1 = K.k01 * l0 + K.k11 * l1 + K.k12 * l2;
+      const T v2 = K.k02 * l0 + K.k12 * l1 + K.k22 * l2;
+      if (a.g_u != nullptr)
+      {
+        gbfem::redAdd(a.g_u + d0, v0);
+        gbfem::redAdd(a.g_u + d1, v1);
+        gbfem::redAdd(a.g_u + d2, v2);
+      }
+      if (a.g_m != nullptr)
+      {
+        // lam^T K u = (K lam) . u
+        a.g_m[e] = v0 * a.u[d0] + v1 * a.u[d1] + v2 * a.u[d2];
+      }
     }
   }
 }
-
 
 } // namespace

@@ -2,8 +2,11 @@
 
 * torch.autograd.Function backward == explicit VJP kernels;
 * directional derivatives of the residual against central finite
-  differences (h = 1e-6) over 32 seeded directions in the control m and the
-  state u — the accuracy gate is 1e-6 relative;
+  differences over 32 seeded directions in the control m and the state u
+  (a scheme whose own error is far below the gate: h = 1 in u, where R is
+  affine, Richardson-extrapolated h = 1e-2 / 5e-3 in m) — the accuracy gate
+  is 1e-6 relative, met at the 512x512 inverse-problem configuration by the
+  FP32-quadrature and FP64 VJPs alike;
 * the reduced gradient of J(m) = 0.5 |u(m) - d|^2 against femx's own
   ReducedFunctional (femx/inverse/ReducedFunctional.hpp:94-117) run on the
   reference library with DenseLinearSolver (tests/golden/inverse_12.npz).
@@ -89,10 +92,26 @@ def test_autograd_backward_equals_vjp_kernels():
     assert rel_inf(m.grad.cpu().numpy(), gm.cpu().numpy()) <= 1e-14
 
 
-# MIXED keeps the gradient in FP64 (the VJP kernels run FP64 element math);
-# FP32_QUAD carries ~1e-7 per element, which cancellation in a directional
-# derivative over many elements amplifies, hence its looser gate.
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-6), ("mixed", 1e-6), ("fp32_quad", 1e-4)])
+def directional_fd(R, u0, m0, lam, d, which):
+    """Central differences of lam^T R along a unit direction, with a scheme
+    whose own error is far below the 1e-6 gate. R is affine in u, so one
+    central difference with h = 1 is exact up to rounding; in m it is smooth
+    (kappa = exp(m)), so two central differences (h = 1e-2 and 5e-3) are
+    combined by Richardson extrapolation, removing the h^2 term."""
+    if which == "u":
+        return float((R(u0 + d, m0) - R(u0 - d, m0)) @ lam) / 2.0
+
+    def central(h):
+        return float((R(u0, m0 + h * d) - R(u0, m0 - h * d)) @ lam) / (2 * h)
+    return (4.0 * central(5e-3) - central(1e-2)) / 3.0
+
+
+# Jittered mesh: the FP32-quadrature element carries the FP32 rounding of its
+# geometry (~1e-7 per element), which a directional derivative over many
+# elements can amplify, hence its looser gate there. On a uniform mesh the
+# FP32 geometry is exact and the gradient reduction runs in FP64, so the
+# FP32-quadrature gradient meets 1e-6 (test_config4_vjp_512 below).
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-8), ("mixed", 1e-8), ("fp32_quad", 1e-4)])
 def test_vjp_matches_central_differences_32_directions(precision, tol):
     coords, conn, amap, bc, bdofs = setup(64, 4)
     rng = np.random.default_rng(4)
@@ -108,18 +127,64 @@ def test_vjp_matches_central_differences_32_directions(precision, tol):
     (r * dev(lam)).sum().backward()
     gu, gm = u.grad.cpu().numpy(), m.grad.cpu().numpy()
     R = OracleResidual(coords, conn, f, bdofs, g)
-    h = 1e-6
     errs = []
     for _ in range(32):
         dm = rng.standard_normal(e)
         dm /= np.linalg.norm(dm)
-        fd = float((R(u0, m0 + h * dm) - R(u0, m0 - h * dm)) @ lam) / (2 * h)
+        fd = directional_fd(R, u0, m0, lam, dm, "m")
         errs.append(abs(fd - gm @ dm) / abs(fd))
         du = rng.standard_normal(n)
         du /= np.linalg.norm(du)
-        fd = float((R(u0 + h * du, m0) - R(u0 - h * du, m0)) @ lam) / (2 * h)
+        fd = directional_fd(R, u0, m0, lam, du, "u")
         errs.append(abs(fd - gu @ du) / abs(fd))
     assert max(errs) <= tol, max(errs)
+
+
+@pytest.mark.parametrize("precision", ["fp32_quad", "fp64"])
+def test_config4_vjp_512(precision):
+    """The inverse-problem configuration: 512x512 uniform mesh, m = log kappa
+    a seeded GRF (correlation length 0.05, variance 1), Dirichlet rows. The
+    state and control VJPs (behind torch.autograd.Function) along 32 seeded
+    unit directions each, against the oracle's exact gradient, and against
+    central differences of the oracle's FP64 residual on 8 of them; gate
+    1e-6 relative, for the FP32-quadrature mode too."""
+    coords, conn, amap, bc, bdofs = setup(512, 4, jitter=False)
+    rng = np.random.default_rng(4)
+    n, e = coords.shape[0], conn.shape[0]
+    f = meshes.fourier_source(coords, 1)
+    m0 = meshes.grf_centroids(coords, conn, seed=4, ell=0.05, var=1.0, grid=512)
+    u0 = rng.standard_normal(n)
+    lam = rng.standard_normal(n)
+    g = np.zeros(len(bdofs))
+    u = dev(u0).requires_grad_()
+    m = dev(m0).requires_grad_()
+    r = p1_kappa_residual(u, m, amap, dev(coords), dev(f), bc, dev(g), precision=precision)
+    (r * dev(lam)).sum().backward()
+    gu, gm = u.grad.cpu().numpy(), m.grad.cpu().numpy()
+    # the oracle's exact gradient (zeroBoundary on lam, lam on the constrained rows)
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    om = orc.AssemblyMap(n, n, offs, dofs, offs, dofs)
+    oq = orc.P1Quad(coords, conn)
+    lt = lam.copy()
+    lt[bdofs] = 0.0
+    ogu, ogm = orc.vjp_p1_kappa(om, oq, np.exp(m0), u0, lt)
+    ogu[bdofs] += lam[bdofs]
+    R = OracleResidual(coords, conn, f, bdofs, g)
+    exact, fd_errs = [], []
+    for i in range(32):
+        dm = rng.standard_normal(e)
+        dm /= np.linalg.norm(dm)
+        du = rng.standard_normal(n)
+        du /= np.linalg.norm(du)
+        exact.append(abs((gm - ogm) @ dm) / abs(ogm @ dm))
+        exact.append(abs((gu - ogu) @ du) / abs(ogu @ du))
+        if i < 8:
+            fd = directional_fd(R, u0, m0, lam, dm, "m")
+            fd_errs.append(abs(fd - gm @ dm) / abs(fd))
+            fd = directional_fd(R, u0, m0, lam, du, "u")
+            fd_errs.append(abs(fd - gu @ du) / abs(fd))
+    assert max(exact) <= 1e-6, max(exact)
+    assert max(fd_errs) <= 1e-6, max(fd_errs)
 
 
 def test_gradcheck_small():

@@ -5,8 +5,9 @@ deterministic mode: exact integrals for linear fields on jittered meshes
 Couette, shear, stagnation flow, a pressure gradient) and the Jacobian's
 identities (tests/th_checks.py). These pins share no code with the oracle.
 
-Tolerances: FP64 1e-12; FP32 quadrature 1e-6 (J and R); MIXED J 1e-6 and
-R 1e-12 (its residual is computed to FP64 accuracy).
+Tolerances: FP64 1e-12; FP32 quadrature 1e-6 (J and R; R relative to the
+size of its terms, which cancel for these fields); MIXED J 1e-6 and R 1e-12
+(its residual is computed to FP64 accuracy).
 """
 import numpy as np
 import pytest
@@ -62,7 +63,8 @@ def gpu_assembler(precision, deterministic):
 
 @pytest.mark.parametrize("precision,det,tol_r,tol_j", MODES, ids=IDS)
 def test_linear_fields_match_exact_integrals(precision, det, tol_r, tol_j):
-    T.check_linear_fields(gpu_assembler(precision, det), tol_r, tol_j)
+    T.check_linear_fields(gpu_assembler(precision, det), tol_r, tol_j,
+                          r_scale="terms" if precision == "fp32_quad" else "ref")
 
 
 @pytest.mark.parametrize("precision,det,tol_r,tol_j", MODES, ids=IDS)

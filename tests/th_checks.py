@@ -27,9 +27,16 @@ def mesh(nx, jitter_seed=None):
     return cp2, conn6, nv, nd
 
 
-def check_linear_fields(assemble, tol_r, tol_j, seeds=(1, 2), nus=(1e-3, 1.0)):
+def check_linear_fields(assemble, tol_r, tol_j, seeds=(1, 2), nus=(1e-3, 1.0),
+                        r_scale="ref"):
     """Every row of R and J against the exact integrals, for random linear
-    velocity and pressure fields on jittered, permuted meshes."""
+    velocity and pressure fields on jittered, permuted meshes.
+
+    R's error is taken relative to ||R_exact||_inf (r_scale="ref"), or, for
+    FP32 element arithmetic, relative to the size of R's terms,
+    max_i sum_j |J_ij U_j| (r_scale="terms"): a linear velocity makes the
+    diffusion terms cancel in the interior rows (lap u = 0), so R is much
+    smaller than the terms whose FP32 rounding it carries."""
     worst = 0.0
     for seed in seeds:
         cp2, conn6, nv, nd = mesh(5, jitter_seed=seed)
@@ -38,7 +45,8 @@ def check_linear_fields(assemble, tol_r, tol_j, seeds=(1, 2), nus=(1e-3, 1.0)):
             state = X.linear_state(cp2, nv, rng.standard_normal((2, 3)), rng.standard_normal(3))
             r_ex, j_ex = X.exact_linear_system(cp2, conn6, cp2.shape[0], nd, nu, state)
             res, jac = assemble(cp2, conn6, nd, nu, state)
-            er, ej = _rel(res, r_ex), _rel(jac, j_ex)
+            scale = None if r_scale == "ref" else float(np.max(np.abs(j_ex) @ np.abs(state)))
+            er, ej = _rel(res, r_ex, scale), _rel(jac, j_ex)
             assert er <= tol_r, (seed, nu, er)
             assert ej <= tol_j, (seed, nu, ej)
             worst = max(worst, er, ej)
