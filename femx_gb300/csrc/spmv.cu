@@ -84,6 +84,15 @@ __global__ void axpbyKernel(int n, double a, const double* __restrict__ x,
   }
 }
 
+__global__ void expKernel(int n, const double* __restrict__ x, double* __restrict__ y)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    y[i] = exp(x[i]);
+  }
+}
+
 void checkArgs(int rows, int cols, const int* row_ptr, const double* x,
                double* y)
 {
@@ -159,5 +168,20 @@ extern "C" int gbfem_axpby(int n, double a, const double* x, double b,
     require(x != nullptr && y != nullptr, "axpby inputs are null");
     axpbyKernel<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, a, x, b, y);
     cudaCheck(cudaGetLastError(), "axpby launch");
+  });
+}
+
+extern "C" int gbfem_exp(int n, const double* x, double* y, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(n >= 0, "exp size must be non-negative");
+    if (n == 0)
+    {
+      return;
+    }
+    require(x != nullptr && y != nullptr, "exp inputs are null");
+    expKernel<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, x, y);
+    cudaCheck(cudaGetLastError(), "exp launch");
   });
 }

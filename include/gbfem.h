@@ -240,6 +240,11 @@ GBFEM_API void gbfem_csr_transpose_destroy(gbfem_csr_transpose* t);
  * (femx/state/StateSolver.hpp:90-108). y is not read when b == 0. */
 GBFEM_API int gbfem_axpby(int n, double a, const double* x, double b, double* y,
                 void* stream);
+/* y = exp(x) elementwise: the control map kappa = exp(m) of the per-element
+ * control of the kappa-Poisson residual (femx's Residual::res and
+ * applyParamJacT take the parameter vector m itself, Residual.hpp:42-59).
+ * x and y may alias. */
+GBFEM_API int gbfem_exp(int n, const double* x, double* y, void* stream);
 
 /* ---------------------------------------------------------------------------
  * kappa-weighted P1 Poisson assembly — replaces assembly::assemble(op, geom,
