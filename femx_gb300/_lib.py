@@ -118,6 +118,7 @@ SIGNATURES = {
     "gbfem_csr_transpose_apply": (_i, [_vp, _vp, _vp, _vp]),
     "gbfem_csr_transpose_destroy": (None, [_vp]),
     "gbfem_axpby": (_i, [_i, _d, _vp, _d, _vp, _vp]),
+    "gbfem_exp": (_i, [_i, _vp, _vp, _vp]),
     "gbfem_assemble_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_vjp_p1_kappa": (_i, [_vp, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _vp]),
     "gbfem_assemble_th_ns": (_i, [_vp, _i, _vp, _vp, _d, _vp, _vp, _vp, _i, _vp]),

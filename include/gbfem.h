@@ -150,7 +150,11 @@ GBFEM_API int gbfem_prepare_forward_solve(const gbfem_boundary_map* bc, double* 
  * every GPU that loads the library until the process exits, so `rows` may be
  * at most GBFEM_NOALLOC_MAX_ROWS; larger calls are rejected with
  * GBFEM_EINVAL. The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress), so make it before any stream capture. It
+ * address (cudaGetSymbolAddress), which also makes CUDA load the part of
+ * the library that holds the array if it is not loaded yet (with CUDA's lazy
+ * module loading, the array's device memory is committed at that moment),
+ * so make the first call before any stream capture and before any section
+ * that must not see device memory change. It
  * synchronizes `stream` to report invalid input (out-of-range or repeated
  * DOFs, a missing diagonal, a malformed pattern) before touching vals/rhs.
  * The pattern is square (rows x rows), as femx's makeBoundaryMap requires

@@ -115,9 +115,13 @@ def test_two_calls_in_a_row_match_the_handle_path_and_the_reference():
     gold = load_golden("p1_jit9")
     dofs, row_ptr, col_ind, vals, rhs, g = case
     # Buffers are made before the calls so that only the C call runs between
-    # the two memory readings around it.
+    # the two memory readings around it. The first call on the device is the
+    # set-up call: it looks up the scratch array's address, which may make
+    # CUDA load the library's module that holds the array (with lazy module
+    # loading the array's device memory is committed then). The calls after
+    # it must leave the device's free memory unchanged.
     v, r = vals.clone(), rhs.clone()
-    for call in range(2):
+    for call in range(3):
         v.copy_(vals)
         r.copy_(rhs)
         torch.cuda.synchronize()
@@ -125,7 +129,9 @@ def test_two_calls_in_a_row_match_the_handle_path_and_the_reference():
         rc = call_no_alloc(dofs, row_ptr, col_ind, v, r, g)
         free1, reserved1 = torch.cuda.mem_get_info()[0], torch.cuda.memory_reserved()
         assert rc == 0, lib().lib().gbfem_last_error().decode()
-        assert free1 == free0 and reserved1 == reserved0  # the call allocated nothing
+        assert reserved1 == reserved0
+        if call > 0:
+            assert free1 == free0  # the call allocated nothing
         assert_same((v, r), ref)
         # femx's own prepareForwardSolve output on this case, bit for bit
         assert np.array_equal(v.cpu().numpy(), gold["vals_fwd"])
