@@ -19,7 +19,8 @@ import torch
 
 from . import assembly as A
 
-__all__ = ["P1KappaResidual", "p1_kappa_residual"]
+__all__ = ["P1KappaResidual", "p1_kappa_residual", "TaylorHoodResidual",
+           "taylor_hood_residual"]
 
 
 class P1KappaResidual(torch.autograd.Function):
@@ -57,3 +58,64 @@ def p1_kappa_residual(u, m, amap, coords, f=None, bc=None, bc_vals=None,
                       precision: str = "fp64"):
     """R(u, m) as a differentiable function of the state u and the control m."""
     return P1KappaResidual.apply(u, m, amap, coords, f, bc, bc_vals, precision)
+
+
+class TaylorHoodResidual(torch.autograd.Function):
+    """The Taylor-Hood P2/P1 steady Navier-Stokes residual R(state, nu), with
+    constrained rows replaced by state - g when a BoundaryMap is given.
+
+    backward() gives the state VJP J(state)^T lam element by element through
+    gbfem_vjp_th_ns without forming J (the transpose action of
+    TimeResidual::applyJacT / the adjoint solves, femx/state/TimeResidual.hpp:
+    223-227, ConstrainedTimeResidual.cpp:379-405, which zeroes the constrained
+    adjoint entries first), plus lam on the constrained rows; and the
+    viscosity derivative: R is affine in nu, so (dR/dnu)^T lam =
+    lam~ . (R(nu = 1) - R(nu = 0)), two residual assemblies.
+    """
+
+    @staticmethod
+    def forward(ctx, state, nu, amap, coords, conn6, bc, bc_vals, precision):
+        res = torch.empty(amap.numRes(), dtype=torch.float64, device=state.device)
+        A.assembleTaylorHood(amap, coords, conn6, float(nu), state, res, None,
+                             precision=precision)
+        if bc is not None:
+            A.replaceRes(bc, state, bc_vals, res)
+        ctx.save_for_backward(state)
+        ctx.nu, ctx.amap, ctx.coords, ctx.conn6, ctx.bc = float(nu), amap, coords, conn6, bc
+        ctx.precision = precision
+        return res
+
+    @staticmethod
+    def backward(ctx, lam):
+        (state,) = ctx.saved_tensors
+        lam = lam.contiguous()
+        lam_t = lam
+        if ctx.bc is not None:
+            lam_t = lam.clone()
+            A.zeroBoundary(ctx.bc, lam_t)
+        g_state = g_nu = None
+        if ctx.needs_input_grad[0]:
+            g_state = torch.empty_like(state)
+            A.vjpTaylorHood(ctx.amap, ctx.coords, ctx.conn6, ctx.nu, state, lam_t, g_state,
+                            precision=ctx.precision)
+            if ctx.bc is not None:
+                rows = ctx.bc.view()["bc_rows"].long()
+                g_state.index_add_(0, rows, lam.index_select(0, rows))
+        if ctx.needs_input_grad[1]:
+            r1 = torch.empty(ctx.amap.numRes(), dtype=torch.float64, device=state.device)
+            r0 = torch.empty_like(r1)
+            A.assembleTaylorHood(ctx.amap, ctx.coords, ctx.conn6, 1.0, state, r1, None,
+                                 precision=ctx.precision)
+            A.assembleTaylorHood(ctx.amap, ctx.coords, ctx.conn6, 0.0, state, r0, None,
+                                 precision=ctx.precision)
+            g_nu = torch.dot(lam_t, r1 - r0).reshape(())
+        return g_state, g_nu, None, None, None, None, None, None
+
+
+def taylor_hood_residual(state, nu, amap, coords, conn6, bc=None, bc_vals=None,
+                         precision: str = "fp64"):
+    """R(state, nu) as a differentiable function of the state and of nu (a
+    float, or a 0-dim float64 tensor to differentiate with respect to it)."""
+    if not torch.is_tensor(nu):
+        nu = torch.tensor(float(nu), dtype=torch.float64, device=state.device)
+    return TaylorHoodResidual.apply(state, nu, amap, coords, conn6, bc, bc_vals, precision)

@@ -233,3 +233,55 @@ def test_reduced_gradient_matches_femx_reduced_functional():
     (r * dev(lam)).sum().backward()
     grad = -m_t.grad.cpu().numpy()
     assert rel_inf(grad, gd["grad"]) <= 1e-9
+
+
+# ------------------------------------------------ Taylor-Hood autograd
+
+def th_setup(nx, seed):
+    c3, k3 = meshes.jittered_tri(nx, seed=seed)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    amap = A.makeAssemblyMap(nd, nd, dev(offs), dev(dofs), dev(offs), dev(dofs))
+    bd, bv = meshes.cavity_dirichlet(cp2, cp2.shape[0])
+    bc = A.makeBoundaryMap(dev(bd), amap.pattern())
+    return cp2, conn6, nv, nd, offs, dofs, amap, bd, bv, bc
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_quad", 1e-6)])
+def test_taylor_hood_autograd_backward_is_the_transpose_action(precision, tol):
+    """backward() of the constrained Taylor-Hood residual against the
+    oracle's Jacobian transposed: g = J~^T lam with the constrained rows of
+    J~ replaced by identity rows (what replaceRes makes of R); and the
+    viscosity derivative against the oracle's residuals at nu = 1 and 0."""
+    from femx_gb300.autograd import taylor_hood_residual
+    cp2, conn6, nv, nd, offs, dofs, amap, bd, bv, bc = th_setup(6, 12)
+    state = meshes.cavity_state(cp2, nv, seed=12)
+    lam = np.random.default_rng(12).standard_normal(nd)
+    s = dev(state).requires_grad_()
+    nu = torch.tensor(2e-2, dtype=torch.float64, device="cuda", requires_grad=True)
+    r = taylor_hood_residual(s, nu, amap, dev(cp2), dev(conn6, torch.int32), bc, dev(bv),
+                             precision=precision)
+    (r * dev(lam)).sum().backward()
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    _, vals = orc.assemble_th_ns(om, cp2, conn6, 2e-2, state)
+    vals = orc.BoundaryMap(bd, om.row_ptr, om.col_ind).replace_rows(vals, 1.0)
+    g_ref = orc.matvec_t(om.row_ptr, om.col_ind, vals, lam, nd)
+    assert rel_inf(s.grad.cpu().numpy(), g_ref) <= tol
+    r1, _ = orc.assemble_th_ns(om, cp2, conn6, 1.0, state)
+    r0, _ = orc.assemble_th_ns(om, cp2, conn6, 0.0, state)
+    lt = lam.copy()
+    lt[bd] = 0.0
+    gnu = float(lt @ (r1 - r0))
+    assert abs(float(nu.grad) - gnu) <= tol * abs(gnu)
+
+
+def test_taylor_hood_gradcheck_small():
+    from femx_gb300.autograd import taylor_hood_residual
+    cp2, conn6, nv, nd, offs, dofs, amap, bd, bv, bc = th_setup(2, 3)
+    s = dev(meshes.cavity_state(cp2, nv, seed=3)).requires_grad_()
+    nu = torch.tensor(0.1, dtype=torch.float64, device="cuda", requires_grad=True)
+    coords_d, c6 = dev(cp2), dev(conn6, torch.int32)
+    g = dev(bv)
+    assert torch.autograd.gradcheck(
+        lambda ss, nn: taylor_hood_residual(ss, nn, amap, coords_d, c6, bc, g), (s, nu),
+        eps=1e-6, atol=1e-8, rtol=1e-6, nondet_tol=1e-12)
