@@ -848,6 +848,43 @@ def main():
             batch.check()
         t_b32, t_b64, t_bmx = runs["fp32_quad"], runs["fp64"], runs["mixed"]
         launches += 6 * args.steps
+        # Baseline of the same kind: one CUDA graph of per-instance calls of
+        # the standalone kernels (assemble + VJP per instance, each with its
+        # own zero fill), replayed like the persistent launch's graph.
+        per_inst, per_inst_err = {}, {}
+        jacs = [A.CsrMatrix(x.amap.pattern(), x.vals) for x in insts]
+
+        def per_instance(prec):
+            for x, jm in zip(insts, jacs):
+                if isinstance(x, P1Instance):
+                    A.assembleP1Kappa(x.amap, x.coords, x.kappa, x.f, x.u, x.res, jm,
+                                      precision=prec)
+                    A.vjpP1Kappa(x.amap, x.coords, x.kappa, x.u, x.lam, x.g_u, x.g_m,
+                                 precision=prec)
+                else:
+                    A.assembleTaylorHood(x.amap, x.coords, x.conn6, x.nu, x.state, x.res, jm,
+                                         precision=prec)
+                    A.vjpTaylorHood(x.amap, x.coords, x.conn6, x.nu, x.state, x.lam, x.g_u,
+                                    precision=prec)
+        for prec in ("fp64", "mixed", "fp32_quad"):
+            per_instance(prec)
+            torch.cuda.synchronize()
+            g_pi = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g_pi):
+                per_instance(prec)
+            per_inst[prec] = maxrank(timer.run(g_pi.replay, args.steps, args.warmup))
+            if prec == "fp64":
+                # same results as the persistent FP64 launch (atomic order only)
+                e_pi = 0.0
+                for x, (r64, v64, gu64, gm64) in zip(insts, ref):
+                    for a_, b_ in ((x.res, r64), (x.vals, v64), (x.g_u, gu64),
+                                   (getattr(x, "g_m", None), gm64)):
+                        if b_ is not None:
+                            e_pi = max(e_pi, float((a_ - b_).abs().max() / b_.abs().max()))
+                per_inst_err["fp64_vs_persistent_fp64"] = e_pi
+            del g_pi
+        # zero fill + element kernel for the assembly and for the VJP
+        launches += 3 * args.steps * 4 * len(insts)
         line["batch"] = {
             "workload": f"{args.batch_instances} uneven instances (P1 Poisson "
                         "jittered/permuted nx in 32..512, "
@@ -868,6 +905,13 @@ def main():
                                          "(Taylor-Hood: double-float, P1: fp64) and P1 "
                                          "gradients fp64; Taylor-Hood J^T lam from the fp32 J"},
             "autotuned": tuned,
+            "per_instance_graph": {
+                "what": "one CUDA graph of per-instance standalone calls (assemble with its "
+                        "zero fill + VJP per instance) on the same instances and outputs",
+                "ms_per_step": {k: v * 1e3 for k, v in per_inst.items()},
+                "elements_per_s": {k: world * batch.num_elems / v for k, v in per_inst.items()},
+                "persistent_speedup": {k: per_inst[k] / runs[k] for k in per_inst},
+                "max_rel_err": per_inst_err},
         }
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             e_p1 = sum(x.kappa.numel() for x in insts if isinstance(x, P1Instance))
