@@ -22,6 +22,7 @@ GBFEM_ENOMEM = 4
 PREC_FP64 = 0
 PREC_FP32_QUAD = 1
 PREC_MIXED = 2
+PREC_DOUBLE_FLOAT = 3
 DETERMINISTIC = 0x100
 
 

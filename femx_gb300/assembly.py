@@ -36,7 +36,7 @@ __all__ = [
 ]
 
 PRECISIONS = {"fp64": _lib.PREC_FP64, "fp32_quad": _lib.PREC_FP32_QUAD,
-              "mixed": _lib.PREC_MIXED}
+              "mixed": _lib.PREC_MIXED, "double_float": _lib.PREC_DOUBLE_FLOAT}
 
 
 def _stream():

@@ -118,4 +118,110 @@ __device__ __forceinline__ double dfToF64(DF x)
   return f32ToF64(x.hi) + f32ToF64(x.lo);
 }
 
+// A double-float value with arithmetic operators, so that element code
+// written once for float and double (thBlock<T>) runs in double-float: the
+// FP64-accurate Taylor-Hood Jacobian on the FP32 pipe. Multiplication is
+// TwoProduct with the cross terms (Dekker with an FMA), addition the "sloppy"
+// double-double sum of Hida, Li and Bailey (TwoSum of the leading parts, the
+// trailing parts added, renormalised): its error is bounded relative to
+// |a| + |b| rather than |a + b|, which is what element sums need (every
+// result is compared with the size of its terms). About 2^-46 relative per
+// operation.
+struct Dd
+{
+  float hi, lo;
+  Dd() = default;
+  __host__ __device__ constexpr Dd(float h, float l) : hi(h), lo(l) {}
+  __host__ __device__ constexpr Dd(int v) : hi(static_cast<float>(v)), lo(0.0f) {}
+  // compile-time split of a double constant
+  __host__ __device__ constexpr explicit Dd(double d)
+    : hi(static_cast<float>(d)),
+      lo(static_cast<float>(d - static_cast<double>(static_cast<float>(d))))
+  {
+  }
+};
+
+__device__ __forceinline__ Dd ddQuick(float a, float b) // |a| >= |b|
+{
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ Dd operator+(Dd a, Dd b)
+{
+  const float s  = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e  = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ddQuick(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ Dd operator-(Dd a)
+{
+  return {-a.hi, -a.lo};
+}
+
+__device__ __forceinline__ Dd operator-(Dd a, Dd b)
+{
+  return a + (-b);
+}
+
+__device__ __forceinline__ Dd operator*(Dd a, Dd b)
+{
+  const float p = __fmul_rn(a.hi, b.hi);
+  float       e = __fmaf_rn(a.hi, b.hi, -p);
+  e             = __fmaf_rn(a.hi, b.lo, e);
+  e             = __fmaf_rn(a.lo, b.hi, e);
+  return ddQuick(p, e);
+}
+
+// Long division of double-double arithmetic: three quotient digits, each a
+// float division of the running remainder's leading part.
+__device__ __forceinline__ Dd operator/(Dd a, Dd b)
+{
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  Dd          r  = a - Dd(q1, 0.0f) * b;
+  const float q2 = __fdiv_rn(r.hi, b.hi);
+  r              = r - Dd(q2, 0.0f) * b;
+  const float q3 = __fdiv_rn(r.hi, b.hi);
+  const Dd    q  = ddQuick(q1, q2);
+  return q + Dd(q3, 0.0f);
+}
+
+__device__ __forceinline__ Dd& operator+=(Dd& a, Dd b)
+{
+  return a = a + b;
+}
+
+__device__ __forceinline__ Dd& operator-=(Dd& a, Dd b)
+{
+  return a = a - b;
+}
+
+__device__ __forceinline__ bool operator<(Dd a, Dd b)
+{
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+
+__device__ __forceinline__ bool operator>=(Dd a, Dd b)
+{
+  return !(a < b);
+}
+
+template <>
+__device__ __forceinline__ Dd fromF64<Dd>(double d)
+{
+  const float h = f64ToF32(d);
+  return {h, f64ToF32(d - f32ToF64(h))};
+}
+
+__device__ __forceinline__ double toF64(Dd x)
+{
+  return f32ToF64(x.hi) + f32ToF64(x.lo);
+}
+
+__device__ __forceinline__ double toF64Ftz(Dd x)
+{
+  return toF64(x);
+}
+
 } // namespace gbfem

@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
 #pragma unroll
       for (int q = 0; q < kNq; ++q)
       {
-        d += R.wN[q][sa] * (R.dNr[q][b][0] * ut[q][0] + R.dNr[q][b][1] * ut[q][1]);
+        d += kConvW.w[q][sa][b][0] * ut[q][0] + kConvW.w[q][sa][b][1] * ut[q][1];
       }
       da[b] = d;
     }
@@ -299,7 +299,7 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
             "Assembly state, residual, and matrix values must not alias");
     const bool det = (precision & GBFEM_DETERMINISTIC) != 0;
     precision &= ~GBFEM_DETERMINISTIC;
-    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
     require(!det || map->num_elems == 0 || map->gather_off != nullptr,
             "deterministic assembly needs gbfem_assembly_map_enable_gather on the map");
@@ -340,6 +340,7 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
       a.geb                 = map->gather_eb;
       a.gres                = map->gather_res;
       const bool     f64    = precision == GBFEM_PREC_FP64
+                       || precision == GBFEM_PREC_DOUBLE_FLOAT
                        || (precision == GBFEM_PREC_MIXED && !jac);
       const unsigned rblk   = blocksFor(map->num_res, kGatherRows);
       if (f64)
@@ -374,6 +375,17 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
     if (precision == GBFEM_PREC_FP64 && jac)
     {
       launchMaybeDependent(dep, thElemKernel64, eblocks, 128, s, a, map->jac_pos_rows);
+    }
+    else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
+    {
+      if (jac)
+      {
+        launchMaybeDependent(dep, thKernelDd<true>, blocks, kThreads, s, a);
+      }
+      else
+      {
+        thResidualDFKernel<<<eblocks, 128, 0, s>>>(a);
+      }
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
@@ -435,8 +447,7 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
             "VJP inputs must not be null");
     require(g_state != nullptr, "VJP output is null");
     require(g_state != state && g_state != lam, "VJP output must not alias its inputs");
-    require(precision == GBFEM_PREC_FP64 || precision == GBFEM_PREC_FP32_QUAD
-                || precision == GBFEM_PREC_MIXED,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
@@ -462,9 +473,18 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
     a.status    = map->status;
     const unsigned blocks = blocksFor(a.ne, kElemsPerBlock);
     // MIXED keeps the Jacobian (and so J^T lam) in FP32 quadrature
-    precision == GBFEM_PREC_FP64
-        ? launchDependent(thVjpKernel<double, false>, blocks, kThreads, s, a)
-        : launchDependent(thVjpKernel<float, false>, blocks, kThreads, s, a);
+    if (precision == GBFEM_PREC_FP64)
+    {
+      launchDependent(thVjpKernel<double, false>, blocks, kThreads, s, a);
+    }
+    else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
+    {
+      launchDependent(thVjpKernel<gbfem::Dd, false>, blocks, kThreads, s, a);
+    }
+    else
+    {
+      launchDependent(thVjpKernel<float, false>, blocks, kThreads, s, a);
+    }
     cudaCheck(cudaGetLastError(), "Taylor-Hood VJP launch");
   });
 }

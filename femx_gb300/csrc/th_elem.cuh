@@ -146,6 +146,11 @@ constexpr gbfem::DF refCast<gbfem::DF>(double d)
 {
   return gbfem::dfConst(d);
 }
+template <>
+constexpr gbfem::Dd refCast<gbfem::Dd>(double d)
+{
+  return gbfem::Dd(d);
+}
 
 template <class R>
 constexpr ThRef<R> castRef()
@@ -206,6 +211,25 @@ __device__ __forceinline__ const ThRef<double>* refTables(double)
 __device__ __forceinline__ const ThRef<float>* refTables(float)
 {
   return &kRefF;
+}
+__device__ const ThRef<gbfem::Dd> kRefDd = castRef<gbfem::Dd>();
+__device__ __forceinline__ const ThRef<gbfem::Dd>* refTables(gbfem::Dd)
+{
+  return &kRefDd;
+}
+
+// Lane shuffle within an element's 16 lanes, for the element's arithmetic
+// type (a double-float moves as its two floats).
+template <class T>
+__device__ __forceinline__ T laneShfl(T v, int src)
+{
+  return __shfl_sync(0xffffffffu, v, src, kLanes);
+}
+template <>
+__device__ __forceinline__ gbfem::Dd laneShfl<gbfem::Dd>(gbfem::Dd v, int src)
+{
+  return {__shfl_sync(0xffffffffu, v.hi, src, kLanes),
+          __shfl_sync(0xffffffffu, v.lo, src, kLanes)};
 }
 
 struct ThArgs
@@ -431,8 +455,8 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   const double dey = xv.y - __shfl_sync(kAll, xv.y, 0, kLanes);
   const T      ex = gbfem::fromF64<T>(dex), ey = gbfem::fromF64<T>(dey);
   // J[a][b] = d x_a / d r_b of the affine map (vertex nodes)
-  const T j00 = __shfl_sync(kAll, ex, 1, kLanes), j10 = __shfl_sync(kAll, ey, 1, kLanes);
-  const T j01 = __shfl_sync(kAll, ex, 2, kLanes), j11 = __shfl_sync(kAll, ey, 2, kLanes);
+  const T j00 = laneShfl(ex, 1), j10 = laneShfl(ey, 1);
+  const T j01 = laneShfl(ex, 2), j11 = laneShfl(ey, 2);
   double  dj[4] = {0.0, 0.0, 0.0, 0.0}; // FP64 edges, for the FP64 residual only
   if constexpr (kRes64)
   {
@@ -680,52 +704,55 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       r += je[sa] * S.st[2 * sa] + jo[sa] * S.st[2 * sa + 1];
     }
   }
-  if (kGather && row_lane)
+  if constexpr (kGather)
   {
-    // one record per element row: its 15 entries (+ one pad) and its
-    // residual term; the row kernel sums the records of each CSR row
-    const int k = a.gslot[15 * e + l];
-    if (kRes)
+    if (row_lane)
     {
-      a.gres[k] = gbfem::toF64(r);
-    }
-    if constexpr (kRes64)
-    {
-      a.gres[k] = rowRes64(*R64, l);
-    }
-    if (kJac)
-    {
-      T          v[16];
-      const bool swap = !kCompOrder && l < 12 && c == 1;
-#pragma unroll
-      for (int b = 0; b < 6; ++b)
+      // one record per element row: its 15 entries (+ one pad) and its
+      // residual term; the row kernel sums the records of each CSR row
+      const int k = a.gslot[15 * e + l];
+      if (kRes)
       {
-        v[2 * b]     = swap ? jo[b] : je[b];
-        v[2 * b + 1] = swap ? je[b] : jo[b];
+        a.gres[k] = gbfem::toF64(r);
       }
-#pragma unroll
-      for (int b = 0; b < 3; ++b)
+      if constexpr (kRes64)
       {
-        v[12 + b] = jp[b]; // zero on pressure rows
+        a.gres[k] = rowRes64(*R64, l);
       }
-      v[15] = T(0);
-      storeRecord(static_cast<T*>(a.geb) + 16LL * k, v);
+      if (kJac)
+      {
+        T          v[16];
+        const bool swap = !kCompOrder && l < 12 && c == 1;
+  #pragma unroll
+        for (int b = 0; b < 6; ++b)
+        {
+          v[2 * b]     = swap ? jo[b] : je[b];
+          v[2 * b + 1] = swap ? je[b] : jo[b];
+        }
+  #pragma unroll
+        for (int b = 0; b < 3; ++b)
+        {
+          v[12 + b] = jp[b]; // zero on pressure rows
+        }
+        v[15] = T(0);
+        storeRecord(static_cast<T*>(a.geb) + 16LL * k, v);
+      }
     }
-  }
-  if (kGather && has && !live && l < 15)
-  {
-    // a rejected element (reported through the status word) adds nothing
-    const int k = a.gslot[15 * e + l];
-    a.gres[k]   = 0.0;
-    if (kJac)
+    if (has && !live && l < 15)
     {
-      T z[16];
-#pragma unroll
-      for (int i = 0; i < 16; ++i)
+      // a rejected element (reported through the status word) adds nothing
+      const int k = a.gslot[15 * e + l];
+      a.gres[k]   = 0.0;
+      if (kJac)
       {
-        z[i] = T(0);
+        T z[16];
+  #pragma unroll
+        for (int i = 0; i < 16; ++i)
+        {
+          z[i] = T(0);
+        }
+        storeRecord(static_cast<T*>(a.geb) + 16LL * k, z);
       }
-      storeRecord(static_cast<T*>(a.geb) + 16LL * k, z);
     }
   }
   // Every global reduction below adds into arrays that the previous kernel
@@ -839,6 +866,17 @@ __global__ void __launch_bounds__(kThreads, 12) thKernel(ThArgs a)
   thBlock<T, kJac, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
 }
 
+// FP64-accurate Jacobian (and residual) in double-float arithmetic on the
+// FP32 pipe, the 16-lane layout of the FP32 kernel.
+template <bool kRes>
+__global__ void __launch_bounds__(kThreads, 4) thKernelDd(ThArgs a)
+{
+  __shared__ ThSmem<gbfem::Dd> sm;
+  thStageRef(sm, a.status);
+  __syncthreads();
+  thBlock<gbfem::Dd, true, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
 // MIXED: FP32-quadrature Jacobian and FP64 residual in one pass.
 __global__ void __launch_bounds__(kThreads) thKernelMixed(ThArgs a)
 {
@@ -862,6 +900,32 @@ __global__ void __launch_bounds__(kThreads) thVjpKernel(ThArgs a)
 // Reference tables in constant memory: the thread-per-element kernel below
 // reads every entry with the same address across the warp (broadcast).
 __constant__ ThRef<double> kRefC = makeRef();
+
+// Convection weights W[q][a][b][k] = w_q N^_a(q) dN^_b,k(q): the convection
+// block is A_ab = sum_q sum_k W[q][a][b][k] ut_k(q), two FMAs per point
+// instead of three.
+struct ConvW
+{
+  double w[kNq][6][6][2];
+};
+constexpr ConvW makeConvW()
+{
+  const ThRef<double> t = makeRef();
+  ConvW               c{};
+  for (int q = 0; q < kNq; ++q)
+  {
+    for (int a = 0; a < 6; ++a)
+    {
+      for (int b = 0; b < 6; ++b)
+      {
+        c.w[q][a][b][0] = t.wN[q][a] * t.dNr[q][b][0];
+        c.w[q][a][b][1] = t.wN[q][a] * t.dNr[q][b][1];
+      }
+    }
+  }
+  return c;
+}
+__constant__ ConvW kConvW = makeConvW();
 
 // FP64 residual, one thread per element, by direct quadrature:
 //   R_(a,c) = sum_q [Ft_c(q) . dN^_a(q) + src_c(q) N^_a(q)],

@@ -198,6 +198,7 @@ def test_taylor_hood_256_pattern_is_bit_exact(cavity256):
 
 @pytest.mark.parametrize("precision,det,tol_j,tol_r", [
     ("fp64", False, 1e-12, 1e-12), ("fp64", True, 1e-12, 1e-12),
+    ("double_float", False, 1e-12, 1e-12),
     ("mixed", False, 1e-6, 1e-12), ("fp32_quad", False, 1e-6, 1e-6)])
 def test_taylor_hood_256_matches_oracle(cavity256, precision, det, tol_j, tol_r):
     """The benchmark's cavity (256x256, Re = 1000, seeded stream-function

@@ -204,6 +204,9 @@ def p1_gpu(m, coords, kappa, f, u, precision="fp64"):
 # (precision, Jacobian tolerance, residual tolerance): MIXED keeps the
 # residual in FP64 while the Jacobian comes from FP32 quadrature.
 PRECS = [("fp64", TOL64, TOL64), ("fp32_quad", TOL32, TOL32), ("mixed", TOL32, TOL64)]
+# Taylor-Hood adds the double-float mode (FP64-accurate element arithmetic
+# on the FP32 pipe), held to the FP64 gate
+TH_PRECS = PRECS + [("double_float", TOL64, TOL64)]
 
 
 @pytest.mark.parametrize("case", ["p1_32", "p1_jit9", "real_sq_p1"])
@@ -349,7 +352,7 @@ def th_gpu(g_coords, conn6, elem_dofs, nd, nu, state, precision="fp64"):
 
 
 @pytest.mark.parametrize("case", ["th_4", "th_jit3", "real_sq_th"])
-@pytest.mark.parametrize("precision,tol_j,tol_r", PRECS)
+@pytest.mark.parametrize("precision,tol_j,tol_r", TH_PRECS)
 def test_taylor_hood_matches_reference(case, precision, tol_j, tol_r):
     g = load_golden(case)
     _, res, vals = th_gpu(g["coords"], g["conn6"], g["elem_dofs"], int(g["num_dofs"]),
@@ -366,7 +369,7 @@ def test_taylor_hood_cavity_matches_oracle():
     state = np.concatenate([vel.reshape(-1), np.random.default_rng(3).standard_normal(nv)])
     om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
     rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-3, state)
-    for precision, tol_j, tol_r in PRECS:
+    for precision, tol_j, tol_r in TH_PRECS:
         _, res, vals = th_gpu(cp2, conn6, dofs, nd, 1e-3, state, precision)
         assert rel_inf(res, rres) <= tol_r
         assert rel_inf(vals, rvals) <= tol_j
@@ -462,7 +465,8 @@ def test_csr_transpose_of_taylor_hood_jacobian():
     assert isinstance(ref, sp.csr_matrix)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_quad", 1e-6), ("mixed", 1e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32_quad", 1e-6), ("mixed", 1e-6),
+                                           ("double_float", 1e-12)])
 def test_taylor_hood_state_vjp_matches_oracle(precision, tol):
     """J(u)^T lam without forming J, against the oracle's J transposed."""
     c3, k3 = meshes.jittered_tri(12, seed=21)

@@ -5,7 +5,7 @@ deterministic mode: exact integrals for linear fields on jittered meshes
 Couette, shear, stagnation flow, a pressure gradient) and the Jacobian's
 identities (tests/th_checks.py). These pins share no code with the oracle.
 
-Tolerances: FP64 1e-12; FP32 quadrature 1e-6 (J and R; R relative to the
+Tolerances: FP64 and double-float 1e-12; FP32 quadrature 1e-6 (J and R; R relative to the
 size of its terms, which cancel for these fields); MIXED J 1e-6 and R 1e-12
 (its residual is computed to FP64 accuracy).
 """
@@ -29,6 +29,8 @@ MODES = [
     ("fp32_quad", True, 1e-6, 1e-6),
     ("mixed", False, 1e-12, 1e-6),
     ("mixed", True, 1e-12, 1e-6),
+    ("double_float", False, 1e-12, 1e-12),
+    ("double_float", True, 1e-12, 1e-12),
 ]
 IDS = [f"{p}{'-det' if d else ''}" for p, d, _, _ in MODES]
 
