@@ -843,7 +843,7 @@ def main():
                     cpu_sample.append(("th", conn6.shape[0], cp2, conn6, offs, dofs, nd,
                                        1.0 / re, st_k, lam_k))
                 n_th += 1
-        batch = Batch(insts)
+        batch = Batch(insts, coloured=True)
         runs, tuned = {}, {}
         for prec in ("fp64", "mixed", "fp32_quad"):
             params, tune = autotune(batch, prec, reps=2, use_cache=False)
@@ -869,6 +869,23 @@ def main():
             batch.check()
         t_b32, t_b64, t_bmx = runs["fp32_quad"], runs["fp64"], runs["mixed"]
         launches += 6 * args.steps
+        # deterministic runs: the colouring scheme (colour rounds, plain adds)
+        det_runs = {}
+        for prec in ("fp64", "fp32_quad"):
+            params, _ = autotune(batch, prec, reps=2, use_cache=False, deterministic=True)
+            gr = batch.graph(prec, **params)
+            det_runs[prec] = {"ms_per_step": maxrank(timer.run(gr.replay, args.steps,
+                                                               args.warmup)) * 1e3,
+                              "params": params}
+            gr.replay()
+            torch.cuda.synchronize()
+            first = [x.vals.clone() for x in insts]
+            gr.replay()
+            torch.cuda.synchronize()
+            det_runs[prec]["bitwise_equal_over_runs"] = all(
+                torch.equal(a, x.vals) for a, x in zip(first, insts))
+            del gr, first
+            launches += args.steps * (2 + max(x.amap.numColours() for x in insts))
         # Baseline of the same kind: one CUDA graph of per-instance calls of
         # the standalone kernels (assemble + VJP per instance, each with its
         # own zero fill), replayed like the persistent launch's graph.
@@ -926,6 +943,7 @@ def main():
                                          "(Taylor-Hood: double-float, P1: fp64) and P1 "
                                          "gradients fp64; Taylor-Hood J^T lam from the fp32 J"},
             "autotuned": tuned,
+            "deterministic_colouring": det_runs,
             "per_instance_graph": {
                 "what": "one CUDA graph of per-instance standalone calls (assemble with its "
                         "zero fill + VJP per instance) on the same instances and outputs",

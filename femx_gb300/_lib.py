@@ -24,6 +24,7 @@ PREC_FP32_QUAD = 1
 PREC_MIXED = 2
 PREC_DOUBLE_FLOAT = 3
 DETERMINISTIC = 0x100
+COLOURED = 0x200
 
 
 class GbfemError(RuntimeError):
@@ -132,7 +133,9 @@ SIGNATURES = {
                                    _vp]),
     "gbfem_probe_fp64_fma": (_i, [_i, _i, _i, _vp, _vp]),
     "gbfem_batch_create": (_i, [_i, C.POINTER(BatchInstance), _vp, C.POINTER(_vp)]),
-    "gbfem_batch_run": (_i, [_vp, _i, _i, _i, _i, _vp]),
+    "gbfem_batch_run": (_i, [_vp, _i, _i, _i, _i, _i, _vp]),
+    "gbfem_assembly_map_enable_colouring": (_i, [_vp, _vp]),
+    "gbfem_assembly_map_num_colours": (_i, [_vp]),
     "gbfem_batch_check": (_i, [_vp, _vp]),
     "gbfem_batch_num_elems": (C.c_longlong, [_vp]),
     "gbfem_batch_destroy": (None, [_vp]),

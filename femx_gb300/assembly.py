@@ -178,6 +178,17 @@ class AssemblyMap:
             call("gbfem_assembly_map_enable_gather", self._h, _stream())
             self._gather = True
 
+    def enableColouring(self):
+        """Colour the elements (no two of a colour share a DOF) for coloured
+        assembly: plain adds colour by colour, no atomics, bitwise
+        reproducible (setup, once per map; synchronizes the current stream).
+        Returns the number of colours."""
+        call("gbfem_assembly_map_enable_colouring", self._h, _stream())
+        return self.numColours()
+
+    def numColours(self):
+        return int(_lib.lib().gbfem_assembly_map_num_colours(self._h))
+
     def check(self):
         """Raise if a kernel met invalid data (e.g. a degenerate element)."""
         call("gbfem_assembly_map_check", self._h, _stream())
@@ -297,9 +308,20 @@ def _jac_ptr(amap: AssemblyMap, jac):
     return _ptr(jac.vals)
 
 
+def _mode(precision, coloured=False, deterministic=False):
+    mode = PRECISIONS[precision]
+    if coloured:
+        mode |= _lib.COLOURED
+    if deterministic:
+        mode |= _lib.DETERMINISTIC
+    return mode
+
+
 def assembleP1Kappa(amap: AssemblyMap, coords, kappa, f_nodal, u, res, jac=None, conn=None,
-                    precision: str = "fp64"):
-    """Residual (and Jacobian) of the kappa-weighted P1 Poisson operator."""
+                    precision: str = "fp64", coloured: bool = False):
+    """Residual (and Jacobian) of the kappa-weighted P1 Poisson operator.
+    coloured=True: colour by colour with plain adds (amap.enableColouring()
+    first), bitwise reproducible."""
     coords = _dev(coords, torch.float64, "coords")
     kappa = _check_vec(kappa, amap.numElems(), "kappa")
     u = _check_vec(u, amap.numStates(), "state")
@@ -308,11 +330,11 @@ def assembleP1Kappa(amap: AssemblyMap, coords, kappa, f_nodal, u, res, jac=None,
     conn = _dev(conn, torch.int32, "conn", allow_none=True)
     call("gbfem_assemble_p1_kappa", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
          _ptr(kappa), _ptr(f_nodal), _ptr(u), _ptr(res), _jac_ptr(amap, jac),
-         PRECISIONS[precision], _stream())
+         _mode(precision, coloured), _stream())
 
 
 def vjpP1Kappa(amap: AssemblyMap, coords, kappa, u, lam, g_u=None, g_m=None, conn=None,
-               precision: str = "fp64"):
+               precision: str = "fp64", coloured: bool = False):
     coords = _dev(coords, torch.float64, "coords")
     kappa = _check_vec(kappa, amap.numElems(), "kappa")
     u = _check_vec(u, amap.numStates(), "state")
@@ -323,26 +345,28 @@ def vjpP1Kappa(amap: AssemblyMap, coords, kappa, u, lam, g_u=None, g_m=None, con
         g_m = _check_vec(g_m, amap.numElems(), "control gradient")
     conn = _dev(conn, torch.int32, "conn", allow_none=True)
     call("gbfem_vjp_p1_kappa", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
-         _ptr(kappa), _ptr(u), _ptr(lam), _ptr(g_u), _ptr(g_m), PRECISIONS[precision],
+         _ptr(kappa), _ptr(u), _ptr(lam), _ptr(g_u), _ptr(g_m), _mode(precision, coloured),
          _stream())
 
 
 def assembleTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, res, jac=None,
-                       precision: str = "fp64", deterministic: bool = False):
+                       precision: str = "fp64", deterministic: bool = False,
+                       coloured: bool = False):
     """Taylor-Hood Newton residual (and Jacobian when jac is given).
     deterministic=True sums element rows per CSR row in element order (no
     atomics): bitwise reproducible; the first call on a map builds its
-    row-gather tables (amap.enableDeterministic())."""
+    row-gather tables (amap.enableDeterministic()). coloured=True runs the
+    elements colour by colour with plain adds (amap.enableColouring()
+    first), also bitwise reproducible."""
     coords = _dev(coords, torch.float64, "coords")
     conn6 = _dev(conn6, torch.int32, "conn6")
     state = _check_vec(state, amap.numStates(), "state")
     res = _check_vec(res, amap.numRes(), "residual")
-    mode = PRECISIONS[precision]
     if deterministic:
         amap.enableDeterministic()
-        mode |= _lib.DETERMINISTIC
     call("gbfem_assemble_th_ns", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn6),
-         float(nu), _ptr(state), _ptr(res), _jac_ptr(amap, jac), mode, _stream())
+         float(nu), _ptr(state), _ptr(res), _jac_ptr(amap, jac),
+         _mode(precision, coloured, deterministic), _stream())
 
 
 def _check_host_vec(v, n, name):
@@ -381,7 +405,7 @@ def newtonSystemTaylorHoodHost(amap: AssemblyMap, bc: BoundaryMap, coords, conn6
 
 
 def vjpTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, lam, g_state,
-                  precision: str = "fp64"):
+                  precision: str = "fp64", coloured: bool = False):
     """g_state = J(state)^T lam of the Taylor-Hood residual, without forming J."""
     coords = _dev(coords, torch.float64, "coords")
     conn6 = _dev(conn6, torch.int32, "conn6")
@@ -389,7 +413,8 @@ def vjpTaylorHood(amap: AssemblyMap, coords, conn6, nu, state, lam, g_state,
     lam = _check_vec(lam, amap.numRes(), "adjoint")
     g_state = _check_vec(g_state, amap.numStates(), "VJP output")
     call("gbfem_vjp_th_ns", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn6),
-         float(nu), _ptr(state), _ptr(lam), _ptr(g_state), PRECISIONS[precision], _stream())
+         float(nu), _ptr(state), _ptr(lam), _ptr(g_state), _mode(precision, coloured),
+         _stream())
 
 
 def assembleNavier(amap: AssemblyMap, coords, conn, rho, mu, dt, step, hist, nxt, res,

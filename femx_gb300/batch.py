@@ -7,10 +7,14 @@ adjoint ``lam`` is given) on its own AssemblyMap. ``run()`` enqueues two
 kernels and allocates nothing, so it can be captured in a CUDA graph
 (``Batch.graph()``).
 
-``autotune()`` times the launch parameters — elements per P1 work item,
-Taylor–Hood elements per work item, resident blocks per SM — on the actual
-batch and caches the fastest per (GPU, precision, batch size class) in a JSON
-file (``$GBFEM_TUNE_CACHE`` or ``~/.cache/gbfem/tune.json``).
+``autotune()`` times the launch parameters on the actual batch — elements
+per P1 work item, Taylor–Hood elements per work item, resident blocks per
+SM, the staging depth (work items claimed ahead with their inputs
+prefetched into L2) and the scatter scheme (FP64 atomics, or colouring:
+colour rounds with plain adds, bitwise reproducible) — and caches the
+fastest per (GPU, precision, batch size class, determinism) in a JSON file
+(``$GBFEM_TUNE_CACHE`` or ``~/.cache/gbfem/tune.json``). With
+``deterministic=True`` only the colouring scheme is a candidate.
 """
 from __future__ import annotations
 
@@ -27,9 +31,11 @@ from .assembly import PRECISIONS, AssemblyMap, _dev, _ptr, _stream
 
 __all__ = ["Batch", "P1Instance", "THInstance", "autotune", "DEFAULT_PARAMS"]
 
-DEFAULT_PARAMS = {"p1_chunk": 512, "th_chunk": 16, "blocks_per_sm": 8}
+DEFAULT_PARAMS = {"p1_chunk": 512, "th_chunk": 16, "blocks_per_sm": 8, "stage_depth": 0,
+                  "scatter": "atomic"}
 SEARCH = {"p1_chunk": (256, 512, 1024, 2048), "th_chunk": (8, 16, 32, 64),
-          "blocks_per_sm": (4, 6, 8, 12)}
+          "blocks_per_sm": (4, 6, 8, 12), "stage_depth": (0, 1),
+          "scatter": ("atomic", "colour")}
 
 
 class P1Instance:
@@ -77,8 +83,15 @@ class THInstance:
 
 
 class Batch:
-    def __init__(self, instances):
+    """coloured=True colours every instance's map first, so that runs may
+    take the colouring scatter scheme (scatter="colour")."""
+
+    def __init__(self, instances, coloured=False):
         self.instances = list(instances)
+        self.coloured = bool(coloured)
+        if self.coloured:
+            for x in self.instances:
+                x.amap.enableColouring()
         arr = (_lib.BatchInstance * len(self.instances))(*[x.desc() for x in self.instances])
         h = C.c_void_p()
         call("gbfem_batch_create", len(self.instances), arr, _stream(), C.byref(h))
@@ -91,12 +104,16 @@ class Batch:
             _lib._lib.gbfem_batch_destroy(h)
             self._h = None
 
-    def run(self, precision="fp32_quad", p1_chunk=None, th_chunk=None, blocks_per_sm=None):
+    def run(self, precision="fp32_quad", p1_chunk=None, th_chunk=None, blocks_per_sm=None,
+            stage_depth=None, scatter=None):
         p = dict(DEFAULT_PARAMS)
         p.update({k: v for k, v in (("p1_chunk", p1_chunk), ("th_chunk", th_chunk),
-                                    ("blocks_per_sm", blocks_per_sm)) if v is not None})
-        call("gbfem_batch_run", self._h, PRECISIONS[precision], p["p1_chunk"], p["th_chunk"],
-             p["blocks_per_sm"], _stream())
+                                    ("blocks_per_sm", blocks_per_sm),
+                                    ("stage_depth", stage_depth), ("scatter", scatter))
+                  if v is not None})
+        mode = PRECISIONS[precision] | (_lib.COLOURED if p["scatter"] == "colour" else 0)
+        call("gbfem_batch_run", self._h, mode, p["p1_chunk"], p["th_chunk"],
+             p["blocks_per_sm"], p["stage_depth"], _stream())
 
     def check(self):
         call("gbfem_batch_check", self._h, _stream())
@@ -120,11 +137,26 @@ def _cache_path():
                           os.path.join(os.path.expanduser("~"), ".cache", "gbfem", "tune.json"))
 
 
-def autotune(batch: Batch, precision="fp32_quad", reps=3, use_cache=True):
-    """Coordinate search over SEARCH, starting from DEFAULT_PARAMS. Returns
-    (params, timings) and stores the winner in the cache."""
+def _candidates(batch: Batch, precision, deterministic):
+    search = dict(SEARCH)
+    if deterministic:
+        search["scatter"] = ("colour",)
+    elif not batch.coloured or precision == "mixed":
+        search["scatter"] = ("atomic",)
+    return search
+
+
+def autotune(batch: Batch, precision="fp32_quad", reps=3, use_cache=True,
+             deterministic=False):
+    """Coordinate search over SEARCH, starting from DEFAULT_PARAMS (the
+    scatter axis needs a Batch made with coloured=True; deterministic=True
+    keeps it at colouring, which MIXED does not offer). Returns (params,
+    timings) and stores the winner in the cache."""
+    if deterministic and (not batch.coloured or precision == "mixed"):
+        raise ValueError("deterministic batch runs need Batch(coloured=True) and FP64 or "
+                         "FP32_QUAD")
     gpu = torch.cuda.get_device_name()
-    key = f"{gpu}|batch|{precision}|{batch.signature()}"
+    key = f"{gpu}|batch|{precision}|det={int(deterministic)}|{batch.signature()}"
     path = _cache_path()
     cache = {}
     if os.path.exists(path):
@@ -147,10 +179,12 @@ def autotune(batch: Batch, precision="fp32_quad", reps=3, use_cache=True):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps
 
+    search = _candidates(batch, precision, deterministic)
     best = dict(DEFAULT_PARAMS)
+    best["scatter"] = search["scatter"][0]
     best_t = time_of(best)
     timings = {json.dumps(best, sort_keys=True): best_t}
-    for name, choices in SEARCH.items():
+    for name, choices in search.items():
         for v in choices:
             cand = dict(best)
             cand[name] = v

@@ -18,6 +18,7 @@
 //      J^T lam (a reduction over the element's rows).
 // The item decode (instance prefix of chunk counts) is built by every block
 // in shared memory from the descriptor table at kernel start.
+#include <algorithm>
 #include <vector>
 
 #include "p1_elem.cuh"
@@ -34,11 +35,16 @@ static_assert(kBatchThreads == kThreads, "Taylor-Hood block shape");
 
 struct BatchDesc
 {
-  int    kind;
-  int    num_elems;
-  P1Args p1;
-  ThArgs th;
+  int        kind;
+  int        num_elems;
+  int        num_colours;  // 0 when the instance's map is not coloured
+  const int* colour_off;   // [num_colours + 1], device
+  const int* colour_elems; // elements colour by colour, device
+  P1Args     p1;
+  ThArgs     th;
 };
+
+constexpr int kMaxRounds = 64; // colours (one launch each) of a coloured run
 
 struct ZeroSeg
 {
@@ -55,7 +61,10 @@ __global__ void zeroSegments(const ZeroSeg* __restrict__ segs,
   {
     if (blockIdx.x == 0)
     {
-      *ticket = 0;
+      for (int r = 0; r < kMaxRounds; ++r)
+      {
+        ticket[r] = 0;
+      }
     }
     int lo = 0, hi = nseg;
     while (hi - lo > 1)
@@ -89,10 +98,35 @@ constexpr int kModeFp64  = 0;
 constexpr int kModeFp32  = 1;
 constexpr int kModeMixed = 2;
 
-__device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th_chunk)
+// Elements of an instance in a launch: all of them, or, in a coloured run,
+// those of colour `round` (none once the instance's colours are exhausted).
+__device__ __forceinline__ int roundElems(const BatchDesc& d, int round)
+{
+  if (round < 0)
+  {
+    return d.num_elems;
+  }
+  return round < d.num_colours ? d.colour_off[round + 1] - d.colour_off[round] : 0;
+}
+
+__device__ __forceinline__ int chunksOf(const BatchDesc& d, int p1_chunk, int th_chunk,
+                                        int round)
 {
   const int c = d.kind == GBFEM_BATCH_P1_KAPPA ? p1_chunk : th_chunk;
-  return (d.num_elems + c - 1) / c;
+  return (roundElems(d, round) + c - 1) / c;
+}
+
+// Staging of the next work item (depth 1): the byte ranges of its element
+// DOF table and connectivity (and the P1 coefficients) are prefetched into
+// L2 while the current item runs, so that its first dependent gathers hit.
+__device__ __forceinline__ void prefetchL2(const void* p, long long bytes)
+{
+  const char* c = static_cast<const char*>(p);
+  for (long long off = static_cast<long long>(threadIdx.x) * 128; off < bytes;
+       off += static_cast<long long>(blockDim.x) * 128)
+  {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(c + off));
+  }
 }
 
 // MIXED: the Taylor-Hood residuals of every instance (double-float on the
@@ -124,40 +158,43 @@ __global__ void __launch_bounds__(kBatchThreads)
   thResidualDFElem(descs[th_idx[lo]].th, static_cast<int>(g - th_prefix[lo]));
 }
 
-template <int kMode, bool kSep, bool kLoad, bool kVjp>
-__device__ __forceinline__ void p1Chunk(const P1Args& a, int e0, int e1)
+// Elements [e0, e1) of an instance, or of its colour list (elems != null:
+// coloured run, plain adds).
+template <int kMode, bool kSep, bool kLoad, bool kVjp, bool kPlain>
+__device__ __forceinline__ void p1Chunk(const P1Args& a, int e0, int e1, const int* elems)
 {
-  for (int e = e0 + static_cast<int>(threadIdx.x); e < e1; e += kBatchThreads)
+  for (int i = e0 + static_cast<int>(threadIdx.x); i < e1; i += kBatchThreads)
   {
+    const int e = kPlain ? elems[i] : i;
     if (kMode == kModeFp64)
     {
-      p1Element<false, kSep, kLoad, true, true, kVjp>(a, e);
+      p1Element<false, kSep, kLoad, true, true, kVjp, kPlain>(a, e);
     }
     else if (kMode == kModeFp32)
     {
-      p1Element<true, kSep, kLoad, true, true, kVjp>(a, e);
+      p1Element<true, kSep, kLoad, true, true, kVjp, kPlain>(a, e);
     }
     else
     {
-      p1Element<true, kSep, false, true, false, false>(a, e);
-      p1Element<false, kSep, kLoad, false, true, kVjp>(a, e);
+      p1Element<true, kSep, false, true, false, false, kPlain>(a, e);
+      p1Element<false, kSep, kLoad, false, true, kVjp, kPlain>(a, e);
     }
   }
 }
 
-template <int kMode, bool kSep>
-__device__ __forceinline__ void p1Dispatch(const P1Args& a, int e0, int e1)
+template <int kMode, bool kSep, bool kPlain>
+__device__ __forceinline__ void p1Dispatch(const P1Args& a, int e0, int e1, const int* elems)
 {
   const bool load = a.f != nullptr, vjp = a.lam != nullptr;
   if (load)
   {
-    vjp ? p1Chunk<kMode, kSep, true, true>(a, e0, e1)
-        : p1Chunk<kMode, kSep, true, false>(a, e0, e1);
+    vjp ? p1Chunk<kMode, kSep, true, true, kPlain>(a, e0, e1, elems)
+        : p1Chunk<kMode, kSep, true, false, kPlain>(a, e0, e1, elems);
   }
   else
   {
-    vjp ? p1Chunk<kMode, kSep, false, true>(a, e0, e1)
-        : p1Chunk<kMode, kSep, false, false>(a, e0, e1);
+    vjp ? p1Chunk<kMode, kSep, false, true, kPlain>(a, e0, e1, elems)
+        : p1Chunk<kMode, kSep, false, false, kPlain>(a, e0, e1, elems);
   }
 }
 
@@ -180,17 +217,76 @@ struct BatchSmem<kModeMixed>
   using type = ThSmem<float>;
 };
 
+// Where a work item lies: instance `inst`, its element range [e0, e1) (in
+// the instance's colour list for a coloured run).
+struct BatchItem
+{
+  int inst, e0, e1;
+};
+
+__device__ __forceinline__ BatchItem decodeItem(const int* prefix, int ni, int it,
+                                                const BatchDesc* descs, int p1_chunk,
+                                                int th_chunk, int round)
+{
+  int lo = 0, hi = ni;
+  while (hi - lo > 1)
+  {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= it)
+    {
+      lo = mid;
+    }
+    else
+    {
+      hi = mid;
+    }
+  }
+  const BatchDesc& d     = descs[lo];
+  const int        chunk = d.kind == GBFEM_BATCH_P1_KAPPA ? p1_chunk : th_chunk;
+  const int        e0    = (it - prefix[lo]) * chunk;
+  return {lo, e0, min(roundElems(d, round), e0 + chunk)};
+}
+
+// The next item's element DOF table and connectivity (and P1 coefficients)
+// into L2 (the staging of depth 1).
+__device__ __forceinline__ void stageItem(const BatchDesc& d, const BatchItem& w, int round)
+{
+  if (round >= 0)
+  {
+    return; // coloured runs gather through the colour list
+  }
+  const long long n = w.e1 - w.e0;
+  if (d.kind == GBFEM_BATCH_P1_KAPPA)
+  {
+    prefetchL2(d.p1.dofs + 3LL * w.e0, 12 * n);
+    prefetchL2(d.p1.kappa + w.e0, 8 * n);
+    if (d.p1.conn != nullptr)
+    {
+      prefetchL2(d.p1.conn + 3LL * w.e0, 12 * n);
+    }
+  }
+  else
+  {
+    prefetchL2(d.th.dofs + 15LL * w.e0, 60 * n);
+    prefetchL2(d.th.conn6 + 6LL * w.e0, 24 * n);
+  }
+}
+
 // FP32 and MIXED: at least six resident blocks per SM (at most 80 registers;
 // left free, the compiler takes 128-147 and four blocks fit, and the
 // kernel, which waits mostly on its dependent gathers, runs 3 % slower).
-template <int kMode>
+// round < 0: every element of every instance, FP64 reductions; round >= 0
+// (kPlain): the elements of colour `round` of each instance, plain adds
+// (elements of one colour share no DOF), one launch per colour. kStage: work
+// items claimed this many ahead, their inputs prefetched into L2 (0 or 1).
+template <int kMode, bool kPlain, int kStage>
 __global__ void __launch_bounds__(kBatchThreads, kMode == kModeFp64 ? 1 : 6)
     batchKernel(const BatchDesc* __restrict__ descs, int ni, int p1_chunk, int th_chunk,
-                int* __restrict__ ticket)
+                int* __restrict__ ticket, int round)
 {
   __shared__ typename BatchSmem<kMode>::type sm;
   __shared__ int                             prefix[kMaxInstances + 1];
-  __shared__ int                             item;
+  __shared__ int                             item[2];
   // every instance reports into the batch's one status word
   DeviceStatus* status = ni > 0 ? (descs[0].kind == GBFEM_BATCH_P1_KAPPA ? descs[0].p1.status
                                                                           : descs[0].th.status)
@@ -202,71 +298,86 @@ __global__ void __launch_bounds__(kBatchThreads, kMode == kModeFp64 ? 1 : 6)
     for (int i = 0; i < ni; ++i)
     {
       prefix[i] = acc;
-      acc += chunksOf(descs[i], p1_chunk, th_chunk);
+      acc += chunksOf(descs[i], p1_chunk, th_chunk, round);
     }
     prefix[ni] = acc;
+    item[0]    = atomicAdd(ticket, 1);
   }
   __syncthreads();
   const int total = prefix[ni];
-  for (;;)
+  for (int k = 0;; k ^= 1)
   {
-    if (threadIdx.x == 0)
-    {
-      item = atomicAdd(ticket, 1);
-    }
-    __syncthreads();
-    const int it = item;
+    const int it = item[k];
     if (it >= total)
     {
       break;
     }
-    int lo = 0, hi = ni;
-    while (hi - lo > 1)
+    if (kStage > 0)
     {
-      const int mid = (lo + hi) >> 1;
-      if (prefix[mid] <= it)
+      // claim the next item now and stage its inputs while this one runs
+      if (threadIdx.x == 0)
       {
-        lo = mid;
+        item[k ^ 1] = atomicAdd(ticket, 1);
       }
-      else
+      __syncthreads();
+      const int nx = item[k ^ 1];
+      if (nx < total)
       {
-        hi = mid;
+        const BatchItem w = decodeItem(prefix, ni, nx, descs, p1_chunk, th_chunk, round);
+        stageItem(descs[w.inst], w, round);
       }
     }
-    const BatchDesc& d = descs[lo];
-    const int        c = it - prefix[lo];
+    const BatchItem  w  = decodeItem(prefix, ni, it, descs, p1_chunk, th_chunk, round);
+    const BatchDesc& d  = descs[w.inst];
+    const int*       el = kPlain ? d.colour_elems + d.colour_off[round] : nullptr;
     if (d.kind == GBFEM_BATCH_P1_KAPPA)
     {
-      const int e0 = c * p1_chunk;
-      const int e1 = min(d.num_elems, e0 + p1_chunk);
-      d.p1.conn != nullptr ? p1Dispatch<kMode, true>(d.p1, e0, e1)
-                           : p1Dispatch<kMode, false>(d.p1, e0, e1);
+      d.p1.conn != nullptr ? p1Dispatch<kMode, true, kPlain>(d.p1, w.e0, w.e1, el)
+                           : p1Dispatch<kMode, false, kPlain>(d.p1, w.e0, w.e1, el);
     }
     else
     {
-      const int  e0  = c * th_chunk;
-      const int  e1  = min(d.num_elems, e0 + th_chunk);
-      const bool vjp = d.th.lam != nullptr;
-      for (int eb = e0; eb < e1; eb += kElemsPerBlock)
+      ThArgs tc; // the coloured run's view of the instance
+      if (kPlain)
+      {
+        tc       = d.th;
+        tc.elems = el;
+        tc.ne    = roundElems(d, round);
+      }
+      const ThArgs& ta  = kPlain ? tc : d.th;
+      const bool    vjp = ta.lam != nullptr;
+      for (int eb = w.e0; eb < w.e1; eb += kElemsPerBlock)
       {
         if constexpr (kMode == kModeFp64)
         {
-          vjp ? thBlock<double, true, true, true>(d.th, eb, sm)
-              : thBlock<double, true, true, false>(d.th, eb, sm);
+          vjp ? thBlock<double, true, true, true, false, false, kPlain>(ta, eb, sm)
+              : thBlock<double, true, true, false, false, false, kPlain>(ta, eb, sm);
         }
         else if constexpr (kMode == kModeFp32)
         {
-          vjp ? thBlock<float, true, true, true>(d.th, eb, sm)
-              : thBlock<float, true, true, false>(d.th, eb, sm);
+          vjp ? thBlock<float, true, true, true, false, false, kPlain>(ta, eb, sm)
+              : thBlock<float, true, true, false, false, false, kPlain>(ta, eb, sm);
         }
         else
         {
-          vjp ? thBlock<float, true, false, true>(d.th, eb, sm)
-              : thBlock<float, true, false, false>(d.th, eb, sm);
+          vjp ? thBlock<float, true, false, true, false, false, kPlain>(ta, eb, sm)
+              : thBlock<float, true, false, false, false, false, kPlain>(ta, eb, sm);
         }
       }
     }
-    __syncthreads(); // everyone has read `item` before it is overwritten
+    if (kStage == 0)
+    {
+      __syncthreads(); // everyone has read item[k] before it is reused
+      if (threadIdx.x == 0)
+      {
+        item[k ^ 1] = atomicAdd(ticket, 1);
+      }
+      __syncthreads();
+    }
+    else
+    {
+      __syncthreads(); // item[k] is free for the claim after next
+    }
   }
 }
 
@@ -288,6 +399,8 @@ struct gbfem_batch
   long long            th_elems      = 0;
   int*                 d_th_idx      = nullptr; // their descriptor indices
   long long*           d_th_prefix   = nullptr; // [nth + 1] element offsets
+  bool                 all_coloured  = false;   // every instance's map coloured at creation
+  int                  max_colours   = 0;
 
   ~gbfem_batch()
   {
@@ -320,7 +433,7 @@ extern "C" int gbfem_batch_create(int n, const gbfem_batch_instance* inst, void*
                 "SM count");
       b->num_instances = n;
       b->d_status      = deviceAlloc<DeviceStatus>(1);
-      b->d_ticket      = deviceAlloc<int>(1);
+      b->d_ticket      = deviceAlloc<int>(kMaxRounds);
       cudaCheck(cudaMemsetAsync(b->d_status, 0, sizeof(DeviceStatus), s), "memset");
       std::vector<BatchDesc> descs(n);
       std::vector<ZeroSeg>   segs;
@@ -334,10 +447,19 @@ extern "C" int gbfem_batch_create(int n, const gbfem_batch_instance* inst, void*
                 "Geometry coordinates must be 16-byte aligned");
         require(m->num_res == m->num_states && m->same_dofs,
                 "batch instances need identical residual and state DOF tables");
-        BatchDesc& d = descs[i];
-        d            = BatchDesc{};
-        d.kind       = x.kind;
-        d.num_elems  = m->num_elems;
+        BatchDesc& d   = descs[i];
+        d              = BatchDesc{};
+        d.kind         = x.kind;
+        d.num_elems    = m->num_elems;
+        d.num_colours  = m->num_colours;
+        d.colour_off   = m->colour_off;
+        d.colour_elems = m->colour_elems;
+        if (i == 0)
+        {
+          b->all_coloured = true;
+        }
+        b->all_coloured = b->all_coloured && (m->num_elems == 0 || m->colour_elems != nullptr);
+        b->max_colours  = std::max(b->max_colours, m->num_colours);
         b->total_elems += m->num_elems;
         if (x.kind == GBFEM_BATCH_P1_KAPPA)
         {
@@ -468,18 +590,26 @@ extern "C" int gbfem_batch_create(int n, const gbfem_batch_instance* inst, void*
 }
 
 extern "C" int gbfem_batch_run(gbfem_batch* b, int precision, int p1_chunk, int th_chunk,
-                               int blocks_per_sm, void* stream)
+                               int blocks_per_sm, int stage_depth, void* stream)
 {
   using namespace gbfem;
   return guarded([&] {
     require(b != nullptr, "batch handle is null");
+    const bool col = (precision & GBFEM_COLOURED) != 0;
+    precision &= ~GBFEM_COLOURED;
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
             "unknown precision mode");
+    require(!col || b->all_coloured,
+            "coloured batch runs need gbfem_assembly_map_enable_colouring on every "
+            "instance's map before gbfem_batch_create");
+    require(!col || precision != GBFEM_PREC_MIXED,
+            "coloured batch runs take FP64 or FP32_QUAD");
     require(p1_chunk >= kBatchThreads && p1_chunk % kBatchThreads == 0,
             "p1_chunk must be a positive multiple of 128");
     require(th_chunk >= kElemsPerBlock && th_chunk % kElemsPerBlock == 0,
             "th_chunk must be a positive multiple of 8");
     require(blocks_per_sm >= 1 && blocks_per_sm <= 32, "blocks_per_sm must be in 1..32");
+    require(stage_depth == 0 || stage_depth == 1, "stage_depth must be 0 or 1");
     cudaStream_t s = asStream(stream);
     if (b->zero_blocks > 0)
     {
@@ -488,34 +618,46 @@ extern "C" int gbfem_batch_run(gbfem_batch* b, int precision, int p1_chunk, int 
     }
     else
     {
-      cudaCheck(cudaMemsetAsync(b->d_ticket, 0, sizeof(int), s), "ticket reset");
+      cudaCheck(cudaMemsetAsync(b->d_ticket, 0, sizeof(int) * kMaxRounds, s), "ticket reset");
     }
     cudaCheck(cudaGetLastError(), "batch zero launch");
     const unsigned grid = static_cast<unsigned>(b->sm_count * blocks_per_sm);
-    if (precision == GBFEM_PREC_FP64)
+    const int      nr   = col ? b->max_colours : 1;
+    for (int r = 0; r < nr; ++r)
     {
-      batchKernel<kModeFp64><<<grid, kBatchThreads, 0, s>>>(
-          b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
-    }
-    else if (precision == GBFEM_PREC_FP32_QUAD)
-    {
-      batchKernel<kModeFp32><<<grid, kBatchThreads, 0, s>>>(
-          b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
-    }
-    else
-    {
-      batchKernel<kModeMixed><<<grid, kBatchThreads, 0, s>>>(
-          b->d_descs, b->num_instances, p1_chunk, th_chunk, b->d_ticket);
-      if (b->th_elems > 0)
+      const int round = col ? r : -1;
+      int*      tk    = b->d_ticket + r;
+      auto      go    = [&](auto kernel) {
+        kernel<<<grid, kBatchThreads, 0, s>>>(b->d_descs, b->num_instances, p1_chunk, th_chunk,
+                                              tk, round);
+      };
+      if (precision == GBFEM_PREC_FP64)
       {
-        cudaCheck(cudaGetLastError(), "batch launch");
-        thResidualBatchKernel<<<static_cast<unsigned>((b->th_elems + kBatchThreads - 1)
-                                                      / kBatchThreads),
-                                kBatchThreads, 0, s>>>(b->d_descs, b->d_th_idx,
-                                                       b->d_th_prefix, b->nth);
+        col ? go(batchKernel<kModeFp64, true, 0>)
+            : (stage_depth ? go(batchKernel<kModeFp64, false, 1>)
+                           : go(batchKernel<kModeFp64, false, 0>));
       }
+      else if (precision == GBFEM_PREC_FP32_QUAD)
+      {
+        col ? go(batchKernel<kModeFp32, true, 0>)
+            : (stage_depth ? go(batchKernel<kModeFp32, false, 1>)
+                           : go(batchKernel<kModeFp32, false, 0>));
+      }
+      else
+      {
+        stage_depth ? go(batchKernel<kModeMixed, false, 1>)
+                    : go(batchKernel<kModeMixed, false, 0>);
+      }
+      cudaCheck(cudaGetLastError(), "batch launch");
     }
-    cudaCheck(cudaGetLastError(), "batch launch");
+    if (precision == GBFEM_PREC_MIXED && b->th_elems > 0)
+    {
+      thResidualBatchKernel<<<static_cast<unsigned>((b->th_elems + kBatchThreads - 1)
+                                                    / kBatchThreads),
+                              kBatchThreads, 0, s>>>(b->d_descs, b->d_th_idx, b->d_th_prefix,
+                                                     b->nth);
+      cudaCheck(cudaGetLastError(), "batch launch");
+    }
   });
 }
 

@@ -405,4 +405,20 @@ __device__ __forceinline__ void redAdd(double* addr, double v)
   asm volatile("red.global.add.f64 [%0], %1;" ::"l"(addr), "d"(v) : "memory");
 }
 
+// Adds v into *addr: an FP64 reduction at L2, or, in coloured assembly
+// (kPlain: no other thread of the launch touches addr), a plain
+// read-add-write.
+template <bool kPlain>
+__device__ __forceinline__ void addTo(double* addr, double v)
+{
+  if constexpr (kPlain)
+  {
+    *addr += v;
+  }
+  else
+  {
+    redAdd(addr, v);
+  }
+}
+
 } // namespace gbfem

@@ -1,6 +1,8 @@
 // maps.cuh — the device-resident AssemblyMap and BoundaryMap handles.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 // femx AssemblyMap<Device> (femx/assembly/AssemblyMap.hpp:78-206) plus the
@@ -63,6 +65,19 @@ struct gbfem_assembly_map
   unsigned char* gather_pos     = nullptr;
   double*        gather_eb      = nullptr;
   double*        gather_res     = nullptr;
+
+  // Element colouring, built on request by
+  // gbfem_assembly_map_enable_colouring: no two elements of one colour share
+  // a residual or state DOF, so the elements of a colour add into the
+  // residual, the matrix and the gradients with plain read-add-writes, no
+  // atomics, and colours run one after another: a fixed summation order,
+  // bitwise reproducible results. colour_elems lists the elements colour by
+  // colour (ascending within a colour); colour c is colour_elems[
+  // colour_off[c] .. colour_off[c + 1]) (host copy and device copy).
+  int               num_colours = 0;
+  std::vector<int>  colour_off_host;
+  int*              colour_off   = nullptr;
+  int*              colour_elems = nullptr;
 
   // Status word written by hot-path kernels that meet invalid data
   // (degenerate elements); read by gbfem_assembly_map_check().

@@ -37,27 +37,73 @@ __global__ void __launch_bounds__(256) p1VjpKernel(P1Args a)
   }
 }
 
-template <bool kF32, bool kSep>
-void launchAssemble(const P1Args& a, bool load, bool jac, cudaStream_t s)
+// Coloured element pass: thread i takes element elems[i] of one colour and
+// adds with plain read-add-writes (no element of the colour shares a DOF).
+template <bool kF32, bool kSep, bool kLoad, bool kJac, bool kRes, bool kVjp>
+__global__ void __launch_bounds__(256)
+    p1ColourKernel(P1Args a, const int* __restrict__ elems, int n)
 {
-  const unsigned blocks = gbfem::blocksFor(a.ne, 256);
-  // dependent launches: each overlaps the zero fill (or the kernel) before
-  // it on the stream up to its first reduction
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    p1Element<kF32, kSep, kLoad, kJac, kRes, kVjp, true>(a, elems[i]);
+  }
+}
+
+// One element pass: every element at once with FP64 reductions, or, when
+// coloured, one launch per colour in colour order. dep: the (first) launch
+// is a dependent of the zero fill before it and overlaps it up to its first
+// addition; later colours wait for the whole colour before them.
+template <bool kF32, bool kSep, bool kLoad, bool kJac, bool kRes, bool kVjp>
+void p1Pass(const P1Args& a, const gbfem_assembly_map* map, bool coloured, bool dep,
+            cudaStream_t s)
+{
+  if (!coloured)
+  {
+    if constexpr (kVjp)
+    {
+      gbfem::launchMaybeDependent(dep, p1VjpKernel<kF32, kSep>, gbfem::blocksFor(a.ne, 256),
+                                  256, s, a);
+    }
+    else
+    {
+      gbfem::launchMaybeDependent(dep, p1AssembleKernel<kF32, kSep, kLoad, kJac, kRes>,
+                                  gbfem::blocksFor(a.ne, 256), 256, s, a);
+    }
+    return;
+  }
+  for (int c = 0; c < map->num_colours; ++c)
+  {
+    const int b = map->colour_off_host[c], n = map->colour_off_host[c + 1] - b;
+    if (n > 0)
+    {
+      gbfem::launchMaybeDependent(dep && c == 0,
+                                  p1ColourKernel<kF32, kSep, kLoad, kJac, kRes, kVjp>,
+                                  gbfem::blocksFor(n, 256), 256, s, a,
+                                  static_cast<const int*>(map->colour_elems + b), n);
+    }
+  }
+}
+
+template <bool kF32, bool kSep>
+void launchAssemble(const P1Args& a, const gbfem_assembly_map* map, bool coloured, bool load,
+                    bool jac, bool dep, cudaStream_t s)
+{
   if (load && jac)
   {
-    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, true, true>, blocks, 256, s, a);
+    p1Pass<kF32, kSep, true, true, true, false>(a, map, coloured, dep, s);
   }
   else if (load)
   {
-    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, true, false>, blocks, 256, s, a);
+    p1Pass<kF32, kSep, true, false, true, false>(a, map, coloured, dep, s);
   }
   else if (jac)
   {
-    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, false, true>, blocks, 256, s, a);
+    p1Pass<kF32, kSep, false, true, true, false>(a, map, coloured, dep, s);
   }
   else
   {
-    gbfem::launchDependent(p1AssembleKernel<kF32, kSep, false, false>, blocks, 256, s, a);
+    p1Pass<kF32, kSep, false, false, true, false>(a, map, coloured, dep, s);
   }
 }
 
@@ -108,8 +154,12 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     require(res != nullptr, "Assembly residual output is null");
     require(res != u && vals != u && (vals == nullptr || res != vals),
             "Assembly state, residual, and matrix values must not alias");
+    const bool col = (precision & GBFEM_COLOURED) != 0;
+    precision &= ~GBFEM_COLOURED;
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
             "unknown precision mode");
+    require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
+            "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
     cudaStream_t s = asStream(stream);
@@ -125,28 +175,21 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     const bool sep  = conn != nullptr;
     if (precision == GBFEM_PREC_FP64 || (precision == GBFEM_PREC_MIXED && !jac))
     {
-      sep ? launchAssemble<false, true>(a, load, jac, s)
-          : launchAssemble<false, false>(a, load, jac, s);
+      sep ? launchAssemble<false, true>(a, map, col, load, jac, true, s)
+          : launchAssemble<false, false>(a, map, col, load, jac, true, s);
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
-      sep ? launchAssemble<true, true>(a, load, jac, s)
-          : launchAssemble<true, false>(a, load, jac, s);
+      sep ? launchAssemble<true, true>(a, map, col, load, jac, true, s)
+          : launchAssemble<true, false>(a, map, col, load, jac, true, s);
     }
     else
     {
       // Jacobian from FP32 quadrature, residual from FP64 element math
-      const unsigned blocks = blocksFor(a.ne, 256);
-      if (sep)
-      {
-        launchDependent(p1AssembleKernel<true, true, false, true, false>, blocks, 256, s, a);
-      }
-      else
-      {
-        launchDependent(p1AssembleKernel<true, false, false, true, false>, blocks, 256, s, a);
-      }
-      sep ? launchAssemble<false, true>(a, load, false, s)
-          : launchAssemble<false, false>(a, load, false, s);
+      sep ? p1Pass<true, true, false, true, false, false>(a, map, col, true, s)
+          : p1Pass<true, false, false, true, false, false>(a, map, col, true, s);
+      sep ? launchAssemble<false, true>(a, map, col, load, false, false, s)
+          : launchAssemble<false, false>(a, map, col, load, false, false, s);
     }
     cudaCheck(cudaGetLastError(), "P1 assembly launch");
   });
@@ -164,8 +207,12 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     require(lam != nullptr, "VJP adjoint input is null");
     require(g_u != lam && g_u != u && g_m != lam && g_m != u,
             "VJP outputs must not alias inputs");
+    const bool col = (precision & GBFEM_COLOURED) != 0;
+    precision &= ~GBFEM_COLOURED;
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
             "unknown precision mode");
+    require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
+            "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");
     cudaStream_t s = asStream(stream);
     a.lam          = lam;
     a.g_u          = g_u;
@@ -179,18 +226,17 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     {
       return;
     }
-    const unsigned blocks = blocksFor(a.ne, 256);
-    const bool     sep    = conn != nullptr;
+    const bool sep = conn != nullptr;
     const bool dep = g_u != nullptr;
     if (precision != GBFEM_PREC_FP32_QUAD)
     {
-      sep ? launchMaybeDependent(dep, p1VjpKernel<false, true>, blocks, 256, s, a)
-          : launchMaybeDependent(dep, p1VjpKernel<false, false>, blocks, 256, s, a);
+      sep ? p1Pass<false, true, false, false, false, true>(a, map, col, dep, s)
+          : p1Pass<false, false, false, false, false, true>(a, map, col, dep, s);
     }
     else
     {
-      sep ? launchMaybeDependent(dep, p1VjpKernel<true, true>, blocks, 256, s, a)
-          : launchMaybeDependent(dep, p1VjpKernel<true, false>, blocks, 256, s, a);
+      sep ? p1Pass<true, true, false, false, false, true>(a, map, col, dep, s)
+          : p1Pass<true, false, false, false, false, true>(a, map, col, dep, s);
     }
     cudaCheck(cudaGetLastError(), "P1 VJP launch");
   });

@@ -76,8 +76,10 @@ __device__ __forceinline__ bool elementK(double2 x0, double2 x1, double2 x2,
 
 // One element: residual (kRes), Jacobian scatter (kJac) and the fused
 // residual VJPs (kVjp: K^T lam into g_u, lam^T K u into g_m), all from one
-// evaluation of the element stiffness.
-template <bool kF32, bool kSepConn, bool kLoad, bool kJac, bool kRes, bool kVjp>
+// evaluation of the element stiffness. kPlain: coloured assembly, plain
+// read-add-writes instead of FP64 reductions.
+template <bool kF32, bool kSepConn, bool kLoad, bool kJac, bool kRes, bool kVjp,
+          bool kPlain = false>
 __device__ __forceinline__ void p1Element(const P1Args& a, int e)
 {
   using T = typename std::conditional<kF32, float, double>::type;
@@ -138,9 +140,9 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
   gbfem::awaitPrerequisites();
   if (kRes)
   {
-    gbfem::redAdd(a.res + d0, gbfem::toF64(r0));
-    gbfem::redAdd(a.res + d1, gbfem::toF64(r1));
-    gbfem::redAdd(a.res + d2, gbfem::toF64(r2));
+    gbfem::addTo<kPlain>(a.res + d0, gbfem::toF64(r0));
+    gbfem::addTo<kPlain>(a.res + d1, gbfem::toF64(r1));
+    gbfem::addTo<kPlain>(a.res + d2, gbfem::toF64(r2));
   }
   if (kJac)
   {
@@ -159,7 +161,7 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
         {
-          gbfem::redAdd(a.vals + rs + int((w >> (8 * j)) & 0xffu), v[3 * i + j]);
+          gbfem::addTo<kPlain>(a.vals + rs + int((w >> (8 * j)) & 0xffu), v[3 * i + j]);
         }
       }
     }
@@ -169,7 +171,7 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
 #pragma unroll
       for (int i = 0; i < 9; ++i)
       {
-        gbfem::redAdd(a.vals + jm[i], v[i]);
+        gbfem::addTo<kPlain>(a.vals + jm[i], v[i]);
       }
     }
   }
@@ -191,9 +193,9 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
       const double v2 = h02 * l0 + h12 * l1 + h22 * l2;
       if (a.g_u != nullptr)
       {
-        gbfem::redAdd(a.g_u + d0, kap * v0);
-        gbfem::redAdd(a.g_u + d1, kap * v1);
-        gbfem::redAdd(a.g_u + d2, kap * v2);
+        gbfem::addTo<kPlain>(a.g_u + d0, kap * v0);
+        gbfem::addTo<kPlain>(a.g_u + d1, kap * v1);
+        gbfem::addTo<kPlain>(a.g_u + d2, kap * v2);
       }
       if (a.g_m != nullptr)
       {
@@ -209,9 +211,9 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
       const T v2 = K.k02 * l0 + K.k12 * l1 + K.k22 * l2;
       if (a.g_u != nullptr)
       {
-        gbfem::redAdd(a.g_u + d0, v0);
-        gbfem::redAdd(a.g_u + d1, v1);
-        gbfem::redAdd(a.g_u + d2, v2);
+        gbfem::addTo<kPlain>(a.g_u + d0, v0);
+        gbfem::addTo<kPlain>(a.g_u + d1, v1);
+        gbfem::addTo<kPlain>(a.g_u + d2, v2);
       }
       if (a.g_m != nullptr)
       {

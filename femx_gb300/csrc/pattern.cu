@@ -405,7 +405,8 @@ void buildGatherTables(gbfem_assembly_map* m, cudaStream_t s)
 gbfem_assembly_map::~gbfem_assembly_map()
 {
   for (int* p : {res_offsets, res_dofs, state_offsets, state_dofs, jac_offsets,
-                 jac_map, row_ptr, col_ind, gather_off, gather_slot})
+                 jac_map, row_ptr, col_ind, gather_off, gather_slot, colour_off,
+                 colour_elems})
   {
     gbfem::deviceFree(p);
   }
@@ -705,4 +706,122 @@ extern "C" int gbfem_assembly_map_enable_gather(gbfem_assembly_map* m, void* str
 extern "C" void gbfem_assembly_map_destroy(gbfem_assembly_map* m)
 {
   delete m;
+}
+
+// Greedy element colouring (setup, on the host): elements in ascending
+// order take the smallest colour that no element sharing one of their
+// residual or state DOFs has taken. A DOF remembers the colours of its
+// elements as a 64-bit mask, so one pass over the DOF tables suffices.
+extern "C" int gbfem_assembly_map_enable_colouring(gbfem_assembly_map* m, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(m != nullptr, "AssemblyMap handle is null");
+    if (m->colour_elems != nullptr || m->num_elems == 0)
+    {
+      return;
+    }
+    cudaStream_t      s  = asStream(stream);
+    const int         ne = m->num_elems;
+    std::vector<int>  ro(ne + 1), so(ne + 1);
+    cudaCheck(cudaMemcpyAsync(ro.data(), m->res_offsets, sizeof(int) * (ne + 1),
+                              cudaMemcpyDeviceToHost, s),
+              "colouring readback");
+    cudaCheck(cudaMemcpyAsync(so.data(), m->state_offsets, sizeof(int) * (ne + 1),
+                              cudaMemcpyDeviceToHost, s),
+              "colouring readback");
+    cudaCheck(cudaStreamSynchronize(s), "colouring readback");
+    std::vector<int> rd(ro[ne]), sd(so[ne]);
+    if (ro[ne] > 0)
+    {
+      cudaCheck(cudaMemcpyAsync(rd.data(), m->res_dofs, sizeof(int) * ro[ne],
+                                cudaMemcpyDeviceToHost, s),
+                "colouring readback");
+    }
+    if (so[ne] > 0)
+    {
+      cudaCheck(cudaMemcpyAsync(sd.data(), m->state_dofs, sizeof(int) * so[ne],
+                                cudaMemcpyDeviceToHost, s),
+                "colouring readback");
+    }
+    cudaCheck(cudaStreamSynchronize(s), "colouring readback");
+    // residual DOF r and state DOF c are one DOF when the tables are shared
+    const long long            nres = m->num_res;
+    std::vector<unsigned long long> used(static_cast<size_t>(nres + m->num_states), 0ull);
+    std::vector<unsigned char>      colour(ne);
+    int                             ncol = 0;
+    auto key = [&](bool state, int d) -> size_t {
+      return static_cast<size_t>(state && !m->same_dofs ? nres + d : d);
+    };
+    for (int e = 0; e < ne; ++e)
+    {
+      unsigned long long forbid = 0ull;
+      for (int k = ro[e]; k < ro[e + 1]; ++k)
+      {
+        forbid |= used[key(false, rd[k])];
+      }
+      for (int k = so[e]; k < so[e + 1]; ++k)
+      {
+        forbid |= used[key(true, sd[k])];
+      }
+      require(forbid != ~0ull, "element colouring needs more than 64 colours");
+      int c = 0;
+      while ((forbid >> c) & 1ull)
+      {
+        ++c;
+      }
+      colour[e] = static_cast<unsigned char>(c);
+      ncol      = c + 1 > ncol ? c + 1 : ncol;
+      for (int k = ro[e]; k < ro[e + 1]; ++k)
+      {
+        used[key(false, rd[k])] |= 1ull << c;
+      }
+      for (int k = so[e]; k < so[e + 1]; ++k)
+      {
+        used[key(true, sd[k])] |= 1ull << c;
+      }
+    }
+    std::vector<int> off(ncol + 1, 0), elems(ne);
+    for (int e = 0; e < ne; ++e)
+    {
+      ++off[colour[e] + 1];
+    }
+    for (int c = 0; c < ncol; ++c)
+    {
+      off[c + 1] += off[c];
+    }
+    std::vector<int> next(off.begin(), off.end() - 1);
+    for (int e = 0; e < ne; ++e)
+    {
+      elems[next[colour[e]]++] = e;
+    }
+    int* d_off   = deviceAlloc<int>(ncol + 1);
+    int* d_elems = nullptr;
+    try
+    {
+      d_elems = deviceAlloc<int>(ne);
+      cudaCheck(cudaMemcpyAsync(d_off, off.data(), sizeof(int) * (ncol + 1),
+                                cudaMemcpyHostToDevice, s),
+                "colouring upload");
+      cudaCheck(cudaMemcpyAsync(d_elems, elems.data(), sizeof(int) * ne,
+                                cudaMemcpyHostToDevice, s),
+                "colouring upload");
+      cudaCheck(cudaStreamSynchronize(s), "colouring upload");
+    }
+    catch (...)
+    {
+      deviceFree(d_off);
+      deviceFree(d_elems);
+      throw;
+    }
+    m->num_colours     = ncol;
+    m->colour_off_host = std::move(off);
+    m->colour_off      = d_off;
+    m->colour_elems    = d_elems;
+  });
+}
+
+extern "C" int gbfem_assembly_map_num_colours(const gbfem_assembly_map* m)
+{
+  return m != nullptr ? m->num_colours : 0;
 }

@@ -33,14 +33,16 @@
 namespace
 {
 
+template <bool kPlain = false>
 __global__ void __launch_bounds__(128) thResidual64Kernel(ThArgs a)
 {
-  thResidual64Elem(a, blockIdx.x * blockDim.x + threadIdx.x);
+  thResidual64Elem<kPlain>(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+template <bool kPlain = false>
 __global__ void __launch_bounds__(128) thResidualDFKernel(ThArgs a)
 {
-  thResidualDFElem(a, blockIdx.x * blockDim.x + threadIdx.x);
+  thResidualDFElem<kPlain>(a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 // Plain FP64 Jacobian + residual, one thread per element. The same
@@ -57,6 +59,9 @@ __global__ void __launch_bounds__(128) thResidualDFKernel(ThArgs a)
 // before the row's values are computed and staged next to them).
 // Four resident blocks per SM (128 registers, a few spilled to L1) measured
 // faster than two without spills: more warps keep the FP64 pipe fed.
+// kPlain: a coloured pass (a.elems = the colour's elements, which share no
+// DOF): plain read-add-writes instead of FP64 reductions; needs pos_rows.
+template <bool kPlain = false>
 __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigned char* pos_rows)
 {
   __shared__ double buf[4][32][17];
@@ -64,8 +69,9 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
   __shared__ uint4  posb[4][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int e0   = blockIdx.x * 128 + warp * 32;
-  const int e    = e0 + lane;
-  bool      live = e < a.ne;
+  const int idx  = e0 + lane;
+  bool      live = idx < a.ne;
+  const int e    = (live && a.elems != nullptr) ? a.elems[idx] : idx;
   const ThRef<double>& R = kRefC;
 
   double aInvJ[4] = {0, 0, 0, 0}, G3[3] = {0, 0, 0};
@@ -167,7 +173,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     gbfem::awaitPrerequisites(); // the outputs' zero fill may still be running
     if (live)
     {
-      gbfem::redAdd(a.res + a.dofs[15 * e + l], r);
+      gbfem::addTo<kPlain>(a.res + a.dofs[15 * e + l], r);
     }
     if (jac)
     {
@@ -197,7 +203,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
         const int slot = pos_rows != nullptr
                              ? rs + reinterpret_cast<const unsigned char*>(&posb[warp][t])[j]
                              : a.jac_map[225LL * (e0 + t) + 15 * l + j];
-        gbfem::redAdd(a.vals + slot, buf[warp][t][j]);
+        gbfem::addTo<kPlain>(a.vals + slot, buf[warp][t][j]);
       }
     }
     __syncwarp();
@@ -298,7 +304,11 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
     require(res != state && vals != state && (vals == nullptr || res != vals),
             "Assembly state, residual, and matrix values must not alias");
     const bool det = (precision & GBFEM_DETERMINISTIC) != 0;
-    precision &= ~GBFEM_DETERMINISTIC;
+    const bool col = (precision & GBFEM_COLOURED) != 0;
+    precision &= ~(GBFEM_DETERMINISTIC | GBFEM_COLOURED);
+    require(!(det && col), "deterministic and coloured assembly are exclusive");
+    require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
+            "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
     require(!det || map->num_elems == 0 || map->gather_off != nullptr,
@@ -371,26 +381,86 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
       cudaCheck(cudaGetLastError(), "Taylor-Hood row pass launch");
       return;
     }
-    const unsigned eblocks = blocksFor(a.ne, 128);
+    // One element pass: every element in one launch (FP64 reductions), or,
+    // coloured, one launch per colour in colour order (plain adds; the
+    // colour's element list in a.elems). Only a pass's first launch may be a
+    // dependent of the zero fill.
+    auto pass = [&](auto&& launch, bool first_dep) {
+      if (!col)
+      {
+        launch(a, first_dep, false);
+        return;
+      }
+      for (int c = 0; c < map->num_colours; ++c)
+      {
+        ThArgs ac = a;
+        ac.elems  = map->colour_elems + map->colour_off_host[c];
+        ac.ne     = map->colour_off_host[c + 1] - map->colour_off_host[c];
+        if (ac.ne > 0)
+        {
+          launch(ac, first_dep && c == 0, true);
+        }
+      }
+    };
+    auto eb = [](const ThArgs& x) { return blocksFor(x.ne, 128); };
+    auto gb = [](const ThArgs& x) { return blocksFor(x.ne, kElemsPerBlock); };
+    auto res64 = [&](const ThArgs& x, bool d, bool plain) {
+      plain ? launchMaybeDependent(d, thResidual64Kernel<true>, eb(x), 128, s, x)
+            : launchMaybeDependent(d, thResidual64Kernel<false>, eb(x), 128, s, x);
+    };
+    auto resDF = [&](const ThArgs& x, bool d, bool plain) {
+      plain ? launchMaybeDependent(d, thResidualDFKernel<true>, eb(x), 128, s, x)
+            : launchMaybeDependent(d, thResidualDFKernel<false>, eb(x), 128, s, x);
+    };
     if (precision == GBFEM_PREC_FP64 && jac)
     {
-      launchMaybeDependent(dep, thElemKernel64, eblocks, 128, s, a, map->jac_pos_rows);
+      require(!col || map->jac_pos_rows != nullptr,
+              "coloured Taylor-Hood assembly needs the compact position map");
+      pass(
+          [&](const ThArgs& x, bool d, bool plain) {
+            plain ? launchMaybeDependent(d, thElemKernel64<true>, eb(x), 128, s, x,
+                                         map->jac_pos_rows)
+                  : launchMaybeDependent(d, thElemKernel64<false>, eb(x), 128, s, x,
+                                         map->jac_pos_rows);
+          },
+          dep);
     }
     else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
     {
       if (jac)
       {
-        launchMaybeDependent(dep, thKernelDd<true>, blocks, kThreads, s, a);
+        pass(
+            [&](const ThArgs& x, bool d, bool plain) {
+              plain ? launchMaybeDependent(d, thKernelColour<gbfem::Dd, true, true>, gb(x),
+                                           kThreads, s, x)
+                    : launchMaybeDependent(d, thKernelDd<true>, gb(x), kThreads, s, x);
+            },
+            dep);
       }
       else
       {
-        thResidualDFKernel<<<eblocks, 128, 0, s>>>(a);
+        pass(resDF, false);
       }
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
-      jac ? launchMaybeDependent(dep, thKernel<float, true, true>, blocks, kThreads, s, a)
-          : launchMaybeDependent(dep, thKernel<float, false, true>, blocks, kThreads, s, a);
+      pass(
+          [&](const ThArgs& x, bool d, bool plain) {
+            if (plain)
+            {
+              jac ? launchMaybeDependent(d, thKernelColour<float, true, true>, gb(x), kThreads,
+                                         s, x)
+                  : launchMaybeDependent(d, thKernelColour<float, false, true>, gb(x),
+                                         kThreads, s, x);
+            }
+            else
+            {
+              jac ? launchMaybeDependent(d, thKernel<float, true, true>, gb(x), kThreads, s, x)
+                  : launchMaybeDependent(d, thKernel<float, false, true>, gb(x), kThreads, s,
+                                         x);
+            }
+          },
+          dep);
     }
     else
     {
@@ -400,13 +470,20 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
         // side by side on two streams they overlapped by 1.5 % only: the
         // residual kernel's 128-register blocks and the Jacobian kernel's
         // 12 blocks per SM do not share SMs.)
-        launchMaybeDependent(dep, thKernel<float, true, false>, blocks, kThreads, s, a);
-        thResidualDFKernel<<<eblocks, 128, 0, s>>>(a);
+        pass(
+            [&](const ThArgs& x, bool d, bool plain) {
+              plain ? launchMaybeDependent(d, thKernelColour<float, true, false>, gb(x),
+                                           kThreads, s, x)
+                    : launchMaybeDependent(d, thKernel<float, true, false>, gb(x), kThreads, s,
+                                           x);
+            },
+            dep);
+        pass(resDF, false);
       }
       else
       {
         // residual-only calls of the FP64 and MIXED modes: FP64
-        thResidual64Kernel<<<eblocks, 128, 0, s>>>(a);
+        pass(res64, false);
       }
     }
     cudaCheck(cudaGetLastError(), "Taylor-Hood assembly launch");
@@ -447,8 +524,12 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
             "VJP inputs must not be null");
     require(g_state != nullptr, "VJP output is null");
     require(g_state != state && g_state != lam, "VJP output must not alias its inputs");
+    const bool col = (precision & GBFEM_COLOURED) != 0;
+    precision &= ~GBFEM_COLOURED;
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
+    require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
+            "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
     cudaStream_t s = asStream(stream);
@@ -471,19 +552,44 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
     a.lam       = lam;
     a.g_state   = g_state;
     a.status    = map->status;
-    const unsigned blocks = blocksFor(a.ne, kElemsPerBlock);
-    // MIXED keeps the Jacobian (and so J^T lam) in FP32 quadrature
-    if (precision == GBFEM_PREC_FP64)
+    // MIXED keeps the Jacobian (and so J^T lam) in FP32 quadrature; coloured:
+    // one launch per colour, plain adds into g_state
+    auto launch = [&](const ThArgs& x, bool d) {
+      const unsigned blocks = blocksFor(x.ne, kElemsPerBlock);
+      const bool     plain  = x.elems != nullptr;
+      if (precision == GBFEM_PREC_FP64)
+      {
+        plain ? launchMaybeDependent(d, thVjpKernelColour<double, false>, blocks, kThreads, s, x)
+              : launchMaybeDependent(d, thVjpKernel<double, false>, blocks, kThreads, s, x);
+      }
+      else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
+      {
+        plain ? launchMaybeDependent(d, thVjpKernelColour<gbfem::Dd, false>, blocks, kThreads,
+                                     s, x)
+              : launchMaybeDependent(d, thVjpKernel<gbfem::Dd, false>, blocks, kThreads, s, x);
+      }
+      else
+      {
+        plain ? launchMaybeDependent(d, thVjpKernelColour<float, false>, blocks, kThreads, s, x)
+              : launchMaybeDependent(d, thVjpKernel<float, false>, blocks, kThreads, s, x);
+      }
+    };
+    if (!col)
     {
-      launchDependent(thVjpKernel<double, false>, blocks, kThreads, s, a);
-    }
-    else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
-    {
-      launchDependent(thVjpKernel<gbfem::Dd, false>, blocks, kThreads, s, a);
+      launch(a, true);
     }
     else
     {
-      launchDependent(thVjpKernel<float, false>, blocks, kThreads, s, a);
+      for (int c = 0; c < map->num_colours; ++c)
+      {
+        ThArgs ac = a;
+        ac.elems  = map->colour_elems + map->colour_off_host[c];
+        ac.ne     = map->colour_off_host[c + 1] - map->colour_off_host[c];
+        if (ac.ne > 0)
+        {
+          launch(ac, c == 0);
+        }
+      }
     }
     cudaCheck(cudaGetLastError(), "Taylor-Hood VJP launch");
   });

@@ -254,6 +254,8 @@ struct ThArgs
   const int*           gslot;
   void*                geb;
   double*              gres;
+  // coloured pass: the colour's element list (ne = its length), or null
+  const int*           elems;
 };
 
 template <class T>
@@ -388,16 +390,21 @@ __device__ __forceinline__ void storeRecord(double* dst, const double (&v)[16])
 //   R_(a,c) = sum_q [ Ft_c(q) . dN^_a(q) + src_c(q) N^_a(q) ],
 //   Ft_c = J^-1 W (nu grad u_c - p e_c),  src_c = W u . grad u_c,
 //   R_p(b)  = -sum_q psi^_b(q) W div u(q).
-template <class T, bool kJac, bool kRes, bool kVjp, bool kRes64 = false, bool kGather = false>
+template <class T, bool kJac, bool kRes, bool kVjp, bool kRes64 = false, bool kGather = false,
+          bool kPlain = false>
 __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& sm)
 {
   static_assert(!(kRes && kRes64), "one residual precision at a time");
   static_assert(!(kGather && kVjp), "the fused VJP scatters its column sums");
+  static_assert(!(kGather && kPlain), "one output scheme at a time");
   const ThRef<T>& ref = sm.ref;
   const int       l   = threadIdx.x & (kLanes - 1);
   const int       le  = threadIdx.x / kLanes;
-  const int       e   = e_base + le;
-  const bool      has = e < a.ne;
+  // element slot e_base + le of this launch: an element index, or, in a
+  // coloured pass, an index into the colour's element list
+  const int       idx = e_base + le;
+  const bool      has = idx < a.ne;
+  const int       e   = (has && a.elems != nullptr) ? a.elems[idx] : idx;
   ElemShared<T>&  S   = sm.sh[le];
 
   Res64* R64 = nullptr;
@@ -765,11 +772,11 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     const int row_dof = a.dofs[15 * e + l];
     if (kRes)
     {
-      gbfem::redAdd(a.res + row_dof, gbfem::toF64(r));
+      gbfem::addTo<kPlain>(a.res + row_dof, gbfem::toF64(r));
     }
     if constexpr (kRes64)
     {
-      gbfem::redAdd(a.res + row_dof, rowRes64(*R64, l));
+      gbfem::addTo<kPlain>(a.res + row_dof, rowRes64(*R64, l));
     }
     if (kJac)
     {
@@ -831,7 +838,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
           {
             const int slot = a.jac_pos != nullptr ? sm.rs[le][row] + pos[row]
                                                   : a.jac_map[225LL * e + 15 * row + l];
-            gbfem::redAdd(a.vals + slot, gbfem::toF64Ftz(sm.outv[le][row][l]));
+            gbfem::addTo<kPlain>(a.vals + slot, gbfem::toF64Ftz(sm.outv[le][row][l]));
           }
         }
       }
@@ -847,7 +854,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
             acc += sm.outv[le][row][l] * sm.lam[le][row];
           }
         }
-        gbfem::redAdd(a.g_state + a.dofs[15 * e + l], gbfem::toF64(acc));
+        gbfem::addTo<kPlain>(a.g_state + a.dofs[15 * e + l], gbfem::toF64(acc));
       }
     }
   }
@@ -875,6 +882,26 @@ __global__ void __launch_bounds__(kThreads, 4) thKernelDd(ThArgs a)
   thStageRef(sm, a.status);
   __syncthreads();
   thBlock<gbfem::Dd, true, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+// Coloured passes (one launch per colour, a.elems = the colour's
+// elements): plain read-add-writes instead of FP64 reductions.
+template <class T, bool kJac, bool kRes>
+__global__ void __launch_bounds__(kThreads, sizeof(T) == 4 ? 12 : 4) thKernelColour(ThArgs a)
+{
+  __shared__ ThSmem<T> sm;
+  thStageRef(sm, a.status);
+  __syncthreads();
+  thBlock<T, kJac, kRes, false, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
+}
+
+template <class T, bool kRes>
+__global__ void __launch_bounds__(kThreads) thVjpKernelColour(ThArgs a)
+{
+  __shared__ ThSmem<T> sm;
+  thStageRef(sm, a.status);
+  __syncthreads();
+  thBlock<T, true, kRes, true, false, false, true>(a, blockIdx.x * kElemsPerBlock, sm);
 }
 
 // MIXED: FP32-quadrature Jacobian and FP64 residual in one pass.
@@ -974,13 +1001,14 @@ __device__ __forceinline__ double sToF64(gbfem::DF x)
   return gbfem::dfToF64(x);
 }
 
-template <class S>
-__device__ __forceinline__ void thResidualElem(const ThArgs& a, int e, const ThRef<S>& rd)
+template <class S, bool kPlain = false>
+__device__ __forceinline__ void thResidualElem(const ThArgs& a, int idx, const ThRef<S>& rd)
 {
-  if (e >= a.ne)
+  if (idx >= a.ne)
   {
     return;
   }
+  const int e = a.elems != nullptr ? a.elems[idx] : idx; // coloured: the colour's list
   int nodes[3];
   for (int k = 0; k < 6; ++k)
   {
@@ -1084,23 +1112,25 @@ __device__ __forceinline__ void thResidualElem(const ThArgs& a, int e, const ThR
 #pragma unroll
   for (int l = 0; l < 15; ++l)
   {
-    gbfem::redAdd(a.res + dofs[l], sToF64(r[l]));
+    gbfem::addTo<kPlain>(a.res + dofs[l], sToF64(r[l]));
   }
 }
 
 // Reference tables in constant memory (warp-uniform operands).
 __constant__ ThRef<gbfem::DF> kRefDF = castRef<gbfem::DF>();
 
+template <bool kPlain = false>
 __device__ __forceinline__ void thResidual64Elem(const ThArgs& a, int e)
 {
-  thResidualElem<double>(a, e, kRefC);
+  thResidualElem<double, kPlain>(a, e, kRefC);
 }
 
 // MIXED residual: double-float arithmetic (~44 significant bits) on the
 // FP32 pipe; error against the FP64 residual ~1e-14 relative.
+template <bool kPlain = false>
 __device__ __forceinline__ void thResidualDFElem(const ThArgs& a, int e)
 {
-  thResidualElem<gbfem::DF>(a, e, kRefDF);
+  thResidualElem<gbfem::DF, kPlain>(a, e, kRefDF);
 }
 
 // Row-gather variants: the element pass writes records, no atomics.

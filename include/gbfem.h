@@ -57,6 +57,11 @@ extern "C" {
  * bit, like femx's serial CPU loop. Needs gbfem_assembly_map_enable_gather
  * on the map first. */
 #define GBFEM_DETERMINISTIC 0x100
+/* OR-ed into a precision argument (P1, Taylor-Hood, their VJPs, the batch):
+ * coloured assembly — elements run colour by colour with plain
+ * read-add-writes, no atomics (gbfem_assembly_map_enable_colouring first);
+ * bitwise reproducible like GBFEM_DETERMINISTIC, for any layout. */
+#define GBFEM_COLOURED 0x200
 
 GBFEM_API const char* gbfem_last_error(void);
 GBFEM_API int         gbfem_version(void);
@@ -102,6 +107,18 @@ GBFEM_API int  gbfem_assembly_map_check(const gbfem_assembly_map* map, void* str
  * the same map. No counterpart in the reference, whose CPU loop is serial
  * and deterministic by construction (Assembly.hpp:186-223). */
 GBFEM_API int  gbfem_assembly_map_enable_gather(gbfem_assembly_map* map, void* stream);
+/* Colours the map's elements so that no two elements of one colour share a
+ * residual or state DOF (greedy, elements in ascending order, at most 64
+ * colours; setup: reads the DOF tables back, allocates, synchronizes
+ * `stream`; later calls return at once). With GBFEM_COLOURED the element
+ * kernels then run colour by colour and add with plain read-add-writes
+ * instead of FP64 atomics: a fixed summation order, bitwise reproducible
+ * results, for any element layout. No counterpart in the reference, whose
+ * OpenMP NS assembly uses atomics (NavierStokesModel.cpp:227-318) and whose
+ * CUDA assembly FP64 atomics (CudaAssembly.hpp:160-168).
+ * gbfem_assembly_map_num_colours: 0 before colouring. */
+GBFEM_API int  gbfem_assembly_map_enable_colouring(gbfem_assembly_map* map, void* stream);
+GBFEM_API int  gbfem_assembly_map_num_colours(const gbfem_assembly_map* map);
 
 /* ---------------------------------------------------------------------------
  * BoundaryMap — replaces femx::assembly::makeBoundaryMap(dofs, pattern)
@@ -392,13 +409,18 @@ GBFEM_API int       gbfem_batch_create(int num_instances,
                                        void* stream, gbfem_batch** out);
 /* precision: GBFEM_PREC_FP64, GBFEM_PREC_FP32_QUAD or GBFEM_PREC_MIXED
  * (Jacobian from FP32 quadrature; residual and P1 gradients in FP64; the
- * Taylor-Hood J^T lam uses the FP32 Jacobian). Work items are
- * p1_chunk P1 elements (multiple of 128) or th_chunk Taylor-Hood elements
- * (multiple of 8); the grid is blocks_per_sm x SM count. */
+ * Taylor-Hood J^T lam uses the FP32 Jacobian), optionally OR-ed with
+ * GBFEM_COLOURED (FP64 and FP32_QUAD): every instance's map coloured before
+ * gbfem_batch_create, the persistent kernel then runs once per colour round
+ * (colour r of every instance) with plain adds, bitwise reproducible. Work
+ * items are p1_chunk P1 elements (multiple of 128) or th_chunk Taylor-Hood
+ * elements (multiple of 8); the grid is blocks_per_sm x SM count.
+ * stage_depth 1: a block claims its next work item while running the current
+ * one and prefetches that item's DOF table, connectivity and coefficients
+ * into L2 (0: claims one at a time). */
 GBFEM_API int       gbfem_batch_run(gbfem_batch* batch, int precision, int p1_chunk,
-                                    int th_chunk, int blocks_per_sm, void* stream);
-/* Reads and clears the batch's device status word (degenerate elements,
- * out-of-range connectivity). Synchronizes `stream`. */
+                                    int th_chunk, int blocks_per_sm, int stage_depth,
+                                    void* stream);
 GBFEM_API int       gbfem_batch_check(const gbfem_batch* batch, void* stream);
 GBFEM_API long long gbfem_batch_num_elems(const gbfem_batch* batch);
 GBFEM_API void      gbfem_batch_destroy(gbfem_batch* batch);

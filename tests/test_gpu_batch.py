@@ -28,7 +28,7 @@ def dev(a, dtype=None):
     return (t if dtype is None else t.to(dtype)).cuda()
 
 
-def make_batch(seed=0):
+def make_batch(seed=0, coloured=False):
     rng = np.random.default_rng(seed)
     insts, refs = [], []
     for k, nx in enumerate((9, 31, 17, 40)):
@@ -51,7 +51,7 @@ def make_batch(seed=0):
         lam = rng.standard_normal(nd)
         insts.append(THInstance(amap, dev(cp2), dev(conn6), 1.0 / re, dev(state), dev(lam)))
         refs.append(("th", cp2, conn6, 1.0 / re, state, lam, offs, dofs, nd))
-    return Batch(insts), insts, refs
+    return Batch(insts, coloured=coloured), insts, refs
 
 
 def check_against_oracle(insts, refs, tol_j, tol_r, tol_g, tol_g_th=None):
@@ -92,7 +92,9 @@ def test_batch_matches_oracle(precision, tj, tr, tg, tgt):
 
 
 @pytest.mark.parametrize("params", [dict(p1_chunk=128, th_chunk=8, blocks_per_sm=1),
-                                    dict(p1_chunk=2048, th_chunk=64, blocks_per_sm=16)])
+                                    dict(p1_chunk=2048, th_chunk=64, blocks_per_sm=16),
+                                    dict(p1_chunk=256, th_chunk=16, blocks_per_sm=4,
+                                         stage_depth=1)])
 def test_batch_independent_of_launch_parameters(params):
     batch, insts, refs = make_batch(seed=3)
     batch.run("fp64", **params)
@@ -113,11 +115,40 @@ def test_batch_cuda_graph_replay():
     check_against_oracle(insts, refs, 1e-12, 1e-12, 1e-12)
 
 
+@pytest.mark.parametrize("precision,tj,tr,tg,tgt", [
+    ("fp64", 1e-12, 1e-12, 1e-12, 1e-12),
+    ("fp32_quad", 1e-6, 1e-6, 1e-6, 1e-6)])
+def test_coloured_batch_matches_oracle_and_is_bitwise_reproducible(precision, tj, tr, tg, tgt):
+    """The colouring scatter scheme: colour rounds with plain adds, no
+    atomics; two runs agree bit for bit, with and without staging."""
+    batch, insts, refs = make_batch(seed=9, coloured=True)
+    assert all(x.amap.numColours() >= 3 for x in insts)
+    outs = []
+    for stage in (0, 1, 0):
+        batch.run(precision, scatter="colour", stage_depth=stage, p1_chunk=256, th_chunk=16)
+        batch.check()
+        torch.cuda.synchronize()
+        outs.append([(x.res.clone(), x.vals.clone(), x.g_u.clone()) for x in insts])
+    check_against_oracle(insts, refs, tj, tr, tg, tgt)
+    for run in outs[1:]:
+        for a, b in zip(run, outs[0]):
+            assert all(torch.equal(p, q) for p, q in zip(a, b))
+
+
+def test_coloured_batch_needs_coloured_maps():
+    batch, insts, refs = make_batch(seed=2)
+    with pytest.raises(A.GbfemError, match="colouring"):
+        batch.run("fp64", scatter="colour")
+
+
 def test_autotune_returns_valid_params(tmp_path, monkeypatch):
     monkeypatch.setenv("GBFEM_TUNE_CACHE", str(tmp_path / "tune.json"))
-    batch, insts, refs = make_batch(seed=7)
+    batch, insts, refs = make_batch(seed=7, coloured=True)
     params, timings = autotune(batch, "fp32_quad", reps=1)
-    assert set(params) == {"p1_chunk", "th_chunk", "blocks_per_sm"}
+    assert set(params) == {"p1_chunk", "th_chunk", "blocks_per_sm", "stage_depth", "scatter"}
+    assert params["scatter"] in ("atomic", "colour") and params["stage_depth"] in (0, 1)
+    det, _ = autotune(batch, "fp64", reps=1, deterministic=True)
+    assert det["scatter"] == "colour"
     again, info = autotune(batch, "fp32_quad")
     assert again == params and info == {"cached": True}
     batch.run("fp64", **params)

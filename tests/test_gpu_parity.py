@@ -583,3 +583,89 @@ def test_taylor_hood_connectivity_out_of_range_is_reported(precision):
     tol = TOL64 if precision == "fp64" else TOL32
     assert rel_inf(host(res), rres) <= tol
     assert rel_inf(host(jac.vals), rvals) <= tol
+
+
+# ------------------------------------------------ coloured (atomic-free) assembly
+
+@pytest.mark.parametrize("precision,tol", [("fp64", TOL64), ("fp32_quad", TOL32),
+                                           ("mixed", TOL32)])
+def test_p1_coloured_assembly_matches_oracle_and_repeats_bitwise(precision, tol):
+    """Coloured assembly: no two elements of a colour share a DOF, colours run
+    one after another with plain adds; residual, Jacobian and both VJPs
+    against the oracle, and bitwise equal over repeated calls."""
+    coords, conn = meshes.jittered_tri(30, seed=31)
+    m, om = p1_setup(coords, conn)
+    nc = m.enableColouring()
+    assert 3 <= nc <= 16
+    n, e = coords.shape[0], conn.shape[0]
+    rng = np.random.default_rng(31)
+    kappa, u, lam = np.exp(rng.standard_normal(e)), rng.standard_normal(n), rng.standard_normal(n)
+    f = meshes.fourier_source(coords, 2)
+    q = orc.P1Quad(coords, conn)
+    rres, rvals = orc.assemble_p1_kappa(om, q, kappa, f, u)
+    rgu, rgm = orc.vjp_p1_kappa(om, q, kappa, u, lam)
+    outs = []
+    for _ in range(2):
+        res = torch.full((n,), 5.0, dtype=torch.float64, device="cuda")
+        jac = A.CsrMatrix(m.pattern(), torch.full((m.pattern().nnz,), 2.0, dtype=torch.float64,
+                                                  device="cuda"))
+        A.assembleP1Kappa(m, dev(coords), dev(kappa), dev(f), dev(u), res, jac,
+                          precision=precision, coloured=True)
+        g_u = torch.zeros(n, dtype=torch.float64, device="cuda")
+        g_m = torch.zeros(e, dtype=torch.float64, device="cuda")
+        A.vjpP1Kappa(m, dev(coords), dev(kappa), dev(u), dev(lam), g_u, g_m,
+                     precision=precision, coloured=True)
+        m.check()
+        outs.append((res, jac.vals, g_u, g_m))
+    res, vals, g_u, g_m = (host(t) for t in outs[0])
+    assert rel_inf(vals, rvals) <= tol
+    assert rel_inf(res, rres) <= (TOL64 if precision == "mixed" else tol)
+    assert rel_inf(g_u, rgu) <= (TOL64 if precision != "fp32_quad" else TOL32)
+    assert rel_inf(g_m, rgm) <= (TOL64 if precision != "fp32_quad" else TOL32)
+    assert all(torch.equal(a, b) for a, b in zip(outs[0], outs[1]))
+
+
+@pytest.mark.parametrize("precision,tol_j,tol_r", TH_PRECS)
+def test_taylor_hood_coloured_assembly_matches_oracle_and_repeats_bitwise(precision, tol_j,
+                                                                           tol_r):
+    c3, k3 = meshes.jittered_tri(14, seed=41)
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    state = meshes.cavity_state(cp2, nv, seed=41)
+    lam = np.random.default_rng(41).standard_normal(nd)
+    m = gpu_map(nd, nd, offs, dofs, offs, dofs)
+    assert m.enableColouring() >= 3
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-2, state)
+    gref = orc.matvec_t(om.row_ptr, om.col_ind, rvals, lam, nd)
+    outs = []
+    for _ in range(2):
+        res = torch.full((nd,), 5.0, dtype=torch.float64, device="cuda")
+        jac = A.CsrMatrix(m.pattern(), torch.full((m.pattern().nnz,), 2.0, dtype=torch.float64,
+                                                  device="cuda"))
+        A.assembleTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), res, jac,
+                             precision=precision, coloured=True)
+        r_only = torch.full((nd,), 3.0, dtype=torch.float64, device="cuda")
+        A.assembleTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), r_only,
+                             None, precision=precision, coloured=True)
+        g = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        A.vjpTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), dev(lam), g,
+                        precision=precision, coloured=True)
+        m.check()
+        outs.append((res, jac.vals, r_only, g))
+    res, vals, r_only, g = (host(t) for t in outs[0])
+    assert rel_inf(vals, rvals) <= tol_j
+    assert rel_inf(res, rres) <= tol_r
+    assert rel_inf(r_only, rres) <= (TOL32 if precision == "fp32_quad" else TOL64)
+    assert rel_inf(g, gref) <= (TOL64 if precision in ("fp64", "double_float") else TOL32)
+    assert all(torch.equal(a, b) for a, b in zip(outs[0], outs[1]))
+
+
+def test_coloured_assembly_needs_a_coloured_map():
+    coords, conn = meshes.jittered_tri(6, seed=3)
+    m, om = p1_setup(coords, conn)
+    n, e = coords.shape[0], conn.shape[0]
+    res = torch.zeros(n, dtype=torch.float64, device="cuda")
+    with pytest.raises(A.GbfemError, match="enable_colouring"):
+        A.assembleP1Kappa(m, dev(coords), dev(np.ones(e)), None, dev(np.zeros(n)), res,
+                          coloured=True)
