@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
 #pragma unroll
       for (int q = 0; q < kNq; ++q)
       {
-        d += kConvW.w[q][sa][b][0] * ut[q][0] + kConvW.w[q][sa][b][1] * ut[q][1];
+        d += R.wN[q][sa] * (R.dNr[q][b][0] * ut[q][0] + R.dNr[q][b][1] * ut[q][1]);
       }
       da[b] = d;
     }

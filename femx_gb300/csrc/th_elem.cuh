@@ -232,6 +232,44 @@ __device__ __forceinline__ gbfem::Dd laneShfl<gbfem::Dd>(gbfem::Dd v, int src)
           __shfl_sync(0xffffffffu, v.lo, src, kLanes)};
 }
 
+// acc + x y: a fused multiply-add in float and double; in double-float the
+// Dot2 accumulation of Ogita, Rump and Oishi (the product's leading part
+// added by TwoSum, its rounding error and the cross terms collected in the
+// trailing part, left unnormalised until accNorm).
+__device__ __forceinline__ float mac(float acc, float x, float y)
+{
+  return acc + x * y;
+}
+__device__ __forceinline__ double mac(double acc, double x, double y)
+{
+  return acc + x * y;
+}
+__device__ __forceinline__ gbfem::Dd mac(gbfem::Dd acc, gbfem::Dd x, gbfem::Dd y)
+{
+  const float p  = __fmul_rn(x.hi, y.hi);
+  const float pe = __fmaf_rn(x.hi, y.hi, -p);
+  const float s  = __fadd_rn(acc.hi, p);
+  const float bb = __fsub_rn(s, acc.hi);
+  const float se = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  float       lo = __fadd_rn(acc.lo, __fadd_rn(se, pe));
+  lo             = __fmaf_rn(x.hi, y.lo, lo);
+  lo             = __fmaf_rn(x.lo, y.hi, lo);
+  return {s, lo};
+}
+__device__ __forceinline__ float accNorm(float x)
+{
+  return x;
+}
+__device__ __forceinline__ double accNorm(double x)
+{
+  return x;
+}
+__device__ __forceinline__ gbfem::Dd accNorm(gbfem::Dd x)
+{
+  const gbfem::DF t = gbfem::dfTwoSum(x.hi, x.lo);
+  return {t.hi, t.lo};
+}
+
 struct ThArgs
 {
   int                  ne;
@@ -670,15 +708,19 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
       }
       else
       {
-        da = S.G3[0] * ref.S00[sa][b] + S.G3[1] * ref.S11[sa][b] + S.G3[2] * ref.S01[sa][b];
+        da = S.G3[0] * ref.S00[sa][b];
+        da = mac(da, S.G3[1], ref.S11[sa][b]);
+        da = mac(da, S.G3[2], ref.S01[sa][b]);
 #pragma unroll
         for (int q = 0; q < kNq; ++q)
         {
-          da += ref.wN[q][sa] * S.vq[q][b];
+          da = mac(da, ref.wN[q][sa], S.vq[q][b]);
         }
+        da = accNorm(da);
       }
-      const T m0 = ref.T[0][sa][b] * G0[0] + ref.T[1][sa][b] * G0[1] + ref.T[2][sa][b] * G0[2];
-      const T m1 = ref.T[0][sa][b] * G1[0] + ref.T[1][sa][b] * G1[1] + ref.T[2][sa][b] * G1[2];
+      T m0 = ref.T[0][sa][b] * G0[0], m1 = ref.T[0][sa][b] * G1[0];
+      m0   = accNorm(mac(mac(m0, ref.T[1][sa][b], G0[1]), ref.T[2][sa][b], G0[2]));
+      m1   = accNorm(mac(mac(m1, ref.T[1][sa][b], G1[1]), ref.T[2][sa][b], G1[2]));
       if constexpr (kCompOrder)
       {
         je[b] = da * w0 + m0;
@@ -689,15 +731,16 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
         je[b] = da + m0;
         jo[b] = m1;
       }
-      r += da * S.st[2 * b + c];
+      r = mac(r, da, S.st[2 * b + c]);
     }
     const T ic0 = S.aInvJ[0 * 2 + c], ic1 = S.aInvJ[1 * 2 + c];
 #pragma unroll
     for (int b = 0; b < 3; ++b)
     {
-      jp[b] = -(ic0 * ref.C[0][sa][b] + ic1 * ref.C[1][sa][b]);
-      r += jp[b] * S.st[12 + b];
+      jp[b] = -accNorm(mac(ic0 * ref.C[0][sa][b], ic1, ref.C[1][sa][b]));
+      r     = mac(r, jp[b], S.st[12 + b]);
     }
+    r = accNorm(r);
   }
   else if (row_lane)
   {
@@ -706,10 +749,11 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     for (int sa = 0; sa < 6; ++sa)
     {
       const T c0 = ref.C[0][sa][b], c1 = ref.C[1][sa][b];
-      je[sa]     = -(S.aInvJ[0] * c0 + S.aInvJ[2] * c1);
-      jo[sa]     = -(S.aInvJ[1] * c0 + S.aInvJ[3] * c1);
-      r += je[sa] * S.st[2 * sa] + jo[sa] * S.st[2 * sa + 1];
+      je[sa]     = -accNorm(mac(S.aInvJ[0] * c0, S.aInvJ[2], c1));
+      jo[sa]     = -accNorm(mac(S.aInvJ[1] * c0, S.aInvJ[3], c1));
+      r          = mac(mac(r, je[sa], S.st[2 * sa]), jo[sa], S.st[2 * sa + 1]);
     }
+    r = accNorm(r);
   }
   if constexpr (kGather)
   {
@@ -876,7 +920,7 @@ __global__ void __launch_bounds__(kThreads, 12) thKernel(ThArgs a)
 // FP64-accurate Jacobian (and residual) in double-float arithmetic on the
 // FP32 pipe, the 16-lane layout of the FP32 kernel.
 template <bool kRes>
-__global__ void __launch_bounds__(kThreads, 4) thKernelDd(ThArgs a)
+__global__ void __launch_bounds__(kThreads, 6) thKernelDd(ThArgs a)
 {
   __shared__ ThSmem<gbfem::Dd> sm;
   thStageRef(sm, a.status);
@@ -927,32 +971,6 @@ __global__ void __launch_bounds__(kThreads) thVjpKernel(ThArgs a)
 // Reference tables in constant memory: the thread-per-element kernel below
 // reads every entry with the same address across the warp (broadcast).
 __constant__ ThRef<double> kRefC = makeRef();
-
-// Convection weights W[q][a][b][k] = w_q N^_a(q) dN^_b,k(q): the convection
-// block is A_ab = sum_q sum_k W[q][a][b][k] ut_k(q), two FMAs per point
-// instead of three.
-struct ConvW
-{
-  double w[kNq][6][6][2];
-};
-constexpr ConvW makeConvW()
-{
-  const ThRef<double> t = makeRef();
-  ConvW               c{};
-  for (int q = 0; q < kNq; ++q)
-  {
-    for (int a = 0; a < 6; ++a)
-    {
-      for (int b = 0; b < 6; ++b)
-      {
-        c.w[q][a][b][0] = t.wN[q][a] * t.dNr[q][b][0];
-        c.w[q][a][b][1] = t.wN[q][a] * t.dNr[q][b][1];
-      }
-    }
-  }
-  return c;
-}
-__constant__ ConvW kConvW = makeConvW();
 
 // FP64 residual, one thread per element, by direct quadrature:
 //   R_(a,c) = sum_q [Ft_c(q) . dN^_a(q) + src_c(q) N^_a(q)],
