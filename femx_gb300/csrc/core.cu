@@ -213,8 +213,12 @@ __device__ void zeroRange(double* p, long long n, long long tid, long long nt)
       p[n - 1] = 0.0;
     }
   }
-  double2* q = reinterpret_cast<double2*>(p + head);
-  for (long long i = tid; i < m / 2; i += nt)
+  // Descending: the grid's last writes are the lowest addresses, where the
+  // dependent element kernel, walking its elements in order, adds first;
+  // those lines are then still in L2 when its reductions reach them.
+  double2*        q  = reinterpret_cast<double2*>(p + head);
+  const long long np = m / 2;
+  for (long long i = np - 1 - tid; i >= 0; i -= nt)
   {
     q[i] = make_double2(0.0, 0.0);
   }
@@ -226,8 +230,8 @@ __global__ void __launch_bounds__(256) zeroForNextKernel(double* a, long long na
   asm volatile("griddepcontrol.launch_dependents;");
   const long long tid = static_cast<long long>(blockIdx.x) * blockDim.x + threadIdx.x;
   const long long nt  = static_cast<long long>(gridDim.x) * blockDim.x;
+  zeroRange(b, nb, tid, nt); // the (small) residual first, the matrix values last
   zeroRange(a, na, tid, nt);
-  zeroRange(b, nb, tid, nt);
 }
 
 int smCount()

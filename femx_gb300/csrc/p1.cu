@@ -17,7 +17,7 @@
 namespace
 {
 
-template <bool kF32, bool kSepConn, bool kLoad, bool kJac, bool kRes = true>
+template <int kF32, bool kSepConn, bool kLoad, bool kJac, bool kRes = true>
 __global__ void __launch_bounds__(256) p1AssembleKernel(P1Args a)
 {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(256) p1AssembleKernel(P1Args a)
   }
 }
 
-template <bool kF32, bool kSepConn>
+template <int kF32, bool kSepConn>
 __global__ void __launch_bounds__(256) p1VjpKernel(P1Args a)
 {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(256) p1VjpKernel(P1Args a)
 
 // Coloured element pass: thread i takes element elems[i] of one colour and
 // adds with plain read-add-writes (no element of the colour shares a DOF).
-template <bool kF32, bool kSep, bool kLoad, bool kJac, bool kRes, bool kVjp>
+template <int kF32, bool kSep, bool kLoad, bool kJac, bool kRes, bool kVjp>
 __global__ void __launch_bounds__(256)
     p1ColourKernel(P1Args a, const int* __restrict__ elems, int n)
 {
@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256)
 // coloured, one launch per colour in colour order. dep: the (first) launch
 // is a dependent of the zero fill before it and overlaps it up to its first
 // addition; later colours wait for the whole colour before them.
-template <bool kF32, bool kSep, bool kLoad, bool kJac, bool kRes, bool kVjp>
+template <int kF32, bool kSep, bool kLoad, bool kJac, bool kRes, bool kVjp>
 void p1Pass(const P1Args& a, const gbfem_assembly_map* map, bool coloured, bool dep,
             cudaStream_t s)
 {
@@ -85,7 +85,7 @@ void p1Pass(const P1Args& a, const gbfem_assembly_map* map, bool coloured, bool 
   }
 }
 
-template <bool kF32, bool kSep>
+template <int kF32, bool kSep>
 void launchAssemble(const P1Args& a, const gbfem_assembly_map* map, bool coloured, bool load,
                     bool jac, bool dep, cudaStream_t s)
 {
@@ -156,7 +156,7 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
             "Assembly state, residual, and matrix values must not alias");
     const bool col = (precision & GBFEM_COLOURED) != 0;
     precision &= ~GBFEM_COLOURED;
-    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
     require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
             "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");
@@ -175,8 +175,13 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     const bool sep  = conn != nullptr;
     if (precision == GBFEM_PREC_FP64 || (precision == GBFEM_PREC_MIXED && !jac))
     {
-      sep ? launchAssemble<false, true>(a, map, col, load, jac, true, s)
-          : launchAssemble<false, false>(a, map, col, load, jac, true, s);
+      sep ? launchAssemble<0, true>(a, map, col, load, jac, true, s)
+          : launchAssemble<0, false>(a, map, col, load, jac, true, s);
+    }
+    else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
+    {
+      sep ? launchAssemble<2, true>(a, map, col, load, jac, true, s)
+          : launchAssemble<2, false>(a, map, col, load, jac, true, s);
     }
     else if (precision == GBFEM_PREC_FP32_QUAD)
     {
@@ -209,7 +214,7 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
             "VJP outputs must not alias inputs");
     const bool col = (precision & GBFEM_COLOURED) != 0;
     precision &= ~GBFEM_COLOURED;
-    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_MIXED,
+    require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
     require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
             "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");

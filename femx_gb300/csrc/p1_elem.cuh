@@ -5,6 +5,7 @@
 
 #include <type_traits>
 
+#include "dfloat.cuh"
 #include "maps.cuh"
 
 namespace
@@ -78,11 +79,17 @@ __device__ __forceinline__ bool elementK(double2 x0, double2 x1, double2 x2,
 // residual VJPs (kVjp: K^T lam into g_u, lam^T K u into g_m), all from one
 // evaluation of the element stiffness. kPlain: coloured assembly, plain
 // read-add-writes instead of FP64 reductions.
-template <bool kF32, bool kSepConn, bool kLoad, bool kJac, bool kRes, bool kVjp,
+// kArith: the element arithmetic, 0 = FP64, 1 = FP32 (quadrature),
+// 2 = double-float (FP64-accurate, on the FP32 pipe; residual and Jacobian
+// only).
+template <int kArith, bool kSepConn, bool kLoad, bool kJac, bool kRes, bool kVjp,
           bool kPlain = false>
 __device__ __forceinline__ void p1Element(const P1Args& a, int e)
 {
-  using T = typename std::conditional<kF32, float, double>::type;
+  static_assert(kArith != 2 || !kVjp, "the double-float P1 element has no VJP");
+  constexpr bool kF32 = kArith == 1;
+  using T = typename std::conditional<
+      kArith == 2, gbfem::Dd, typename std::conditional<kF32, float, double>::type>::type;
   const int d0 = a.dofs[3 * e + 0], d1 = a.dofs[3 * e + 1], d2 = a.dofs[3 * e + 2];
   int       n0 = d0, n1 = d1, n2 = d2;
   if (kSepConn)
@@ -175,7 +182,7 @@ __device__ __forceinline__ void p1Element(const P1Args& a, int e)
       }
     }
   }
-  if (kVjp)
+  if constexpr (kVjp)
   {
     gbfem::awaitPrerequisites(); // g_u's zero fill may still be running
     if constexpr (kF32)

@@ -442,7 +442,7 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
   // coloured pass, an index into the colour's element list
   const int       idx = e_base + le;
   const bool      has = idx < a.ne;
-  const int       e   = (has && a.elems != nullptr) ? a.elems[idx] : idx;
+  const int       e   = (kPlain && has) ? a.elems[idx] : idx;
   ElemShared<T>&  S   = sm.sh[le];
 
   Res64* R64 = nullptr;
@@ -698,47 +698,71 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     const T   G0[3] = {S.Gv[0][c * 2 + k0], S.Gv[1][c * 2 + k0], S.Gv[2][c * 2 + k0]};
     const T   G1[3] = {S.Gv[0][c * 2 + k1], S.Gv[1][c * 2 + k1], S.Gv[2][c * 2 + k1]};
     const T   w0    = c == 0 ? T(1) : T(0), w1 = T(1) - w0;
-#pragma unroll
-    for (int b = 0; b < 6; ++b)
+    if constexpr (kCompOrder)
     {
-      T da;
-      if constexpr (kCompOrder)
-      {
-        da = (b & 1) == c ? dsh[b >> 1] : dpt[b >> 1];
-      }
-      else
-      {
-        da = S.G3[0] * ref.S00[sa][b];
-        da = mac(da, S.G3[1], ref.S11[sa][b]);
-        da = mac(da, S.G3[2], ref.S01[sa][b]);
 #pragma unroll
-        for (int q = 0; q < kNq; ++q)
+      for (int b = 0; b < 6; ++b)
+      {
+        const T da = (b & 1) == c ? dsh[b >> 1] : dpt[b >> 1];
+        const T m0 = ref.T[0][sa][b] * G0[0] + ref.T[1][sa][b] * G0[1]
+                     + ref.T[2][sa][b] * G0[2];
+        const T m1 = ref.T[0][sa][b] * G1[0] + ref.T[1][sa][b] * G1[1]
+                     + ref.T[2][sa][b] * G1[2];
+        je[b]      = da * w0 + m0;
+        jo[b]      = da * w1 + m1;
+        r += da * S.st[2 * b + c];
+      }
+    }
+    else
+    {
+      // the scalar block da[b] = diffusion + convection of the six columns,
+      // accumulated column-interleaved (six independent chains)
+      T da[6];
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
+      {
+        da[b] = S.G3[0] * ref.S00[sa][b];
+      }
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
+      {
+        da[b] = mac(mac(da[b], S.G3[1], ref.S11[sa][b]), S.G3[2], ref.S01[sa][b]);
+      }
+#pragma unroll
+      for (int q = 0; q < kNq; ++q)
+      {
+#pragma unroll
+        for (int b = 0; b < 6; ++b)
         {
-          da = mac(da, ref.wN[q][sa], S.vq[q][b]);
+          da[b] = mac(da[b], ref.wN[q][sa], S.vq[q][b]);
         }
-        da = accNorm(da);
       }
-      T m0 = ref.T[0][sa][b] * G0[0], m1 = ref.T[0][sa][b] * G1[0];
-      m0   = accNorm(mac(mac(m0, ref.T[1][sa][b], G0[1]), ref.T[2][sa][b], G0[2]));
-      m1   = accNorm(mac(mac(m1, ref.T[1][sa][b], G1[1]), ref.T[2][sa][b], G1[2]));
-      if constexpr (kCompOrder)
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
       {
-        je[b] = da * w0 + m0;
-        jo[b] = da * w1 + m1;
+        da[b]    = accNorm(da[b]);
+        T m0     = ref.T[0][sa][b] * G0[0], m1 = ref.T[0][sa][b] * G1[0];
+        m0       = accNorm(mac(mac(m0, ref.T[1][sa][b], G0[1]), ref.T[2][sa][b], G0[2]));
+        m1       = accNorm(mac(mac(m1, ref.T[1][sa][b], G1[1]), ref.T[2][sa][b], G1[2]));
+        je[b]    = da[b] + m0;
+        jo[b]    = m1;
+        r        = mac(r, da[b], S.st[2 * b + c]);
       }
-      else
-      {
-        je[b] = da + m0;
-        jo[b] = m1;
-      }
-      r = mac(r, da, S.st[2 * b + c]);
     }
     const T ic0 = S.aInvJ[0 * 2 + c], ic1 = S.aInvJ[1 * 2 + c];
 #pragma unroll
     for (int b = 0; b < 3; ++b)
     {
-      jp[b] = -accNorm(mac(ic0 * ref.C[0][sa][b], ic1, ref.C[1][sa][b]));
-      r     = mac(r, jp[b], S.st[12 + b]);
+      if constexpr (kCompOrder)
+      {
+        jp[b] = -(ic0 * ref.C[0][sa][b] + ic1 * ref.C[1][sa][b]);
+        r += jp[b] * S.st[12 + b];
+      }
+      else
+      {
+        jp[b] = -accNorm(mac(ic0 * ref.C[0][sa][b], ic1, ref.C[1][sa][b]));
+        r     = mac(r, jp[b], S.st[12 + b]);
+      }
     }
     r = accNorm(r);
   }
@@ -749,9 +773,18 @@ __device__ __forceinline__ void thBlock(const ThArgs& a, int e_base, ThSmem<T>& 
     for (int sa = 0; sa < 6; ++sa)
     {
       const T c0 = ref.C[0][sa][b], c1 = ref.C[1][sa][b];
-      je[sa]     = -accNorm(mac(S.aInvJ[0] * c0, S.aInvJ[2], c1));
-      jo[sa]     = -accNorm(mac(S.aInvJ[1] * c0, S.aInvJ[3], c1));
-      r          = mac(mac(r, je[sa], S.st[2 * sa]), jo[sa], S.st[2 * sa + 1]);
+      if constexpr (kCompOrder)
+      {
+        je[sa] = -(S.aInvJ[0] * c0 + S.aInvJ[2] * c1);
+        jo[sa] = -(S.aInvJ[1] * c0 + S.aInvJ[3] * c1);
+        r += je[sa] * S.st[2 * sa] + jo[sa] * S.st[2 * sa + 1];
+      }
+      else
+      {
+        je[sa] = -accNorm(mac(S.aInvJ[0] * c0, S.aInvJ[2], c1));
+        jo[sa] = -accNorm(mac(S.aInvJ[1] * c0, S.aInvJ[3], c1));
+        r      = mac(mac(r, je[sa], S.st[2 * sa]), jo[sa], S.st[2 * sa + 1]);
+      }
     }
     r = accNorm(r);
   }

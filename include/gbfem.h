@@ -44,12 +44,13 @@ extern "C" {
 #define GBFEM_PREC_FP64 0
 #define GBFEM_PREC_FP32_QUAD 1
 #define GBFEM_PREC_MIXED 2
-/* DOUBLE_FLOAT (Taylor-Hood): the element arithmetic of the Jacobian and
- * residual in double-float (each value a pair of floats, about 48
- * significant bits) on the FP32 pipe, which GB300 issues about 64x faster
- * than FP64; accumulation, scatter and vectors in FP64. Results within
- * about 1e-14 (relative to the largest entry) of the FP64 path: the
- * FP64-accurate fast path. Deterministic calls use FP64 records. */
+/* DOUBLE_FLOAT (Taylor-Hood and P1 assembly, Taylor-Hood state VJP): the
+ * element arithmetic of the Jacobian and residual in double-float (each
+ * value a pair of floats, about 48 significant bits) on the FP32 pipe, which
+ * GB300 issues about 64x faster than FP64; accumulation, scatter and vectors
+ * in FP64. Results within about 1e-14 (relative to the largest entry) of
+ * the FP64 path: the FP64-accurate fast path. Deterministic Taylor-Hood
+ * calls use FP64 records; the P1 VJP runs FP64. */
 #define GBFEM_PREC_DOUBLE_FLOAT 3
 /* OR-ed into a Taylor-Hood precision argument: deterministic assembly —
  * element rows are written as records and each CSR row sums its records in

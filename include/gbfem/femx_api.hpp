@@ -281,7 +281,7 @@ enum class Precision : int
   FP64     = GBFEM_PREC_FP64,
   FP32Quad = GBFEM_PREC_FP32_QUAD,
   Mixed    = GBFEM_PREC_MIXED,
-  DoubleFloat = GBFEM_PREC_DOUBLE_FLOAT, // Taylor-Hood only
+  DoubleFloat = GBFEM_PREC_DOUBLE_FLOAT,
 };
 
 /** Element operator tag: kappa-weighted P1 Poisson with nodal load. */

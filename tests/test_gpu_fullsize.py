@@ -243,6 +243,11 @@ def test_poisson_1024_matches_oracle_after_lifting(poisson1024):
 
     res = torch.zeros(n, dtype=torch.float64, device="cuda")
     jac = A.CsrMatrix(amap.pattern())
+    # the double-float (FP64-accurate) assembly meets the same gate
+    A.assembleP1Kappa(amap, dev(p["coords"]), dev(p["kappa"]), dev(f), dev(u), res, jac,
+                      precision="double_float")
+    assert rel_inf(jac.vals.cpu().numpy(), rvals) <= 1e-12
+    assert rel_inf(res.cpu().numpy(), rres) <= 1e-12
     A.assembleP1Kappa(amap, dev(p["coords"]), dev(p["kappa"]), dev(f), dev(u), res, jac)
     amap.check()
     assert rel_inf(jac.vals.cpu().numpy(), rvals) <= 1e-12

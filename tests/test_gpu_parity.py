@@ -204,13 +204,13 @@ def p1_gpu(m, coords, kappa, f, u, precision="fp64"):
 # (precision, Jacobian tolerance, residual tolerance): MIXED keeps the
 # residual in FP64 while the Jacobian comes from FP32 quadrature.
 PRECS = [("fp64", TOL64, TOL64), ("fp32_quad", TOL32, TOL32), ("mixed", TOL32, TOL64)]
-# Taylor-Hood adds the double-float mode (FP64-accurate element arithmetic
-# on the FP32 pipe), held to the FP64 gate
+# the assemblies add the double-float mode (FP64-accurate element
+# arithmetic on the FP32 pipe), held to the FP64 gate
 TH_PRECS = PRECS + [("double_float", TOL64, TOL64)]
 
 
 @pytest.mark.parametrize("case", ["p1_32", "p1_jit9", "real_sq_p1"])
-@pytest.mark.parametrize("precision,tol_j,tol_r", PRECS)
+@pytest.mark.parametrize("precision,tol_j,tol_r", TH_PRECS)
 def test_p1_assembly_matches_reference(case, precision, tol_j, tol_r):
     g = load_golden(case)
     m, _ = p1_setup(g["coords"], g["conn"])

@@ -5,9 +5,11 @@ deterministic mode: exact integrals for linear fields on jittered meshes
 Couette, shear, stagnation flow, a pressure gradient) and the Jacobian's
 identities (tests/th_checks.py). These pins share no code with the oracle.
 
-Tolerances: FP64 and double-float 1e-12; FP32 quadrature 1e-6 (J and R; R relative to the
-size of its terms, which cancel for these fields); MIXED J 1e-6 and R 1e-12
-(its residual is computed to FP64 accuracy).
+Tolerances: FP64 and double-float 1e-12; FP32 quadrature 1e-6 (J and R);
+MIXED J 1e-6 and R 1e-12 (its residual is computed to FP64 accuracy). For
+linear fields the diffusion terms cancel in the interior rows, so R is much
+smaller than its terms: the FP32 and double-float residuals (about 24 and 48
+significant bits) are measured against the size of the terms there.
 """
 import numpy as np
 import pytest
@@ -65,8 +67,12 @@ def gpu_assembler(precision, deterministic):
 
 @pytest.mark.parametrize("precision,det,tol_r,tol_j", MODES, ids=IDS)
 def test_linear_fields_match_exact_integrals(precision, det, tol_r, tol_j):
+    # FP32 and double-float round relative to the size of R's terms, which
+    # cancel for these fields (R is much smaller than its terms); FP64 and
+    # MIXED (FP64-accurate residual) are held to ||R||_inf itself
     T.check_linear_fields(gpu_assembler(precision, det), tol_r, tol_j,
-                          r_scale="terms" if precision == "fp32_quad" else "ref")
+                          r_scale="terms" if precision in ("fp32_quad", "double_float")
+                          else "ref")
 
 
 @pytest.mark.parametrize("precision,det,tol_r,tol_j", MODES, ids=IDS)
