@@ -58,7 +58,8 @@ __global__ void __launch_bounds__(128) thResidualDFKernel(ThArgs a)
 // reduction instruction, positions from the row-major in-row map (loaded
 // before the row's values are computed and staged next to them).
 // Four resident blocks per SM (128 registers, a few spilled to L1) measured
-// faster than two without spills: more warps keep the FP64 pipe fed.
+// faster than two or three with fewer spills: more warps keep the FP64 pipe
+// fed.
 // kPlain: a coloured pass (a.elems = the colour's elements, which share no
 // DOF): plain read-add-writes instead of FP64 reductions; needs pos_rows.
 template <bool kPlain = false>
@@ -71,7 +72,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
   const int e0   = blockIdx.x * 128 + warp * 32;
   const int idx  = e0 + lane;
   bool      live = idx < a.ne;
-  const int e    = (live && a.elems != nullptr) ? a.elems[idx] : idx;
+  const int e    = (kPlain && live) ? a.elems[idx] : idx;
   const ThRef<double>& R = kRefC;
 
   double aInvJ[4] = {0, 0, 0, 0}, G3[3] = {0, 0, 0};
@@ -169,7 +170,10 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
       }
     }
   };
-  auto stage = [&](int l, int rs, const uint4& pw, const double (&v)[15], double r) {
+  // row values go straight to this lane's staging row bv (not held in
+  // registers: the row loop is register-bound)
+  double* const bv = buf[warp][lane];
+  auto stage = [&](int l, int rs, const uint4& pw, double r) {
     gbfem::awaitPrerequisites(); // the outputs' zero fill may still be running
     if (live)
     {
@@ -177,11 +181,6 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     }
     if (jac)
     {
-#pragma unroll
-      for (int j = 0; j < 15; ++j)
-      {
-        buf[warp][lane][j] = v[j];
-      }
       rsb[warp][lane]  = rs;
       posb[warp][lane] = pw;
     }
@@ -209,6 +208,19 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     __syncwarp();
   };
 
+  // vq[q][b] = dN^_b(q) . ut_q does not depend on the row: formed once per
+  // element (72 FMAs) instead of once per velocity node row pair (432)
+  double vq[kNq][6];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q)
+  {
+#pragma unroll
+    for (int b = 0; b < 6; ++b)
+    {
+      vq[q][b] = R.dNr[q][b][0] * ut[q][0] + R.dNr[q][b][1] * ut[q][1];
+    }
+  }
+
 #pragma unroll
   for (int sa = 0; sa < 6; ++sa)
   {
@@ -220,7 +232,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
 #pragma unroll
       for (int q = 0; q < kNq; ++q)
       {
-        d += R.wN[q][sa] * (R.dNr[q][b][0] * ut[q][0] + R.dNr[q][b][1] * ut[q][1]);
+        d += R.wN[q][sa] * vq[q][b];
       }
       da[b] = d;
     }
@@ -231,8 +243,7 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
       uint4 pw;
       rowRef(2 * sa + c, rs, pw);
       const int oc = c ^ 1;
-      double    v[15];
-      double    r = 0;
+      double    r  = 0;
 #pragma unroll
       for (int b = 0; b < 6; ++b)
       {
@@ -240,17 +251,18 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
                            + R.T[2][sa][b] * Gv[2][c][c];
         const double mco = R.T[0][sa][b] * Gv[0][c][oc] + R.T[1][sa][b] * Gv[1][c][oc]
                            + R.T[2][sa][b] * Gv[2][c][oc];
-        v[2 * b + c]  = da[b] + mcc;
-        v[2 * b + oc] = mco;
+        bv[2 * b + c]  = da[b] + mcc;
+        bv[2 * b + oc] = mco;
         r += da[b] * st[2 * b + c];
       }
 #pragma unroll
       for (int b = 0; b < 3; ++b)
       {
-        v[12 + b] = -(aInvJ[c] * R.C[0][sa][b] + aInvJ[2 + c] * R.C[1][sa][b]);
-        r += v[12 + b] * st[12 + b];
+        const double vp = -(aInvJ[c] * R.C[0][sa][b] + aInvJ[2 + c] * R.C[1][sa][b]);
+        bv[12 + b]      = vp;
+        r += vp * st[12 + b];
       }
-      stage(2 * sa + c, rs, pw, v, r);
+      stage(2 * sa + c, rs, pw, r);
       scatterRow(2 * sa + c);
     }
   }
@@ -260,18 +272,19 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     int   rs;
     uint4 pw;
     rowRef(12 + b, rs, pw);
-    double v[15];
     double r = 0;
 #pragma unroll
     for (int sa = 0; sa < 6; ++sa)
     {
       const double c0 = R.C[0][sa][b], c1 = R.C[1][sa][b];
-      v[2 * sa]       = -(aInvJ[0] * c0 + aInvJ[2] * c1);
-      v[2 * sa + 1]   = -(aInvJ[1] * c0 + aInvJ[3] * c1);
-      r += v[2 * sa] * st[2 * sa] + v[2 * sa + 1] * st[2 * sa + 1];
+      const double v0 = -(aInvJ[0] * c0 + aInvJ[2] * c1);
+      const double v1 = -(aInvJ[1] * c0 + aInvJ[3] * c1);
+      bv[2 * sa]      = v0;
+      bv[2 * sa + 1]  = v1;
+      r += v0 * st[2 * sa] + v1 * st[2 * sa + 1];
     }
-    v[12] = v[13] = v[14] = 0.0; // structurally present, nothing added
-    stage(12 + b, rs, pw, v, r);
+    bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    stage(12 + b, rs, pw, r);
     scatterRow(12 + b);
   }
 }
