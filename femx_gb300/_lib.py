@@ -25,6 +25,7 @@ PREC_MIXED = 2
 PREC_DOUBLE_FLOAT = 3
 DETERMINISTIC = 0x100
 COLOURED = 0x200
+TILED = 0x400
 
 
 class GbfemError(RuntimeError):
@@ -136,12 +137,15 @@ SIGNATURES = {
     "gbfem_batch_run": (_i, [_vp, _i, _i, _i, _i, _i, _vp]),
     "gbfem_assembly_map_enable_colouring": (_i, [_vp, _vp]),
     "gbfem_assembly_map_num_colours": (_i, [_vp]),
+    "gbfem_assembly_map_enable_tiles": (_i, [_vp, _i, _vp, _vp, _vp]),
+    "gbfem_assembly_map_num_tiles": (_i, [_vp]),
     "gbfem_batch_check": (_i, [_vp, _vp]),
     "gbfem_batch_num_elems": (C.c_longlong, [_vp]),
     "gbfem_batch_destroy": (None, [_vp]),
     "gbfem_probe_convert": (_i, [_i, _vp, _vp, _vp, _vp]),
     "gbfem_probe_convert_ftz": (_i, [_i, _vp, _vp, _vp]),
     "gbfem_probe_rcp": (_i, [_i, _vp, _vp, _i, _vp]),
+    "gbfem_probe_dd": (_i, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None

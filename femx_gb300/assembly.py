@@ -189,6 +189,21 @@ class AssemblyMap:
     def numColours(self):
         return int(_lib.lib().gbfem_assembly_map_num_colours(self._h))
 
+    def enableTiles(self, coords, conn=None):
+        """Build the owner-computes tiles behind tiled P1 assembly (setup,
+        once per map; synchronizes the current stream). coords: [nodes, 2]
+        FP64 on the device; conn: the geometry connectivity when it is passed
+        to the assembly calls (then always), else None. Returns the number of
+        tiles."""
+        coords = _dev(coords, torch.float64, "coords")
+        conn = _dev(conn, torch.int32, "conn", allow_none=True)
+        call("gbfem_assembly_map_enable_tiles", self._h, coords.shape[0], _ptr(coords),
+             _ptr(conn), _stream())
+        return self.numTiles()
+
+    def numTiles(self):
+        return int(_lib.lib().gbfem_assembly_map_num_tiles(self._h))
+
     def check(self):
         """Raise if a kernel met invalid data (e.g. a degenerate element)."""
         call("gbfem_assembly_map_check", self._h, _stream())
@@ -308,20 +323,25 @@ def _jac_ptr(amap: AssemblyMap, jac):
     return _ptr(jac.vals)
 
 
-def _mode(precision, coloured=False, deterministic=False):
+def _mode(precision, coloured=False, deterministic=False, tiled=False):
     mode = PRECISIONS[precision]
     if coloured:
         mode |= _lib.COLOURED
     if deterministic:
         mode |= _lib.DETERMINISTIC
+    if tiled:
+        mode |= _lib.TILED
     return mode
 
 
 def assembleP1Kappa(amap: AssemblyMap, coords, kappa, f_nodal, u, res, jac=None, conn=None,
-                    precision: str = "fp64", coloured: bool = False):
+                    precision: str = "fp64", coloured: bool = False, tiled: bool = False):
     """Residual (and Jacobian) of the kappa-weighted P1 Poisson operator.
     coloured=True: colour by colour with plain adds (amap.enableColouring()
-    first), bitwise reproducible."""
+    first), bitwise reproducible. tiled=True: owner-computes tiles, each row
+    written once, no atomics (amap.enableTiles(coords, conn) first), bitwise
+    reproducible; with precision="double_float" the FP64-accurate fast
+    path."""
     coords = _dev(coords, torch.float64, "coords")
     kappa = _check_vec(kappa, amap.numElems(), "kappa")
     u = _check_vec(u, amap.numStates(), "state")
@@ -330,7 +350,7 @@ def assembleP1Kappa(amap: AssemblyMap, coords, kappa, f_nodal, u, res, jac=None,
     conn = _dev(conn, torch.int32, "conn", allow_none=True)
     call("gbfem_assemble_p1_kappa", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
          _ptr(kappa), _ptr(f_nodal), _ptr(u), _ptr(res), _jac_ptr(amap, jac),
-         _mode(precision, coloured), _stream())
+         _mode(precision, coloured, tiled=tiled), _stream())
 
 
 def vjpP1Kappa(amap: AssemblyMap, coords, kappa, u, lam, g_u=None, g_m=None, conn=None,

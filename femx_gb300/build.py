@@ -20,7 +20,7 @@ LIB = os.path.join(PKG, "libgbfem.so")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["core.cu", "pattern.cu", "boundary.cu", "p1.cu", "spmv.cu", "th.cu", "measure.cu",
-           "noalloc.cu", "batch.cu", "transpose.cu",
+           "noalloc.cu", "batch.cu", "transpose.cu", "tiles.cu",
            "navier.cu", "gmsh.cu", "hostio.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",

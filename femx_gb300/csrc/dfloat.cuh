@@ -224,4 +224,78 @@ __device__ __forceinline__ double toF64Ftz(Dd x)
   return toF64(x);
 }
 
+// double -> double-float entirely on the integer and FP32 pipes (no FP64
+// instruction, no hardware conversion): hi takes the leading 24 significant
+// bits of x (truncated), lo the next 23. The remaining 6 bits are dropped,
+// so hi + lo is within 2^-47 |x| of x. lo is built without normalising: the
+// 23 bits are placed under an implicit leading one of weight 2^(E-23) (E the
+// exponent of x) and that one is subtracted again in FP32, exactly
+// (Sterbenz). Finite x with 2^-126 <= |x| < 2^127 are split (below 2^-103
+// lo is 0); smaller magnitudes become 0; larger ones take the FP64 path.
+__device__ __forceinline__ Dd ddSplitInt(double x)
+{
+  const unsigned hi32 = static_cast<unsigned>(__double2hiint(x));
+  const unsigned lo32 = static_cast<unsigned>(__double2loint(x));
+  const unsigned sgn  = hi32 & 0x80000000u;
+  const unsigned ax   = hi32 & 0x7fffffffu;
+  const unsigned e    = ax >> 20; // biased FP64 exponent
+  if (e >= 1150u)
+  {
+    return fromF64<Dd>(x);
+  }
+  // (e - 896) << 23 | 23 leading fraction bits: the float with x's sign
+  const unsigned hb = sgn | __funnelshift_l(lo32, ax - 0x38000000u, 3);
+  const unsigned eb = (e - 919u) << 23; // weight 2^(E-23) as a float exponent
+  const unsigned lb = sgn | eb | ((lo32 >> 6) & 0x7fffffu);
+  const float    lo = __fsub_rn(__uint_as_float(lb), __uint_as_float(sgn | eb));
+  return Dd(e > 896u ? __uint_as_float(hb) : 0.0f, e >= 920u ? lo : 0.0f);
+}
+
+// double-float -> double on the integer pipe, for a normalised pair
+// (|lo| <= ulp(hi)/2, as every Dd operation leaves it). hi is widened
+// exactly into the FP64 bit pattern; lo, expressed in units of the last
+// FP64 place of hi (at most 2^28 of them, truncated toward zero), is added
+// to that pattern as a 64-bit integer. The sum stays inside hi's binade
+// except when hi is a power of two and lo negative: the result then lies in
+// the binade below, whose unit is half as large, so twice the count is
+// taken. Faithful (within one unit of the last FP64 place). Zero and
+// subnormal hi give 0; an infinite or NaN hi is widened as it is.
+__device__ __forceinline__ double ddJoinInt(Dd v)
+{
+  const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
+  const unsigned ha = hb & 0x7fffffffu, la = lb & 0x7fffffffu;
+  const unsigned eh = ha >> 23, el = la >> 23;
+  if (eh == 0xffu)
+  {
+    return f32ToF64Slow(v.hi);
+  }
+  const unsigned ml = (la & 0x7fffffu) | 0x800000u;
+  // lo = ml 2^(el-150); the FP64 unit of hi is 2^(eh-127-52)
+  unsigned t = __funnelshift_rc(ml << 5, 0u, eh - el - 24u);
+  t          = el != 0u ? t : 0u;
+  const bool neg = ((hb ^ lb) & 0x80000000u) != 0u;
+  t              = (neg && (ha & 0x7fffffu) == 0u) ? 2u * t : t;
+  const unsigned long long w =
+      ((static_cast<unsigned long long>((ha >> 3) + 0x38000000u) << 32)
+       | static_cast<unsigned long long>(ha << 29))
+      + static_cast<unsigned long long>(neg ? -static_cast<long long>(t)
+                                            : static_cast<long long>(t));
+  const unsigned long long bits =
+      eh != 0u ? (w | (static_cast<unsigned long long>(hb & 0x80000000u) << 32)) : 0ull;
+  return __longlong_as_double(static_cast<long long>(bits));
+}
+
+// 1/x in double-float: a float reciprocal refined by one Newton step,
+// y = y0 + y0 (1 - x y0), with x y0 formed exactly (TwoProduct) so that the
+// residual 1 - x y0 carries x's low part; relative error about 2^-46.
+__device__ __forceinline__ Dd ddRcp(Dd x)
+{
+  const float y0 = __frcp_rn(x.hi);
+  const float p  = __fmul_rn(x.hi, y0);
+  const float pe = __fmaf_rn(x.hi, y0, -p);
+  // 1 - x y0 = (1 - p) - pe - x.lo y0; 1 - p is exact (p is within an ulp of 1)
+  const float r = __fsub_rn(__fsub_rn(__fsub_rn(1.0f, p), pe), __fmul_rn(x.lo, y0));
+  return ddQuick(y0, __fmul_rn(y0, r));
+}
+
 } // namespace gbfem

@@ -79,6 +79,43 @@ struct gbfem_assembly_map
   int*              colour_off   = nullptr;
   int*              colour_elems = nullptr;
 
+  // Owner-computes tiles of a P1 layout, built on request by
+  // gbfem_assembly_map_enable_tiles. Every residual row is owned by one
+  // tile; a tile's elements are all elements with a vertex among its rows
+  // (elements on a tile border belong to two or three tiles and are
+  // evaluated once in each). A tiled assembly runs one block per tile: the
+  // block evaluates its elements into shared memory, then each owned row
+  // sums its entries from there and writes every CSR value and residual
+  // entry of the row once (no atomics, no zero fill, bitwise reproducible).
+  //   tile_row_off[t] .. [t + 1]    owned rows (tile_rows, ascending)
+  //   tile_elem_off[t] .. [t + 1]   elements (tile_elems, ascending) and
+  //                                 their vertices as tile-local indices,
+  //                                 three 10-bit fields (tile_conn)
+  //   tile_vert_off[t] .. [t + 1]   tile vertices: DOF and geometry node
+  //   slot_ref[s]                   CSR slot s of an owned row (r, c), c != r:
+  //                                 the one or two element edges joining r
+  //                                 and c, 16 bits each (0xffff: none):
+  //                                 tile element << 4 | edge << 2 |
+  //                                 carries-residual << 1 | which-end; the
+  //                                 diagonal slot holds 0xffffffff.
+  // An edge is numbered by its opposite vertex. Each (element, vertex r)
+  // residual term is carried by exactly one slot of row r: the one whose
+  // column is the element's next vertex after r.
+  int       num_tiles      = 0;
+  int       tile_max_rows  = 0;
+  int       tile_max_elems = 0;
+  int       tile_max_verts = 0;
+  bool      tile_sep_conn  = false; // geometry nodes differ from DOFs
+  int*      tile_row_off   = nullptr;
+  int*      tile_rows      = nullptr;
+  int*      tile_elem_off  = nullptr;
+  int*      tile_elems     = nullptr;
+  unsigned* tile_conn      = nullptr;
+  int*      tile_vert_off  = nullptr;
+  int*      tile_vert_dof  = nullptr;
+  int*      tile_vert_node = nullptr;
+  unsigned* slot_ref       = nullptr;
+
   // Status word written by hot-path kernels that meet invalid data
   // (degenerate elements); read by gbfem_assembly_map_check().
   gbfem::DeviceStatus* status = nullptr;

@@ -1,5 +1,6 @@
 // measure.cu — FP64 FMA throughput probe (see include/gbfem_measure.h).
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "gbfem_measure.h"
 
 namespace
@@ -56,6 +57,18 @@ __global__ void rcpProbe(int n, const double* in, double* out, int rsqrt)
     out[i] = rsqrt ? gbfem::rsqrtF64(in[i]) : gbfem::rcpF64(in[i]);
   }
 }
+__global__ void ddProbe(int n, const double* in, float* hi, float* lo, const float* jhi,
+                        const float* jlo, double* joined)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    const gbfem::Dd d = gbfem::ddSplitInt(in[i]);
+    hi[i]             = d.hi;
+    lo[i]             = d.lo;
+    joined[i]         = gbfem::ddJoinInt(gbfem::Dd(jhi[i], jlo[i]));
+  }
+}
 } // namespace
 
 extern "C" int gbfem_probe_rcp(int n, const double* in, double* out, int rsqrt, void* stream)
@@ -107,5 +120,20 @@ extern "C" int gbfem_probe_fp64_fma(int blocks, int threads, int iters,
             "probe arguments are invalid");
     fp64FmaProbe<<<blocks, threads, 0, asStream(stream)>>>(iters, out);
     cudaCheck(cudaGetLastError(), "probe launch");
+  });
+}
+
+extern "C" int gbfem_probe_dd(int n, const double* in, float* hi, float* lo, const float* jhi,
+                              const float* jlo, double* joined, void* stream)
+{
+  using namespace gbfem;
+  return guarded([&] {
+    require(n >= 0 && (n == 0 || (in && hi && lo && jhi && jlo && joined)),
+            "probe arguments are invalid");
+    if (n > 0)
+    {
+      ddProbe<<<blocksFor(n, 256), 256, 0, asStream(stream)>>>(n, in, hi, lo, jhi, jlo, joined);
+      cudaCheck(cudaGetLastError(), "double-float probe launch");
+    }
   });
 }

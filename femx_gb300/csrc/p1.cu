@@ -13,6 +13,7 @@
 // source is exact for that rule: F_i = |det|/24 (f_i + f_0 + f_1 + f_2).
 // Results are scatter-added with FP64 reductions at L2 (red.global.add.f64).
 #include "p1_elem.cuh"
+#include "p1_tiled.cuh"
 
 namespace
 {
@@ -154,8 +155,9 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     require(res != nullptr, "Assembly residual output is null");
     require(res != u && vals != u && (vals == nullptr || res != vals),
             "Assembly state, residual, and matrix values must not alias");
-    const bool col = (precision & GBFEM_COLOURED) != 0;
-    precision &= ~GBFEM_COLOURED;
+    const bool col   = (precision & GBFEM_COLOURED) != 0;
+    const bool tiled = (precision & GBFEM_TILED) != 0;
+    precision &= ~(GBFEM_COLOURED | GBFEM_TILED);
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
     require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
@@ -166,6 +168,59 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
     a.f            = f_nodal;
     a.res          = res;
     a.vals         = vals;
+    if (tiled)
+    {
+      require(!col, "tiled and coloured assembly are exclusive");
+      require(precision != GBFEM_PREC_MIXED,
+              "tiled assembly runs in FP64, FP32_QUAD or DOUBLE_FLOAT");
+      require(map->tile_row_off != nullptr,
+              "tiled assembly needs gbfem_assembly_map_enable_tiles on the map");
+      require((conn != nullptr) == map->tile_sep_conn,
+              "tiled assembly: pass the geometry connectivity exactly when the tiles were "
+              "built with it");
+      P1TileArgs t{};
+      t.row_off   = map->tile_row_off;
+      t.rows      = map->tile_rows;
+      t.elem_off  = map->tile_elem_off;
+      t.elems     = map->tile_elems;
+      t.tconn     = map->tile_conn;
+      t.vert_off  = map->tile_vert_off;
+      t.vert_dof  = map->tile_vert_dof;
+      t.vert_node = map->tile_vert_node;
+      t.slot_ref  = map->slot_ref;
+      t.row_ptr   = map->row_ptr;
+      t.coords    = a.coords;
+      t.kappa     = kappa;
+      t.f         = f_nodal;
+      t.u         = u;
+      t.res       = res;
+      t.vals      = vals;
+      t.status    = map->status;
+      const bool load = f_nodal != nullptr, jac = vals != nullptr;
+      if (precision == GBFEM_PREC_DOUBLE_FLOAT)
+      {
+        load ? (jac ? launchP1Tiled<Dd, true, true>(t, map, s)
+                    : launchP1Tiled<Dd, true, false>(t, map, s))
+             : (jac ? launchP1Tiled<Dd, false, true>(t, map, s)
+                    : launchP1Tiled<Dd, false, false>(t, map, s));
+      }
+      else if (precision == GBFEM_PREC_FP64)
+      {
+        load ? (jac ? launchP1Tiled<double, true, true>(t, map, s)
+                    : launchP1Tiled<double, true, false>(t, map, s))
+             : (jac ? launchP1Tiled<double, false, true>(t, map, s)
+                    : launchP1Tiled<double, false, false>(t, map, s));
+      }
+      else
+      {
+        load ? (jac ? launchP1Tiled<float, true, true>(t, map, s)
+                    : launchP1Tiled<float, true, false>(t, map, s))
+             : (jac ? launchP1Tiled<float, false, true>(t, map, s)
+                    : launchP1Tiled<float, false, false>(t, map, s));
+      }
+      cudaCheck(cudaGetLastError(), "tiled P1 assembly launch");
+      return;
+    }
     zeroForNext(vals, vals != nullptr ? map->nnz : 0, res, map->num_res, s);
     if (a.ne == 0)
     {
@@ -212,6 +267,7 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     require(lam != nullptr, "VJP adjoint input is null");
     require(g_u != lam && g_u != u && g_m != lam && g_m != u,
             "VJP outputs must not alias inputs");
+    require((precision & GBFEM_TILED) == 0, "the P1 VJP has no tiled form");
     const bool col = (precision & GBFEM_COLOURED) != 0;
     precision &= ~GBFEM_COLOURED;
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,

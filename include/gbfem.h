@@ -63,6 +63,15 @@ extern "C" {
  * read-add-writes, no atomics (gbfem_assembly_map_enable_colouring first);
  * bitwise reproducible like GBFEM_DETERMINISTIC, for any layout. */
 #define GBFEM_COLOURED 0x200
+/* OR-ed into a P1 assembly precision argument (FP64, FP32_QUAD or
+ * DOUBLE_FLOAT): owner-computes tiled assembly (gbfem_assembly_map_enable_tiles
+ * first). Every residual row belongs to one tile of nearby rows; a block per
+ * tile evaluates the tile's elements into shared memory, then writes each of
+ * its rows once: no atomics, no zero fill, bitwise reproducible. With
+ * DOUBLE_FLOAT it is the FP64-accurate fast assembly: the element
+ * arithmetic and every conversion run on the FP32 and integer pipes, FP64
+ * instructions only form the coordinate differences. */
+#define GBFEM_TILED 0x400
 
 GBFEM_API const char* gbfem_last_error(void);
 GBFEM_API int         gbfem_version(void);
@@ -120,6 +129,24 @@ GBFEM_API int  gbfem_assembly_map_enable_gather(gbfem_assembly_map* map, void* s
  * gbfem_assembly_map_num_colours: 0 before colouring. */
 GBFEM_API int  gbfem_assembly_map_enable_colouring(gbfem_assembly_map* map, void* stream);
 GBFEM_API int  gbfem_assembly_map_num_colours(const gbfem_assembly_map* map);
+/* Builds the owner-computes tiles behind GBFEM_TILED for a P1 layout (three
+ * identical residual and state DOFs per element; setup: reads the DOF table,
+ * `conn`, `coords` and the pattern back, builds on the host, allocates and
+ * synchronizes `stream`; later calls return at once). Rows are ordered along
+ * a Morton curve of their vertex coordinates (coords: num_nodes x 2,
+ * node-major; conn: the geometry connectivity, num_elems x 3, or null when
+ * geometry nodes are the DOFs, and then null in every tiled assembly call
+ * too); tiles are runs of at most 256 rows, 1024 elements and 1024
+ * vertices. About 4 bytes per CSR slot plus 20 bytes per element of device
+ * memory. GBFEM_EINVAL for other layouts, for an element with a repeated
+ * DOF, a DOF on two geometry nodes, or an edge shared by more than two
+ * elements (a non-conforming mesh). No counterpart in the reference, whose
+ * assembly scatter-adds (Assembly.hpp:186-223, CudaAssembly.hpp:160-168).
+ * gbfem_assembly_map_num_tiles: 0 before tiling. */
+GBFEM_API int  gbfem_assembly_map_enable_tiles(gbfem_assembly_map* map, int num_nodes,
+                                               const double* coords, const int* conn,
+                                               void* stream);
+GBFEM_API int  gbfem_assembly_map_num_tiles(const gbfem_assembly_map* map);
 
 /* ---------------------------------------------------------------------------
  * BoundaryMap — replaces femx::assembly::makeBoundaryMap(dofs, pattern)
