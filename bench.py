@@ -650,6 +650,7 @@ def main():
         n, e = p["coords"].shape[0], p["conn"].shape[0]
         amap = A.makeAssemblyMap(n, n, d(p["offs"]), d(p["dofs"]), d(p["offs"]), d(p["dofs"]))
         pat = amap.pattern()
+        b_p1 = 20 * e + 32 * n + 8 * pat.nnz   # algorithmic bytes of one assembly
         bc = A.makeBoundaryMap(d(p["bdofs"]), pat)
         coords, kappa, f = d(p["coords"]), d(p["kappa"]), d(p["f"])
         u = torch.zeros(n, dtype=torch.float64, device="cuda")
@@ -692,6 +693,31 @@ def main():
         err_df = {"jacobian": float((v_df - jac.vals).abs().max() / jac.vals.abs().max()),
                   "residual": float((r_df - res).abs().max() / res.abs().max())}
         del v_df, r_df
+        # the owner-computes tiled assembly (each CSR row written once, no
+        # atomics, no zero fill) in double-float (FP64-accurate), FP64 and FP32
+        ntiles = amap.enableTiles(coords)
+        tiled = {}
+        A.assembleP1Kappa(amap, coords, kappa, f, u, res, jac, precision="fp64")
+        v64, r64 = jac.vals.clone(), res.clone()
+        for prec in ("double_float", "fp64", "fp32_quad"):
+            def fn(prec=prec):
+                A.assembleP1Kappa(amap, coords, kappa, f, u, res, jac, precision=prec,
+                                  tiled=True)
+            t_t = timer.run(fn, args.steps, args.warmup)
+            fn()
+            v1, r1 = jac.vals.clone(), res.clone()
+            fn()
+            tiled[prec] = {
+                "bound": "hbm", "achieved": b_p1 / t_t / 1e9, "peak": hbm, "unit": "GB/s",
+                "frac": b_p1 / t_t / 1e9 / hbm, "launch_ms": t_t * 1e3,
+                "elements_per_s": e / t_t, "nnz_per_s": pat.nnz / t_t,
+                "rel_err_vs_fp64": {
+                    "jacobian": float((v1 - v64).abs().max() / v64.abs().max()),
+                    "residual": float((r1 - r64).abs().max() / r64.abs().max())},
+                "bitwise_equal_over_runs": bool(torch.equal(v1, jac.vals)
+                                                and torch.equal(r1, res))}
+            del v1, r1
+        del v64, r64
         asm()
         bcs()
         t_spmv = timer.run(spmvs, args.steps, args.warmup) / NSPMV
@@ -745,6 +771,13 @@ def main():
                                       "rel_err_vs_fp64": err_df,
                                       "precision": "FP64-accurate: element arithmetic in "
                                                    "double-float on the FP32 pipe"},
+            "assembly_tiled": dict(tiled, tiles=ntiles,
+                                   scheme="owner-computes tiles: each CSR row written once, "
+                                          "no atomics, no zero fill",
+                                   precision={"double_float": "FP64-accurate: double-float "
+                                              "element arithmetic, integer-pipe conversions",
+                                              "fp64": "IEEE FP64 element arithmetic",
+                                              "fp32_quad": "FP32 element arithmetic"}),
             "spmv": {"bound": "hbm", "achieved": b_spmv / t_spmv / 1e9, "peak": hbm,
                      "unit": "GB/s", "frac": b_spmv / t_spmv / 1e9 / hbm,
                      "launch_ms": t_spmv * 1e3, "traffic": traffic.get("spmv"),

@@ -11,6 +11,7 @@ import glob
 import os
 import shutil
 import subprocess
+import sysconfig
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
@@ -36,7 +37,8 @@ def nvcc() -> str:
 
 
 def _newest_dep() -> float:
-    files = glob.glob(os.path.join(CSRC, "*")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+    files = [f for f in glob.glob(os.path.join(CSRC, "*")) + glob.glob(os.path.join(INCLUDE, "*.h"))
+             if not f.endswith("pycore.cpp")]
     return max(os.path.getmtime(f) for f in files)
 
 
@@ -47,6 +49,37 @@ def _compile(src: str, extra: list[str]) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
     return obj
+
+
+def _core_path() -> str:
+    return os.path.join(PKG, "_core" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_core(force: bool = False) -> str:
+    """Build the pybind11 module femx_gb300._core (femx's Python surface for
+    the assembly path) against libgbfem.so, with the pybind11 headers that
+    ship with torch and the interpreter's headers. Host C++ only (g++)."""
+    lib = build()
+    out = _core_path()
+    src = os.path.join(CSRC, "pycore.cpp")
+    deps = [lib, src, os.path.join(INCLUDE, "gbfem.h")]
+    if not force and os.path.exists(out) and os.path.getmtime(out) >= max(
+            os.path.getmtime(f) for f in deps):
+        return out
+    import torch.utils.cpp_extension as ext
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("g++ not found: needed to build femx_gb300._core")
+    incs = [sysconfig.get_paths()["include"], INCLUDE] + ext.include_paths()[:1]
+    tmp = out + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-fvisibility=hidden",
+           *["-I" + i for i in incs], src, "-L" + PKG, "-l:libgbfem.so",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"femx_gb300._core build failed:\n{r.stderr[-4000:]}")
+    os.replace(tmp, out)
+    return out
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
@@ -67,3 +100,4 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
 
 if __name__ == "__main__":
     print(build(force=True))
+    print(build_core(force=True))

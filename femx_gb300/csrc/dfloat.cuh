@@ -227,7 +227,7 @@ __device__ __forceinline__ double toF64Ftz(Dd x)
 // double -> double-float entirely on the integer and FP32 pipes (no FP64
 // instruction, no hardware conversion): hi takes the leading 24 significant
 // bits of x (truncated), lo the next 23. The remaining 6 bits are dropped,
-// so hi + lo is within 2^-47 |x| of x. lo is built without normalising: the
+// so hi + lo is within 2^-46 |x| of x. lo is built without normalising: the
 // 23 bits are placed under an implicit leading one of weight 2^(E-23) (E the
 // exponent of x) and that one is subtracted again in FP32, exactly
 // (Sterbenz). Finite x with 2^-126 <= |x| < 2^127 are split (below 2^-103
