@@ -254,12 +254,13 @@ __device__ __forceinline__ Dd ddSplitInt(double x)
 // double-float -> double on the integer pipe, for a normalised pair
 // (|lo| <= ulp(hi)/2, as every Dd operation leaves it). hi is widened
 // exactly into the FP64 bit pattern; lo, expressed in units of the last
-// FP64 place of hi (at most 2^28 of them, truncated toward zero), is added
-// to that pattern as a 64-bit integer. The sum stays inside hi's binade
-// except when hi is a power of two and lo negative: the result then lies in
-// the binade below, whose unit is half as large, so twice the count is
-// taken. Faithful (within one unit of the last FP64 place). Zero and
-// subnormal hi give 0; an infinite or NaN hi is widened as it is.
+// FP64 place of hi (fewer than 2^29 of them, truncated toward zero), is
+// added to that pattern as a 64-bit integer. The sum stays inside hi's
+// binade except when hi is a power of two and lo of the other sign: the
+// result then lies in the binade below, whose unit is half as large, so lo
+// is counted in those units. Faithful (within one unit of the last FP64
+// place) for |hi| >= 2^-103; below that lo is dropped (the result is hi).
+// Zero and subnormal hi give 0; an infinite or NaN hi is widened as it is.
 __device__ __forceinline__ double ddJoinInt(Dd v)
 {
   const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
@@ -269,12 +270,13 @@ __device__ __forceinline__ double ddJoinInt(Dd v)
   {
     return f32ToF64Slow(v.hi);
   }
-  const unsigned ml = (la & 0x7fffffu) | 0x800000u;
-  // lo = ml 2^(el-150); the FP64 unit of hi is 2^(eh-127-52)
-  unsigned t = __funnelshift_rc(ml << 5, 0u, eh - el - 24u);
-  t          = el != 0u ? t : 0u;
-  const bool neg = ((hb ^ lb) & 0x80000000u) != 0u;
-  t              = (neg && (ha & 0x7fffffu) == 0u) ? 2u * t : t;
+  // lo = ml 2^(max(el,1)-150) (subnormal lo without the implicit one); the
+  // FP64 unit of hi is 2^(eh-179), so lo counts ml 2^(max(el,1)-eh+29) units
+  const unsigned ml  = (la & 0x7fffffu) | (el != 0u ? 0x800000u : 0u);
+  const unsigned ee  = el != 0u ? el : 1u;
+  const bool     neg = ((hb ^ lb) & 0x80000000u) != 0u;
+  const unsigned dn  = (neg && (ha & 0x7fffffu) == 0u) ? 1u : 0u; // into the binade below
+  const unsigned t   = __funnelshift_rc(ml << 6, 0u, eh - ee - 23u - dn);
   const unsigned long long w =
       ((static_cast<unsigned long long>((ha >> 3) + 0x38000000u) << 32)
        | static_cast<unsigned long long>(ha << 29))

@@ -194,7 +194,7 @@ int precisionMode(const std::string& p)
   throw std::runtime_error("unknown precision mode: " + p);
 }
 
-// A read-only view of a device array owned by a handle, exposing
+// A view of a device array owned by a handle (not to be written), exposing
 // __cuda_array_interface__ (torch.as_tensor(view, device="cuda") shares it).
 struct DeviceView
 {
@@ -206,7 +206,7 @@ struct DeviceView
     py::dict d;
     d["shape"]   = py::make_tuple(n);
     d["typestr"] = typestr;
-    d["data"]    = py::make_tuple(ptr, true);
+    d["data"]    = py::make_tuple(ptr, false);
     d["version"] = 3;
     d["strides"] = py::none();
     return d;

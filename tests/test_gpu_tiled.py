@@ -100,7 +100,9 @@ def test_double_float_split_keeps_47_bits():
                                   np.nextafter(1.0, 2.0), np.nextafter(1.0, 0.0)])])
     hi, lo, _ = dd_probe(x, np.zeros_like(x), np.zeros_like(x))
     s = hi.astype(np.float64) + lo.astype(np.float64)   # exact: 24 + 23 bits
-    assert np.all(np.abs(s - x) <= 2.0 ** -46 * np.abs(x))
+    big = np.abs(x) >= 2.0 ** -103                       # below, lo is 0
+    assert np.all(np.abs(s - x)[big] <= 2.0 ** -46 * np.abs(x)[big])
+    assert np.all(np.abs(s - x)[~big] <= 2.0 ** -23 * np.abs(x)[~big])
     # hi is x truncated to float: same sign, not larger in magnitude
     assert np.all(np.abs(hi.astype(np.float64)) <= np.abs(x))
     assert np.all((hi == 0) | (np.sign(hi) == np.sign(x)))
@@ -121,7 +123,9 @@ def test_double_float_join_is_faithful():
     jlo = np.concatenate([jlo, pl, np.zeros(4096, np.float32), -pl, np.float32([0.0, 0.0])])
     _, _, out = dd_probe(np.zeros(jhi.size), jhi, jlo)
     exact = jhi.astype(np.float64) + jlo.astype(np.float64)    # exact in FP64
-    assert np.all(np.abs(out - exact) <= np.spacing(np.abs(exact)))
+    big = np.abs(jhi) >= 2.0 ** -103                           # below, lo is dropped
+    assert np.all(np.abs(out - exact)[big] <= np.spacing(np.abs(exact))[big])
+    assert np.all(out[~big] == jhi[~big].astype(np.float64))
     assert out[-2] == 0.0 and out[-1] == 1.5
 
 
@@ -156,7 +160,8 @@ def test_tiled_is_bitwise_reproducible_and_agrees_with_atomic(precision):
     res = torch.zeros(p["n"], dtype=torch.float64, device="cuda")
     mat = A.CsrMatrix(p["amap"].pattern())
     A.assembleP1Kappa(p["amap"], p["coords"], p["kappa"], p["f"], p["u"], res, mat)
-    assert rel_inf(v1, mat.vals.cpu().numpy()) <= 1e-14
+    # double-float carries about 2^-46 per operation
+    assert rel_inf(v1, mat.vals.cpu().numpy()) <= 1e-13
     assert rel_inf(r1, res.cpu().numpy()) <= 1e-13
 
 
@@ -244,7 +249,7 @@ def test_tiled_builder_refusals():
         A.assembleP1Kappa(amap, dev(coords), dev(np.ones(conn.shape[0])), None,
                           dev(np.zeros(n)), res, conn=dev(conn), tiled=True)
     # the Taylor-Hood layout is not P1
-    c2, k6 = meshes.p2_mesh(*meshes.structured_tri(2))
+    c2, k6, _ = meshes.p2_mesh(*meshes.structured_tri(2))
     offs6, dofs6 = meshes.th_elem_dofs(k6, c2.shape[0])
     nd = int(dofs6.max()) + 1
     tmap = A.makeAssemblyMap(nd, nd, dev(offs6), dev(dofs6), dev(offs6), dev(dofs6))
