@@ -94,13 +94,14 @@ struct gbfem_assembly_map
   //   tile_vert_off[t] .. [t + 1]   tile vertices: DOF and geometry node
   //   slot_ref[s]                   CSR slot s of an owned row (r, c), c != r:
   //                                 the one or two element edges joining r
-  //                                 and c, 16 bits each (0xffff: none):
-  //                                 tile element << 4 | edge << 2 |
-  //                                 carries-residual << 1 | which-end; the
-  //                                 diagonal slot holds 0xffffffff.
-  // An edge is numbered by its opposite vertex. Each (element, vertex r)
-  // residual term is carried by exactly one slot of row r: the one whose
-  // column is the element's next vertex after r.
+  //                                 and c, 13 bits each (bits 0-12, 13-25):
+  //                                 edge record 3 l + k (0xfff: none) |
+  //                                 carries-residual << 12; the diagonal
+  //                                 slot holds 0xffffffff.
+  // Edge k of tile element l is the edge opposite its vertex k; its record
+  // holds the stiffness entry of the edge and the residual term of vertex
+  // k + 1 (mod 3), which the slot of the direction k + 1 -> k + 2 carries:
+  // every (element, vertex) residual term is carried by exactly one slot.
   int       num_tiles      = 0;
   int       tile_max_rows  = 0;
   int       tile_max_elems = 0;

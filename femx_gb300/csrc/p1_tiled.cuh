@@ -122,24 +122,95 @@ __device__ __forceinline__ T tAbs(T x)
   return tLead(x) < 0.0 ? -x : x;
 }
 
-// tile-local element record in shared memory: the three edge weights
-// (edge k opposite vertex k) and the three residual terms
+// Row sums: double-float terms are added with TwoSum of the leading parts
+// and the trailing parts summed unnormalised (Dot2-style accumulation),
+// normalised once before the conversion; float and double add plainly.
 template <class T>
-struct TileElem
+__device__ __forceinline__ T tAcc(T acc, T x)
 {
-  T k[3];
-  T r[3];
+  return acc + x;
+}
+template <>
+__device__ __forceinline__ Dd tAcc<Dd>(Dd acc, Dd x)
+{
+  const float s  = __fadd_rn(acc.hi, x.hi);
+  const float bb = __fsub_rn(s, acc.hi);
+  const float e  = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bb)), __fsub_rn(x.hi, bb));
+  return Dd(s, __fadd_rn(__fadd_rn(acc.lo, x.lo), e));
+}
+template <class T>
+__device__ __forceinline__ T tNorm(T x)
+{
+  return x;
+}
+template <>
+__device__ __forceinline__ Dd tNorm<Dd>(Dd x)
+{
+  return gbfem::ddQuick(x.hi, x.lo);
+}
+
+// a x + b y with one rounding chain (Dot2 for double-float: both products
+// split exactly, their leading parts added with TwoSum, every error and
+// cross term gathered in the trailing part)
+template <class T>
+__device__ __forceinline__ T tDot2(T a, T x, T b, T y)
+{
+  return a * x + b * y;
+}
+template <>
+__device__ __forceinline__ Dd tDot2<Dd>(Dd a, Dd x, Dd b, Dd y)
+{
+  const float p  = __fmul_rn(a.hi, x.hi);
+  const float pe = __fmaf_rn(a.hi, x.hi, -p);
+  const float q  = __fmul_rn(b.hi, y.hi);
+  const float qe = __fmaf_rn(b.hi, y.hi, -q);
+  const float s  = __fadd_rn(p, q);
+  const float bb = __fsub_rn(s, p);
+  float       e  = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bb)), __fsub_rn(q, bb));
+  e              = __fadd_rn(e, __fadd_rn(pe, qe));
+  e              = __fmaf_rn(a.hi, x.lo, e);
+  e              = __fmaf_rn(a.lo, x.hi, e);
+  e              = __fmaf_rn(b.hi, y.lo, e);
+  e              = __fmaf_rn(b.lo, y.hi, e);
+  return gbfem::ddQuick(s, e);
+}
+
+// exact scaling by a power of two
+__device__ __forceinline__ double tScale(double x, float p2)
+{
+  return x * p2;
+}
+__device__ __forceinline__ float tScale(float x, float p2)
+{
+  return x * p2;
+}
+__device__ __forceinline__ Dd tScale(Dd x, float p2)
+{
+  return Dd(__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2));
+}
+
+// tile-local edge record in shared memory: edge k of element l (opposite
+// its vertex k) at 3 l + k holds the edge's stiffness entry and the
+// residual term of vertex k + 1 (mod 3)
+template <class T>
+struct EdgeRec
+{
+  T K;
+  T R;
 };
 
 template <class T>
 constexpr int tileSmemBytes(int verts, int elems, bool load)
 {
   return verts * static_cast<int>(sizeof(double2) + (load ? 2 : 1) * sizeof(T))
-         + elems * static_cast<int>(sizeof(TileElem<T>));
+         + 3 * elems * static_cast<int>(sizeof(EdgeRec<T>));
 }
 
+constexpr int kTileThreads = 256; // rows per tile at most; elements at most twice that
+constexpr int kRowPrefetch = 8;   // slot records of a row held in registers
+
 template <class T, bool kLoad, bool kJac>
-__global__ void __launch_bounds__(256) p1TiledKernel(P1TileArgs a)
+__global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const int t   = blockIdx.x;
@@ -150,46 +221,64 @@ __global__ void __launch_bounds__(256) p1TiledKernel(P1TileArgs a)
   const int r0  = a.row_off[t];
   const int nr  = a.row_off[t + 1] - r0;
 
-  double2*     sx = reinterpret_cast<double2*>(smem);
-  T*           su = reinterpret_cast<T*>(sx + nv);
-  T*           sf = su + nv;
-  TileElem<T>* se = reinterpret_cast<TileElem<T>*>(sf + (kLoad ? nv : 0));
+  double2*    sx = reinterpret_cast<double2*>(smem);
+  T*          su = reinterpret_cast<T*>(sx + nv);
+  T*          sf = su + nv;
+  EdgeRec<T>* se = reinterpret_cast<EdgeRec<T>*>(sf + (kLoad ? nv : 0));
+
+  // the row phase's global inputs, loaded before the barriers so that their
+  // latency hides behind the vertex and element phases
+  const int i  = threadIdx.x;
+  int       r  = -1, rs = 0, re = 0;
+  unsigned  w[kRowPrefetch];
+  if (i < nr)
+  {
+    r  = a.rows[r0 + i];
+    rs = a.row_ptr[r];
+    re = a.row_ptr[r + 1];
+  }
+#pragma unroll
+  for (int k = 0; k < kRowPrefetch; ++k)
+  {
+    w[k] = rs + k < re ? a.slot_ref[rs + k] : 0u;
+  }
 
   // 0. vertices
-  for (int i = threadIdx.x; i < nv; i += blockDim.x)
+  for (int j = i; j < nv; j += kTileThreads)
   {
-    const int d = a.vert_dof[v0 + i];
-    const int n = a.vert_node[v0 + i];
-    sx[i]       = a.coords[n];
-    su[i]       = tSplit<T>(a.u[d]);
+    const int d = a.vert_dof[v0 + j];
+    const int n = a.vert_node[v0 + j];
+    sx[j]       = a.coords[n];
+    su[j]       = tSplit<T>(a.u[d]);
     if (kLoad)
     {
-      sf[i] = tSplit<T>(a.f[n]);
+      sf[j] = tSplit<T>(a.f[n]);
     }
   }
   __syncthreads();
 
   // 1. elements
-  for (int l = threadIdx.x; l < nel; l += blockDim.x)
+  for (int l = i; l < nel; l += kTileThreads)
   {
     const unsigned c    = a.tconn[e0 + l];
+    const int      e    = a.elems[e0 + l];
+    const double   kap  = a.kappa[e];
     const int      i0   = c & 1023u, i1 = (c >> 10) & 1023u, i2 = c >> 20;
     const double2  x0   = sx[i0], x1 = sx[i1], x2 = sx[i2];
     const T        ax   = tSplit<T>(x1.x - x0.x), ay = tSplit<T>(x1.y - x0.y);
     const T        bx   = tSplit<T>(x2.x - x0.x), by = tSplit<T>(x2.y - x0.y);
-    const T        det  = ax * by - bx * ay;
+    const T        det  = tDot2(ax, by, -bx, ay);
     T              adet = tAbs(det);
-    const int      e    = a.elems[e0 + l];
     if (!(tLead(adet) >= 1.0e-30))
     {
       gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
       adet = T(1);
     }
-    const T s   = tSplit<T>(a.kappa[e]) * tRcp(adet) * T(0.5);
+    const T s   = tScale(tSplit<T>(kap) * tRcp(adet), 0.5f);
     const T cx  = bx - ax, cy = by - ay;
-    const T k12 = -(s * (ax * bx + ay * by));
-    const T k01 = -(s * (bx * cx + by * cy));
-    const T k02 = s * (ax * cx + ay * cy);
+    const T k12 = -(s * tDot2(ax, bx, ay, by));
+    const T k01 = -(s * tDot2(bx, cx, by, cy));
+    const T k02 = s * tDot2(ax, cx, ay, cy);
     const T u0 = su[i0], u1 = su[i1], u2 = su[i2];
     const T P = k01 * (u1 - u0), Q = k02 * (u2 - u0), R = k12 * (u2 - u1);
     T       rr0 = P + Q, rr1 = R - P, rr2 = -(Q + R);
@@ -202,61 +291,62 @@ __global__ void __launch_bounds__(256) p1TiledKernel(P1TileArgs a)
       rr1 -= cf * (f1 + fs);
       rr2 -= cf * (f2 + fs);
     }
-    TileElem<T>& E = se[l];
-    E.k[0]         = k12;
-    E.k[1]         = k02;
-    E.k[2]         = k01;
-    E.r[0]         = rr0;
-    E.r[1]         = rr1;
-    E.r[2]         = rr2;
+    se[3 * l + 0] = EdgeRec<T>{k12, rr1};
+    se[3 * l + 1] = EdgeRec<T>{k02, rr2};
+    se[3 * l + 2] = EdgeRec<T>{k01, rr0};
   }
   __syncthreads();
 
   // 2. rows
-  for (int i = threadIdx.x; i < nr; i += blockDim.x)
+  if (i < nr)
   {
-    const int r  = a.rows[r0 + i];
-    const int rs = a.row_ptr[r], re = a.row_ptr[r + 1];
-    T         off = T(0), res = T(0);
-    int       ds  = -1;
-    for (int sl = rs; sl < re; ++sl)
-    {
-      const unsigned w = a.slot_ref[sl];
-      if (w == 0xffffffffu)
+    T    off = T(0), res = T(0);
+    int  ds  = -1;
+    auto slot = [&](int sl, unsigned wk) {
+      if (wk == 0xffffffffu)
       {
         ds = sl;
-        continue;
+        return;
       }
-      T K = T(0);
-#pragma unroll
-      for (int h = 0; h < 2; ++h)
+      const EdgeRec<T> e1 = se[wk & 0xfffu];
+      T                K  = e1.K;
+      if (wk & 0x1000u)
       {
-        const unsigned p = h == 0 ? (w & 0xffffu) : (w >> 16);
-        if (p != 0xffffu)
+        res = tAcc(res, e1.R);
+      }
+      const unsigned o2 = (wk >> 13) & 0xfffu;
+      if (o2 != 0xfffu)
+      {
+        const EdgeRec<T> e2 = se[o2];
+        K                   = K + e2.K;
+        if (wk & 0x2000000u)
         {
-          const TileElem<T>& E = se[p >> 4];
-          const unsigned     k = (p >> 2) & 3u;
-          K                    = h == 0 ? E.k[k] : K + E.k[k];
-          if (p & 2u)
-          {
-            // the row's vertex is the edge end after (which-end 0) or
-            // before (1) the opposite vertex
-            const unsigned v = (p & 1u) ? (k + 2u) % 3u : (k + 1u) % 3u;
-            res += E.r[v];
-          }
+          res = tAcc(res, e2.R);
         }
       }
-      off += K;
+      off = tAcc(off, K);
       if (kJac)
       {
         a.vals[sl] = tJoin(K);
       }
+    };
+#pragma unroll
+    for (int k = 0; k < kRowPrefetch; ++k)
+    {
+      if (rs + k < re)
+      {
+        slot(rs + k, w[k]);
+      }
+    }
+    for (int sl = rs + kRowPrefetch; sl < re; ++sl)
+    {
+      slot(sl, a.slot_ref[sl]);
     }
     if (kJac && ds >= 0)
     {
-      a.vals[ds] = tJoin(-off);
+      a.vals[ds] = tJoin(-tNorm(off));
     }
-    a.res[r] = tJoin(res);
+    a.res[r] = tJoin(tNorm(res));
   }
 }
 
@@ -273,7 +363,7 @@ void launchP1Tiled(const P1TileArgs& a, const gbfem_assembly_map* m, cudaStream_
   }
   if (m->num_tiles > 0)
   {
-    p1TiledKernel<T, kLoad, kJac><<<m->num_tiles, 256, bytes, s>>>(a);
+    p1TiledKernel<T, kLoad, kJac><<<m->num_tiles, kTileThreads, bytes, s>>>(a);
   }
 }
 

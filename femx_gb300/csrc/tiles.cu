@@ -12,8 +12,9 @@
 //   1. rows are ordered along a Morton (Z-order) curve of their vertex
 //      coordinates, so consecutive rows are close in space;
 //   2. tiles are greedy runs of that order, closed when a tile would exceed
-//      256 rows, 1024 elements or 1024 vertices (the field widths of the
-//      tile-local indices);
+//      256 rows, 512 elements (two per thread of the 256-thread block that
+//      evaluates them) or 1024 vertices (the field width of the tile-local
+//      vertex indices);
 //   3. for every CSR slot (r, c), c != r, of a row the slot records which
 //      one or two element edges join r and c (a P1 edge belongs to at most
 //      two triangles of a conforming mesh; more is refused), and which
@@ -34,7 +35,7 @@ using gbfem::cudaCheck;
 using gbfem::require;
 
 constexpr int kTileRows  = 256;
-constexpr int kTileElems = 1024;
+constexpr int kTileElems = 512;
 constexpr int kTileVerts = 1024;
 
 template <class T>
@@ -274,18 +275,19 @@ Tiles buildTiles(int ne, int nrows, const std::vector<int>& dofs,
           const int* en = col_ind.data() + row_ptr[r + 1];
           const int* it = std::lower_bound(b, en, c);
           require(it != en && *it == c, "tiled assembly: the CSR pattern lacks an element entry");
-          const unsigned ref = (static_cast<unsigned>(l) << 4) | (static_cast<unsigned>(k) << 2)
-                               | ((vc == (vr + 1) % 3 ? 1u : 0u) << 1) | (w == 1 ? 1u : 0u);
+          // edge record 3 l + k; the direction from vertex k+1 to vertex
+          // k+2 carries the residual term of vertex k+1
+          const unsigned ref = static_cast<unsigned>(3 * l + k) | (w == 0 ? 0x1000u : 0u);
           unsigned& slot = T.slot_ref[static_cast<size_t>(it - col_ind.data())];
-          if ((slot & 0xffffu) == 0xffffu)
+          if (slot == 0xffffffffu)
           {
-            slot = (slot & 0xffff0000u) | ref;
+            slot = ref | (0xfffu << 13);
           }
           else
           {
-            require((slot >> 16) == 0xffffu,
+            require((slot >> 13) == 0xfffu,
                     "tiled assembly: more than two elements share an edge");
-            slot = (slot & 0xffffu) | (ref << 16);
+            slot = (slot & 0x1fffu) | (ref << 13);
           }
         }
       }
