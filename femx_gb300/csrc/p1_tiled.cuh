@@ -242,6 +242,16 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
   {
     w[k] = rs + k < re ? a.slot_ref[rs + k] : 0u;
   }
+  // the element phase's global inputs (at most two elements per thread)
+  unsigned ec[2];
+  double   ek[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+  {
+    const int l = i + h * kTileThreads;
+    ec[h]       = l < nel ? a.tconn[e0 + l] : 0u;
+    ek[h]       = l < nel ? a.kappa[a.elems[e0 + l]] : 0.0;
+  }
 
   // 0. vertices
   for (int j = i; j < nv; j += kTileThreads)
@@ -258,11 +268,16 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
   __syncthreads();
 
   // 1. elements
-  for (int l = i; l < nel; l += kTileThreads)
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
   {
-    const unsigned c    = a.tconn[e0 + l];
-    const int      e    = a.elems[e0 + l];
-    const double   kap  = a.kappa[e];
+    const int l = i + h * kTileThreads;
+    if (l >= nel)
+    {
+      break;
+    }
+    const unsigned c    = ec[h];
+    const double   kap  = ek[h];
     const int      i0   = c & 1023u, i1 = (c >> 10) & 1023u, i2 = c >> 20;
     const double2  x0   = sx[i0], x1 = sx[i1], x2 = sx[i2];
     const T        ax   = tSplit<T>(x1.x - x0.x), ay = tSplit<T>(x1.y - x0.y);
@@ -271,7 +286,7 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
     T              adet = tAbs(det);
     if (!(tLead(adet) >= 1.0e-30))
     {
-      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, a.elems[e0 + l]);
       adet = T(1);
     }
     const T s   = tScale(tSplit<T>(kap) * tRcp(adet), 0.5f);

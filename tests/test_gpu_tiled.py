@@ -250,7 +250,7 @@ def test_tiled_builder_refusals():
                           dev(np.zeros(n)), res, conn=dev(conn), tiled=True)
     # the Taylor-Hood layout is not P1
     c2, k6, _ = meshes.p2_mesh(*meshes.structured_tri(2))
-    offs6, dofs6 = meshes.th_elem_dofs(k6, c2.shape[0])
+    offs6, dofs6, _ = meshes.th_elem_dofs(k6, c2.shape[0])
     nd = int(dofs6.max()) + 1
     tmap = A.makeAssemblyMap(nd, nd, dev(offs6), dev(dofs6), dev(offs6), dev(dofs6))
     with pytest.raises(_lib.GbfemError, match="P1 layout"):
