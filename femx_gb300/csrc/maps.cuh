@@ -87,7 +87,14 @@ struct gbfem_assembly_map
   // block evaluates its elements into shared memory, then each owned row
   // sums its entries from there and writes every CSR value and residual
   // entry of the row once (no atomics, no zero fill, bitwise reproducible).
-  //   tile_row_off[t] .. [t + 1]    owned rows (tile_rows, ascending)
+  //   tile_row_off[t] .. [t + 1]    owned rows, ascending: {row, first CSR
+  //                                 slot, end slot, first slot in the tile's
+  //                                 staged row values} (tile_row_info)
+  //   tile_run_off[t] .. [t + 1]    runs of consecutive owned rows, for the
+  //                                 coalesced write-out: {first row, its
+  //                                 index in the tile, first CSR slot, its
+  //                                 index in the staged values}, closed by a
+  //                                 sentinel {0, rows, 0, slots} (tile_runs)
   //   tile_elem_off[t] .. [t + 1]   elements (tile_elems, ascending) and
   //                                 their vertices as tile-local indices,
   //                                 three 10-bit fields (tile_conn)
@@ -106,9 +113,13 @@ struct gbfem_assembly_map
   int       tile_max_rows  = 0;
   int       tile_max_elems = 0;
   int       tile_max_verts = 0;
+  int       tile_max_slots = 0;
+  int       tile_max_runs  = 0;     // runs of one tile, sentinel included
   bool      tile_sep_conn  = false; // geometry nodes differ from DOFs
   int*      tile_row_off   = nullptr;
-  int*      tile_rows      = nullptr;
+  int4*     tile_row_info  = nullptr;
+  int*      tile_run_off   = nullptr;
+  int4*     tile_runs      = nullptr;
   int*      tile_elem_off  = nullptr;
   int*      tile_elems     = nullptr;
   unsigned* tile_conn      = nullptr;

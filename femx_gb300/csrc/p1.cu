@@ -180,7 +180,9 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
               "built with it");
       P1TileArgs t{};
       t.row_off   = map->tile_row_off;
-      t.rows      = map->tile_rows;
+      t.row_info  = map->tile_row_info;
+      t.run_off   = map->tile_run_off;
+      t.runs      = map->tile_runs;
       t.elem_off  = map->tile_elem_off;
       t.elems     = map->tile_elems;
       t.tconn     = map->tile_conn;
@@ -188,7 +190,6 @@ extern "C" int gbfem_assemble_p1_kappa(const gbfem_assembly_map* map,
       t.vert_dof  = map->tile_vert_dof;
       t.vert_node = map->tile_vert_node;
       t.slot_ref  = map->slot_ref;
-      t.row_ptr   = map->row_ptr;
       t.coords    = a.coords;
       t.kappa     = kappa;
       t.f         = f_nodal;

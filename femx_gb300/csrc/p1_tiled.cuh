@@ -2,25 +2,31 @@
 // Poisson residual and Jacobian: the atomic-free replacement of the element
 // pass with FP64 reductions (tiles.cu builds the tiles and explains them).
 //
-// One block per tile, three phases separated by block barriers:
-//   0. the tile's vertices are staged in shared memory: coordinates (FP64),
-//      state and nodal source (converted to the arithmetic type T);
+// One block per tile, four phases separated by block barriers:
+//   0. the tile's vertices are staged in shared memory: coordinates, state
+//      and nodal source (converted to the arithmetic type T);
 //   1. each tile element is evaluated once: its three off-diagonal stiffness
 //      entries (one per edge, the matrix is symmetric) and its three
 //      residual terms, into shared memory;
 //   2. each owned row walks its CSR slots: slot (r, c) sums the one or two
-//      element edges joining r and c and is written once; the diagonal is
-//      minus the sum of the off-diagonals (P1 element rows sum to zero, as
-//      femx's quadrature sum of dN_i . dN_j JxW does); the residual is the
-//      sum of the element terms the row's slots carry.
+//      element edges joining r and c; the diagonal is minus the sum of the
+//      off-diagonals (P1 element rows sum to zero, as femx's quadrature sum
+//      of dN_i . dN_j JxW does); the residual is the sum of the element terms
+//      the row's slots carry. Values are staged in shared memory as FP64;
+//   3. the staged rows are written out run by run (consecutive rows have
+//      consecutive CSR slots), coalesced.
 // Every CSR value and residual entry is written exactly once with a plain
-// store: no zero fill, no atomics, the same bits on every run.
+// store: no zero fill, no atomics, the same bits on every run. The global
+// inputs of phases 1 and 2 (element connectivity and coefficient, row
+// extents and slot records) are loaded at the start, so that their latency
+// hides behind phase 0.
 //
 // T = double: plain FP64. T = gbfem::Dd: FP64-accurate double-float on the
-// FP32 pipe; the only FP64 instructions are the four coordinate
-// differences per element (they carry the mesh scale exactly), every
-// conversion runs on the integer pipe (ddSplitInt / ddJoinInt). T = float:
-// FP32 element arithmetic, FP64 outputs.
+// FP32 pipe with no FP64 instruction at all: coordinates are split exactly
+// into three floats on the integer pipe and edge vectors formed from them
+// with error-free sums; every conversion runs on the integer pipe
+// (ddSplitInt / ddJoinInt). T = float: FP32 element arithmetic (edge vectors
+// from the same exact split), FP64 outputs.
 //
 // Element formulas (edge vectors a = x1 - x0, b = x2 - x0, c = b - a):
 //   det = a x b,  s = kappa / (2 |det|)
@@ -41,7 +47,9 @@ using gbfem::Dd;
 struct P1TileArgs
 {
   const int*           row_off;
-  const int*           rows;
+  const int4*          row_info;
+  const int*           run_off;
+  const int4*          runs;
   const int*           elem_off;
   const int*           elems;
   const unsigned*      tconn;
@@ -49,7 +57,6 @@ struct P1TileArgs
   const int*           vert_dof;
   const int*           vert_node;
   const unsigned*      slot_ref;
-  const int*           row_ptr;
   const double2*       coords;
   const double*        kappa;
   const double*        f;
@@ -189,6 +196,102 @@ __device__ __forceinline__ Dd tScale(Dd x, float p2)
   return Dd(__fmul_rn(x.hi, p2), __fmul_rn(x.lo, p2));
 }
 
+// x split exactly into three floats on the integer pipe: the leading 24
+// significant bits, the next 23 and the last 6 (the x, y, z members), each
+// lower part placed under an implicit one that is subtracted again in FP32
+// (exact). Finite |x| in [2^-80, 2^127) splits exactly; smaller parts become
+// 0 below that (an absolute error under 2^-132).
+__device__ __forceinline__ float3 split3Int(double x)
+{
+  const unsigned hi32 = static_cast<unsigned>(__double2hiint(x));
+  const unsigned lo32 = static_cast<unsigned>(__double2loint(x));
+  const unsigned sgn  = hi32 & 0x80000000u;
+  const unsigned ax   = hi32 & 0x7fffffffu;
+  const unsigned e    = ax >> 20;
+  if (e >= 1150u)
+  {
+    return make_float3(gbfem::f64ToF32(x), 0.0f, 0.0f);
+  }
+  const unsigned hb = sgn | __funnelshift_l(lo32, ax - 0x38000000u, 3);
+  const unsigned e2 = (e - 919u) << 23, e3 = (e - 942u) << 23;
+  const float    a2 = __fsub_rn(__uint_as_float(sgn | e2 | ((lo32 >> 6) & 0x7fffffu)),
+                                __uint_as_float(sgn | e2));
+  const float    a3 = __fsub_rn(__uint_as_float(sgn | e3 | ((lo32 & 0x3fu) << 17)),
+                                __uint_as_float(sgn | e3));
+  return make_float3(e > 896u ? __uint_as_float(hb) : 0.0f, e >= 920u ? a2 : 0.0f,
+                     e >= 943u ? a3 : 0.0f);
+}
+
+// Coordinates as staged in shared memory: FP64 for the FP64 kernel, the
+// exact three-float split for the others.
+template <class T>
+struct VertXY
+{
+  float3 x, y;
+};
+template <>
+struct VertXY<double>
+{
+  double2 p;
+};
+
+template <class T>
+__device__ __forceinline__ VertXY<T> stageXY(double2 p)
+{
+  return VertXY<T>{split3Int(p.x), split3Int(p.y)};
+}
+template <>
+__device__ __forceinline__ VertXY<double> stageXY<double>(double2 p)
+{
+  return VertXY<double>{p};
+}
+
+__device__ __forceinline__ float twoSumErr(float a, float b, float s)
+{
+  const float bb = __fsub_rn(s, a);
+  return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// a - b from exact splits: the leading and middle differences by TwoSum,
+// their sums by TwoSum, every error term and the last difference (exact)
+// gathered in the trailing part; within about 2^-47 |a - b|.
+__device__ __forceinline__ Dd ddDiff3(float3 a, float3 b)
+{
+  const float s  = __fsub_rn(a.x, b.x);
+  const float e1 = twoSumErr(a.x, -b.x, s);
+  const float t  = __fsub_rn(a.y, b.y);
+  const float e2 = twoSumErr(a.y, -b.y, t);
+  const float h  = __fadd_rn(s, t);
+  const float l  = twoSumErr(s, t, h);
+  const float r  = __fadd_rn(l, __fadd_rn(__fadd_rn(e1, e2), __fsub_rn(a.z, b.z)));
+  return gbfem::ddQuick(h, r);
+}
+
+// the edge vector x_j - x_i in T
+template <class T>
+__device__ __forceinline__ void edge(const VertXY<T>& i, const VertXY<T>& j, T& dx, T& dy);
+template <>
+__device__ __forceinline__ void edge<double>(const VertXY<double>& i, const VertXY<double>& j,
+                                             double& dx, double& dy)
+{
+  dx = j.p.x - i.p.x;
+  dy = j.p.y - i.p.y;
+}
+template <>
+__device__ __forceinline__ void edge<Dd>(const VertXY<Dd>& i, const VertXY<Dd>& j, Dd& dx,
+                                         Dd& dy)
+{
+  dx = ddDiff3(j.x, i.x);
+  dy = ddDiff3(j.y, i.y);
+}
+template <>
+__device__ __forceinline__ void edge<float>(const VertXY<float>& i, const VertXY<float>& j,
+                                            float& dx, float& dy)
+{
+  dx = __fsub_rn(j.x.x, i.x.x) + __fsub_rn(j.x.y, i.x.y);
+  dy = __fsub_rn(j.y.x, i.y.x) + __fsub_rn(j.y.y, i.y.y);
+}
+
 // tile-local edge record in shared memory: edge k of element l (opposite
 // its vertex k) at 3 l + k holds the edge's stiffness entry and the
 // residual term of vertex k + 1 (mod 3)
@@ -199,50 +302,74 @@ struct EdgeRec
   T R;
 };
 
-template <class T>
-constexpr int tileSmemBytes(int verts, int elems, bool load)
-{
-  return verts * static_cast<int>(sizeof(double2) + (load ? 2 : 1) * sizeof(T))
-         + 3 * elems * static_cast<int>(sizeof(EdgeRec<T>));
-}
-
 constexpr int kTileThreads = 256; // rows per tile at most; elements at most twice that
 constexpr int kRowPrefetch = 8;   // slot records of a row held in registers
 
+__host__ __device__ constexpr int align16(int b)
+{
+  return (b + 15) & ~15;
+}
+
+// Shared-memory layout of a block (sizes from the map's largest tile): the
+// edge records and the runs live through the whole kernel; the staged
+// vertices (phases 0-1) and the staged row values (phases 2-3) share one
+// region, separated by the barrier after phase 1.
+template <class T>
+struct TileSmem
+{
+  int e, runs, xy, u, f, v, r, total;
+  __host__ __device__ TileSmem(int verts, int elems, int slots, int rows, int runs_, bool load)
+  {
+    e              = 0;
+    runs           = align16(e + 3 * elems * static_cast<int>(sizeof(EdgeRec<T>)));
+    xy             = align16(runs + runs_ * static_cast<int>(sizeof(int4)));
+    u              = align16(xy + verts * static_cast<int>(sizeof(VertXY<T>)));
+    f              = align16(u + verts * static_cast<int>(sizeof(T)));
+    const int vend = align16(f + (load ? verts * static_cast<int>(sizeof(T)) : 0));
+    v              = xy;
+    r              = align16(v + slots * static_cast<int>(sizeof(double)));
+    const int rend = align16(r + rows * static_cast<int>(sizeof(double)));
+    total          = vend > rend ? vend : rend;
+  }
+};
+
 template <class T, bool kLoad, bool kJac>
-__global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
+__global__ void __launch_bounds__(kTileThreads)
+    p1TiledKernel(P1TileArgs a, int max_verts, int max_elems, int max_slots, int max_runs)
 {
   extern __shared__ __align__(16) unsigned char smem[];
+  const TileSmem<T> L(max_verts, max_elems, max_slots, kTileThreads, max_runs, kLoad);
+  VertXY<T>*        sx = reinterpret_cast<VertXY<T>*>(smem + L.xy);
+  T*                su = reinterpret_cast<T*>(smem + L.u);
+  T*                sf = reinterpret_cast<T*>(smem + L.f);
+  EdgeRec<T>*       se = reinterpret_cast<EdgeRec<T>*>(smem + L.e);
+  double*           sv = reinterpret_cast<double*>(smem + L.v);
+  double*           sr = reinterpret_cast<double*>(smem + L.r);
+  int4*             sq = reinterpret_cast<int4*>(smem + L.runs);
+
   const int t   = blockIdx.x;
+  const int i   = threadIdx.x;
   const int v0  = a.vert_off[t];
   const int nv  = a.vert_off[t + 1] - v0;
   const int e0  = a.elem_off[t];
   const int nel = a.elem_off[t + 1] - e0;
   const int r0  = a.row_off[t];
   const int nr  = a.row_off[t + 1] - r0;
+  const int q0  = a.run_off[t];
+  const int nq  = a.run_off[t + 1] - q0;
 
-  double2*    sx = reinterpret_cast<double2*>(smem);
-  T*          su = reinterpret_cast<T*>(sx + nv);
-  T*          sf = su + nv;
-  EdgeRec<T>* se = reinterpret_cast<EdgeRec<T>*>(sf + (kLoad ? nv : 0));
-
-  // the row phase's global inputs, loaded before the barriers so that their
-  // latency hides behind the vertex and element phases
-  const int i  = threadIdx.x;
-  int       r  = -1, rs = 0, re = 0;
-  unsigned  w[kRowPrefetch];
+  // phase 1 and 2 inputs, loaded first (latency hidden behind phase 0)
+  int4 row = make_int4(0, 0, 0, 0);
   if (i < nr)
   {
-    r  = a.rows[r0 + i];
-    rs = a.row_ptr[r];
-    re = a.row_ptr[r + 1];
+    row = a.row_info[r0 + i];
   }
+  unsigned w[kRowPrefetch];
 #pragma unroll
   for (int k = 0; k < kRowPrefetch; ++k)
   {
-    w[k] = rs + k < re ? a.slot_ref[rs + k] : 0u;
+    w[k] = row.y + k < row.z ? a.slot_ref[row.y + k] : 0u;
   }
-  // the element phase's global inputs (at most two elements per thread)
   unsigned ec[2];
   double   ek[2];
 #pragma unroll
@@ -252,18 +379,23 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
     ec[h]       = l < nel ? a.tconn[e0 + l] : 0u;
     ek[h]       = l < nel ? a.kappa[a.elems[e0 + l]] : 0.0;
   }
+  const int4 run = i < nq ? a.runs[q0 + i] : make_int4(0, 0, 0, 0);
 
   // 0. vertices
   for (int j = i; j < nv; j += kTileThreads)
   {
     const int d = a.vert_dof[v0 + j];
     const int n = a.vert_node[v0 + j];
-    sx[j]       = a.coords[n];
+    sx[j]       = stageXY<T>(a.coords[n]);
     su[j]       = tSplit<T>(a.u[d]);
     if (kLoad)
     {
       sf[j] = tSplit<T>(a.f[n]);
     }
+  }
+  if (i < nq)
+  {
+    sq[i] = run;
   }
   __syncthreads();
 
@@ -276,20 +408,19 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
     {
       break;
     }
-    const unsigned c    = ec[h];
-    const double   kap  = ek[h];
-    const int      i0   = c & 1023u, i1 = (c >> 10) & 1023u, i2 = c >> 20;
-    const double2  x0   = sx[i0], x1 = sx[i1], x2 = sx[i2];
-    const T        ax   = tSplit<T>(x1.x - x0.x), ay = tSplit<T>(x1.y - x0.y);
-    const T        bx   = tSplit<T>(x2.x - x0.x), by = tSplit<T>(x2.y - x0.y);
-    const T        det  = tDot2(ax, by, -bx, ay);
-    T              adet = tAbs(det);
+    const unsigned c  = ec[h];
+    const int      i0 = c & 1023u, i1 = (c >> 10) & 1023u, i2 = c >> 20;
+    T              ax, ay, bx, by;
+    edge<T>(sx[i0], sx[i1], ax, ay);
+    edge<T>(sx[i0], sx[i2], bx, by);
+    const T det  = tDot2(ax, by, -bx, ay);
+    T       adet = tAbs(det);
     if (!(tLead(adet) >= 1.0e-30))
     {
       gbfem::devFail(a.status, gbfem::kDevSingularJacobian, a.elems[e0 + l]);
       adet = T(1);
     }
-    const T s   = tScale(tSplit<T>(kap) * tRcp(adet), 0.5f);
+    const T s   = tScale(tSplit<T>(ek[h]) * tRcp(adet), 0.5f);
     const T cx  = bx - ax, cy = by - ay;
     const T k12 = -(s * tDot2(ax, bx, ay, by));
     const T k01 = -(s * tDot2(bx, cx, by, cy));
@@ -312,15 +443,15 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
   }
   __syncthreads();
 
-  // 2. rows
+  // 2. rows, staged in shared memory
   if (i < nr)
   {
     T    off = T(0), res = T(0);
-    int  ds  = -1;
-    auto slot = [&](int sl, unsigned wk) {
+    int  dk  = -1;
+    auto slot = [&](int k, unsigned wk) {
       if (wk == 0xffffffffu)
       {
-        ds = sl;
+        dk = k;
         return;
       }
       const EdgeRec<T> e1 = se[wk & 0xfffu];
@@ -342,26 +473,46 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
       off = tAcc(off, K);
       if (kJac)
       {
-        a.vals[sl] = tJoin(K);
+        sv[row.w + k] = tJoin(K);
       }
     };
+    const int len = row.z - row.y;
 #pragma unroll
     for (int k = 0; k < kRowPrefetch; ++k)
     {
-      if (rs + k < re)
+      if (k < len)
       {
-        slot(rs + k, w[k]);
+        slot(k, w[k]);
       }
     }
-    for (int sl = rs + kRowPrefetch; sl < re; ++sl)
+    for (int k = kRowPrefetch; k < len; ++k)
     {
-      slot(sl, a.slot_ref[sl]);
+      slot(k, a.slot_ref[row.y + k]);
     }
-    if (kJac && ds >= 0)
+    if (kJac && dk >= 0)
     {
-      a.vals[ds] = tJoin(-tNorm(off));
+      sv[row.w + dk] = tJoin(-tNorm(off));
     }
-    a.res[r] = tJoin(tNorm(res));
+    sr[i] = tJoin(tNorm(res));
+  }
+  __syncthreads();
+
+  // 3. coalesced write-out, one warp per run of consecutive rows
+  const int warp = i >> 5, lane = i & 31;
+  for (int q = warp; q < nq - 1; q += kTileThreads / 32)
+  {
+    const int4 b = sq[q], n = sq[q + 1];
+    if (kJac)
+    {
+      for (int j = lane; j < n.w - b.w; j += 32)
+      {
+        a.vals[b.z + j] = sv[b.w + j];
+      }
+    }
+    for (int j = lane; j < n.y - b.y; j += 32)
+    {
+      a.res[b.x + j] = sr[b.y + j];
+    }
   }
 }
 
@@ -369,16 +520,18 @@ __global__ void __launch_bounds__(kTileThreads) p1TiledKernel(P1TileArgs a)
 template <class T, bool kLoad, bool kJac>
 void launchP1Tiled(const P1TileArgs& a, const gbfem_assembly_map* m, cudaStream_t s)
 {
-  const int bytes = tileSmemBytes<T>(m->tile_max_verts, m->tile_max_elems, kLoad);
-  if (bytes > 48 * 1024)
+  const TileSmem<T> L(m->tile_max_verts, m->tile_max_elems, m->tile_max_slots, kTileThreads,
+                      m->tile_max_runs, kLoad);
+  if (L.total > 48 * 1024)
   {
     gbfem::cudaCheck(cudaFuncSetAttribute(p1TiledKernel<T, kLoad, kJac>,
-                                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, L.total),
                      "tiled assembly shared memory");
   }
   if (m->num_tiles > 0)
   {
-    p1TiledKernel<T, kLoad, kJac><<<m->num_tiles, kTileThreads, bytes, s>>>(a);
+    p1TiledKernel<T, kLoad, kJac><<<m->num_tiles, kTileThreads, L.total, s>>>(
+        a, m->tile_max_verts, m->tile_max_elems, m->tile_max_slots, m->tile_max_runs);
   }
 }
 

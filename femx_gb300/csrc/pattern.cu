@@ -406,11 +406,13 @@ gbfem_assembly_map::~gbfem_assembly_map()
 {
   for (int* p : {res_offsets, res_dofs, state_offsets, state_dofs, jac_offsets,
                  jac_map, row_ptr, col_ind, gather_off, gather_slot, colour_off,
-                 colour_elems, tile_row_off, tile_rows, tile_elem_off, tile_elems,
+                 colour_elems, tile_row_off, tile_run_off, tile_elem_off, tile_elems,
                  tile_vert_off, tile_vert_dof, tile_vert_node})
   {
     gbfem::deviceFree(p);
   }
+  gbfem::deviceFree(tile_row_info);
+  gbfem::deviceFree(tile_runs);
   gbfem::deviceFree(tile_conn);
   gbfem::deviceFree(slot_ref);
   gbfem::deviceFree(status);

@@ -76,9 +76,10 @@ unsigned spread16(unsigned x)
 
 struct Tiles
 {
-  int                   max_rows = 0, max_elems = 0, max_verts = 0;
-  std::vector<int>      row_off{0}, rows, elem_off{0}, elems, vert_off{0}, vert_dof,
-      vert_node;
+  int                   max_rows = 0, max_elems = 0, max_verts = 0, max_slots = 0, max_runs = 0;
+  std::vector<int>      row_off{0}, rows, run_off{0}, elem_off{0}, elems, vert_off{0},
+      vert_dof, vert_node;
+  std::vector<int4>     row_info, runs;
   std::vector<unsigned> conn, slot_ref;
 };
 
@@ -162,6 +163,21 @@ Tiles buildTiles(int ne, int nrows, const std::vector<int>& dofs,
     std::sort(cur_elems.begin(), cur_elems.end());
     std::sort(cur_verts.begin(), cur_verts.end());
     T.rows.insert(T.rows.end(), cur_rows.begin(), cur_rows.end());
+    int nslots = 0;
+    for (size_t i = 0; i < cur_rows.size(); ++i)
+    {
+      const int r = cur_rows[i];
+      if (i == 0 || r != cur_rows[i - 1] + 1)
+      {
+        T.runs.push_back(int4{r, static_cast<int>(i), row_ptr[r], nslots});
+      }
+      T.row_info.push_back(int4{r, row_ptr[r], row_ptr[r + 1], nslots});
+      nslots += row_ptr[r + 1] - row_ptr[r];
+    }
+    T.runs.push_back(int4{0, static_cast<int>(cur_rows.size()), 0, nslots});
+    T.max_slots = std::max(T.max_slots, nslots);
+    T.max_runs  = std::max(T.max_runs, static_cast<int>(T.runs.size()) - T.run_off.back());
+    T.run_off.push_back(static_cast<int>(T.runs.size()));
     for (size_t i = 0; i < cur_verts.size(); ++i)
     {
       vloc[cur_verts[i]] = static_cast<int>(i);
@@ -330,7 +346,9 @@ extern "C" int gbfem_assembly_map_enable_tiles(gbfem_assembly_map* m, int num_no
     }
     const Tiles T          = buildTiles(ne, m->num_res, dofs, nodes, xy, rp, ci);
     int*        d_row_off  = nullptr;
-    int*        d_rows     = nullptr;
+    int4*       d_rinfo    = nullptr;
+    int*        d_run_off  = nullptr;
+    int4*       d_runs     = nullptr;
     int*        d_elem_off = nullptr;
     int*        d_elems    = nullptr;
     unsigned*   d_conn     = nullptr;
@@ -341,7 +359,9 @@ extern "C" int gbfem_assembly_map_enable_tiles(gbfem_assembly_map* m, int num_no
     try
     {
       d_row_off  = upload(T.row_off, s);
-      d_rows     = upload(T.rows, s);
+      d_rinfo    = upload(T.row_info, s);
+      d_run_off  = upload(T.run_off, s);
+      d_runs     = upload(T.runs, s);
       d_elem_off = upload(T.elem_off, s);
       d_elems    = upload(T.elems, s);
       d_conn     = upload(T.conn, s);
@@ -353,10 +373,12 @@ extern "C" int gbfem_assembly_map_enable_tiles(gbfem_assembly_map* m, int num_no
     }
     catch (...)
     {
-      for (int* p : {d_row_off, d_rows, d_elem_off, d_elems, d_vert_off, d_vdof, d_vnode})
+      for (int* p : {d_row_off, d_run_off, d_elem_off, d_elems, d_vert_off, d_vdof, d_vnode})
       {
         deviceFree(p);
       }
+      deviceFree(d_rinfo);
+      deviceFree(d_runs);
       deviceFree(d_conn);
       deviceFree(d_ref);
       throw;
@@ -366,8 +388,12 @@ extern "C" int gbfem_assembly_map_enable_tiles(gbfem_assembly_map* m, int num_no
     m->tile_max_elems = T.max_elems;
     m->tile_max_verts = T.max_verts;
     m->tile_sep_conn  = conn != nullptr;
+    m->tile_max_slots = T.max_slots;
+    m->tile_max_runs  = T.max_runs;
     m->tile_row_off   = d_row_off;
-    m->tile_rows      = d_rows;
+    m->tile_row_info  = d_rinfo;
+    m->tile_run_off   = d_run_off;
+    m->tile_runs      = d_runs;
     m->tile_elem_off  = d_elem_off;
     m->tile_elems     = d_elems;
     m->tile_conn      = d_conn;
