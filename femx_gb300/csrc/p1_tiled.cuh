@@ -22,11 +22,11 @@
 // hides behind phase 0.
 //
 // T = double: plain FP64. T = gbfem::Dd: FP64-accurate double-float on the
-// FP32 pipe with no FP64 instruction at all: coordinates are split exactly
-// into three floats on the integer pipe and edge vectors formed from them
-// with error-free sums; every conversion runs on the integer pipe
-// (ddSplitInt / ddJoinInt). T = float: FP32 element arithmetic (edge vectors
-// from the same exact split), FP64 outputs.
+// FP32 pipe; the only FP64 instructions are the four coordinate differences
+// per element (they carry the mesh scale exactly), every conversion runs on
+// the integer pipe (ddSplitInt / ddJoinInt). T = float: FP32 element
+// arithmetic, edge vectors from an exact split of the coordinates (no FP64
+// instruction), FP64 outputs.
 //
 // Element formulas (edge vectors a = x1 - x0, b = x2 - x0, c = b - a):
 //   det = a x b,  s = kappa / (2 |det|)
@@ -200,7 +200,9 @@ __device__ __forceinline__ Dd tScale(Dd x, float p2)
 // significant bits, the next 23 and the last 6 (the x, y, z members), each
 // lower part placed under an implicit one that is subtracted again in FP32
 // (exact). Finite |x| in [2^-80, 2^127) splits exactly; smaller parts become
-// 0 below that (an absolute error under 2^-132).
+// 0 below that (an absolute error under 2^-132). The FP32 kernel forms its
+// edge vectors from the leading two parts, (a.x - b.x) + (a.y - b.y): the
+// mesh scale survives the subtraction of nearby coordinates.
 __device__ __forceinline__ float3 split3Int(double x)
 {
   const unsigned hi32 = static_cast<unsigned>(__double2hiint(x));
@@ -222,49 +224,32 @@ __device__ __forceinline__ float3 split3Int(double x)
                      e >= 943u ? a3 : 0.0f);
 }
 
-// Coordinates as staged in shared memory: FP64 for the FP64 kernel, the
-// exact three-float split for the others.
+// Coordinates as staged in shared memory: FP64 for the FP64 and the
+// double-float kernels (their edge vectors are four FP64 subtractions, which
+// the otherwise idle FP64 pipe absorbs more cheaply than an exact float
+// difference costs in issue slots), the leading two parts of the exact split
+// for the FP32 kernel.
 template <class T>
 struct VertXY
 {
-  float3 x, y;
+  double2 p;
 };
 template <>
-struct VertXY<double>
+struct VertXY<float>
 {
-  double2 p;
+  float2 x, y;
 };
 
 template <class T>
 __device__ __forceinline__ VertXY<T> stageXY(double2 p)
 {
-  return VertXY<T>{split3Int(p.x), split3Int(p.y)};
+  return VertXY<T>{p};
 }
 template <>
-__device__ __forceinline__ VertXY<double> stageXY<double>(double2 p)
+__device__ __forceinline__ VertXY<float> stageXY<float>(double2 p)
 {
-  return VertXY<double>{p};
-}
-
-__device__ __forceinline__ float twoSumErr(float a, float b, float s)
-{
-  const float bb = __fsub_rn(s, a);
-  return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-
-// a - b from exact splits: the leading and middle differences by TwoSum,
-// their sums by TwoSum, every error term and the last difference (exact)
-// gathered in the trailing part; within about 2^-47 |a - b|.
-__device__ __forceinline__ Dd ddDiff3(float3 a, float3 b)
-{
-  const float s  = __fsub_rn(a.x, b.x);
-  const float e1 = twoSumErr(a.x, -b.x, s);
-  const float t  = __fsub_rn(a.y, b.y);
-  const float e2 = twoSumErr(a.y, -b.y, t);
-  const float h  = __fadd_rn(s, t);
-  const float l  = twoSumErr(s, t, h);
-  const float r  = __fadd_rn(l, __fadd_rn(__fadd_rn(e1, e2), __fsub_rn(a.z, b.z)));
-  return gbfem::ddQuick(h, r);
+  const float3 x = split3Int(p.x), y = split3Int(p.y);
+  return VertXY<float>{make_float2(x.x, x.y), make_float2(y.x, y.y)};
 }
 
 // the edge vector x_j - x_i in T
@@ -281,8 +266,8 @@ template <>
 __device__ __forceinline__ void edge<Dd>(const VertXY<Dd>& i, const VertXY<Dd>& j, Dd& dx,
                                          Dd& dy)
 {
-  dx = ddDiff3(j.x, i.x);
-  dy = ddDiff3(j.y, i.y);
+  dx = gbfem::ddSplitInt(j.p.x - i.p.x);
+  dy = gbfem::ddSplitInt(j.p.y - i.p.y);
 }
 template <>
 __device__ __forceinline__ void edge<float>(const VertXY<float>& i, const VertXY<float>& j,
