@@ -14,7 +14,8 @@
 //      of dN_i . dN_j JxW does); the residual is the sum of the element terms
 //      the row's slots carry. Values are staged in shared memory as FP64;
 //   3. the staged rows are written out run by run (consecutive rows have
-//      consecutive CSR slots), coalesced.
+//      consecutive CSR slots), coalesced (the double-float kernel stores
+//      its rows directly from phase 2 instead, see tileStaged).
 // Every CSR value and residual entry is written exactly once with a plain
 // store: no zero fill, no atomics, the same bits on every run. The global
 // inputs of phases 1 and 2 (element connectivity and coefficient, row
@@ -36,6 +37,8 @@
 //             F_i = |det|/24 (f_i + f0 + f1 + f2) (the order-2 rule is exact
 //             for the P1-interpolated source).
 #pragma once
+
+#include <type_traits>
 
 #include "dfloat.cuh"
 #include "maps.cuh"
@@ -318,10 +321,21 @@ struct TileSmem
   }
 };
 
+// Row output: staged in shared memory and written out in coalesced runs
+// (FP32 and FP64 kernels, which wait on memory), or stored directly from the
+// row phase (double-float kernel, which is bound by instruction issue and
+// pays more for the extra phase than for scattered stores).
+template <class T>
+constexpr bool tileStaged()
+{
+  return !std::is_same<T, Dd>::value;
+}
+
 template <class T, bool kLoad, bool kJac>
 __global__ void __launch_bounds__(kTileThreads)
     p1TiledKernel(P1TileArgs a, int max_verts, int max_elems, int max_slots, int max_runs)
 {
+  constexpr bool kStage = tileStaged<T>();
   extern __shared__ __align__(16) unsigned char smem[];
   const TileSmem<T> L(max_verts, max_elems, max_slots, kTileThreads, max_runs, kLoad);
   VertXY<T>*        sx = reinterpret_cast<VertXY<T>*>(smem + L.xy);
@@ -364,7 +378,7 @@ __global__ void __launch_bounds__(kTileThreads)
     ec[h]       = l < nel ? a.tconn[e0 + l] : 0u;
     ek[h]       = l < nel ? a.kappa[a.elems[e0 + l]] : 0.0;
   }
-  const int4 run = i < nq ? a.runs[q0 + i] : make_int4(0, 0, 0, 0);
+  const int4 run = kStage && i < nq ? a.runs[q0 + i] : make_int4(0, 0, 0, 0);
 
   // 0. vertices
   for (int j = i; j < nv; j += kTileThreads)
@@ -378,7 +392,7 @@ __global__ void __launch_bounds__(kTileThreads)
       sf[j] = tSplit<T>(a.f[n]);
     }
   }
-  if (i < nq)
+  if (kStage && i < nq)
   {
     sq[i] = run;
   }
@@ -458,7 +472,14 @@ __global__ void __launch_bounds__(kTileThreads)
       off = tAcc(off, K);
       if (kJac)
       {
-        sv[row.w + k] = tJoin(K);
+        if (kStage)
+        {
+          sv[row.w + k] = tJoin(K);
+        }
+        else
+        {
+          a.vals[row.y + k] = tJoin(K);
+        }
       }
     };
     const int len = row.z - row.y;
@@ -476,9 +497,27 @@ __global__ void __launch_bounds__(kTileThreads)
     }
     if (kJac && dk >= 0)
     {
-      sv[row.w + dk] = tJoin(-tNorm(off));
+      if (kStage)
+      {
+        sv[row.w + dk] = tJoin(-tNorm(off));
+      }
+      else
+      {
+        a.vals[row.y + dk] = tJoin(-tNorm(off));
+      }
     }
-    sr[i] = tJoin(tNorm(res));
+    if (kStage)
+    {
+      sr[i] = tJoin(tNorm(res));
+    }
+    else
+    {
+      a.res[row.x] = tJoin(tNorm(res));
+    }
+  }
+  if (!kStage)
+  {
+    return;
   }
   __syncthreads();
 
