@@ -298,6 +298,16 @@ __host__ __device__ constexpr int align16(int b)
   return (b + 15) & ~15;
 }
 
+// Row output: staged in shared memory and written out in coalesced runs
+// (FP32 and FP64 kernels, which wait on memory), or stored directly from the
+// row phase (double-float kernel, which is bound by instruction issue and
+// pays more for the extra phase than for scattered stores).
+template <class T>
+constexpr bool tileStaged()
+{
+  return !std::is_same<T, Dd>::value;
+}
+
 // Shared-memory layout of a block (sizes from the map's largest tile): the
 // edge records and the runs live through the whole kernel; the staged
 // vertices (phases 0-1) and the staged row values (phases 2-3) share one
@@ -308,6 +318,10 @@ struct TileSmem
   int e, runs, xy, u, f, v, r, total;
   __host__ __device__ TileSmem(int verts, int elems, int slots, int rows, int runs_, bool load)
   {
+    if (!tileStaged<T>())
+    {
+      slots = rows = runs_ = 0;
+    }
     e              = 0;
     runs           = align16(e + 3 * elems * static_cast<int>(sizeof(EdgeRec<T>)));
     xy             = align16(runs + runs_ * static_cast<int>(sizeof(int4)));
@@ -320,16 +334,6 @@ struct TileSmem
     total          = vend > rend ? vend : rend;
   }
 };
-
-// Row output: staged in shared memory and written out in coalesced runs
-// (FP32 and FP64 kernels, which wait on memory), or stored directly from the
-// row phase (double-float kernel, which is bound by instruction issue and
-// pays more for the extra phase than for scattered stores).
-template <class T>
-constexpr bool tileStaged()
-{
-  return !std::is_same<T, Dd>::value;
-}
 
 template <class T, bool kLoad, bool kJac>
 __global__ void __launch_bounds__(kTileThreads)
