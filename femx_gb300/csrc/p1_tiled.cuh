@@ -113,15 +113,17 @@ __device__ __forceinline__ Dd tRcp(Dd x)
   return gbfem::ddRcp(x);
 }
 
+// the leading part, compared in its own type (a widening to double would be
+// a conversion on GB300's slow FP64 pipe)
 __device__ __forceinline__ double tLead(double x)
 {
   return x;
 }
-__device__ __forceinline__ double tLead(float x)
+__device__ __forceinline__ float tLead(float x)
 {
   return x;
 }
-__device__ __forceinline__ double tLead(Dd x)
+__device__ __forceinline__ float tLead(Dd x)
 {
   return x.hi;
 }
@@ -129,7 +131,7 @@ __device__ __forceinline__ double tLead(Dd x)
 template <class T>
 __device__ __forceinline__ T tAbs(T x)
 {
-  return tLead(x) < 0.0 ? -x : x;
+  return tLead(x) < 0.0f ? -x : x;
 }
 
 // Row sums: double-float terms are added with TwoSum of the leading parts
@@ -335,8 +337,16 @@ struct TileSmem
   }
 };
 
+// resident blocks per SM the register allocation is held to (five for the
+// issue-bound double-float kernel: 51 registers, no spills)
+template <class T>
+constexpr int tileMinBlocks()
+{
+  return std::is_same<T, Dd>::value ? 5 : (std::is_same<T, float>::value ? 6 : 3);
+}
+
 template <class T, bool kLoad, bool kJac>
-__global__ void __launch_bounds__(kTileThreads)
+__global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
     p1TiledKernel(P1TileArgs a, int max_verts, int max_elems, int max_slots, int max_runs)
 {
   constexpr bool kStage = tileStaged<T>();
@@ -418,7 +428,7 @@ __global__ void __launch_bounds__(kTileThreads)
     edge<T>(sx[i0], sx[i2], bx, by);
     const T det  = tDot2(ax, by, -bx, ay);
     T       adet = tAbs(det);
-    if (!(tLead(adet) >= 1.0e-30))
+    if (!(tLead(adet) >= 1.0e-30f))
     {
       gbfem::devFail(a.status, gbfem::kDevSingularJacobian, a.elems[e0 + l]);
       adet = T(1);
