@@ -337,8 +337,11 @@ struct TileSmem
   }
 };
 
-// resident blocks per SM the register allocation is held to (five for the
-// issue-bound double-float kernel: 51 registers, no spills)
+// Resident blocks per SM the register allocation is held to (measured on
+// the 1024x1024 benchmark mesh): five for the issue-bound double-float
+// kernel (48 registers; 101 -> 91 us against the unbounded 57), six for the
+// latency-bound FP32 kernel (40 registers; 81 -> 70 us), three for the
+// FP64-pipe-bound FP64 kernel.
 template <class T>
 constexpr int tileMinBlocks()
 {
