@@ -726,6 +726,10 @@ def main():
                 "bitwise_equal_over_runs": bool(torch.equal(v1, jac.vals)
                                                 and torch.equal(r1, res))}
             del v1, r1
+        # the reference's own CUDA assembly (femx's assembleKernel with the same
+        # operator in femx's plug-in form), timed on the same GPU
+        ref_bar = reference_gpu_bar(torch, timer, args, p, coords, kappa, f, u, amap, pat,
+                                    v64, r64)
         del v64, r64
         asm()
         bcs()
@@ -790,6 +794,11 @@ def main():
                                               "element arithmetic, integer-pipe conversions",
                                               "fp64": "IEEE FP64 element arithmetic",
                                               "fp32_quad": "FP32 element arithmetic"}),
+            "reference_gpu_assembly": dict(ref_bar, **({"speedup": {
+                "plain_fp64": ref_bar["launch_ms"] / (t_asm * 1e3),
+                "tiled_double_float": ref_bar["launch_ms"] / tiled["double_float"]["launch_ms"],
+                "tiled_fp32": ref_bar["launch_ms"] / tiled["fp32_quad"]["launch_ms"]}}
+                if "launch_ms" in ref_bar else {})),
             "spmv": {"bound": "hbm", "achieved": b_spmv / t_spmv / 1e9, "peak": hbm,
                      "unit": "GB/s", "frac": b_spmv / t_spmv / 1e9 / hbm,
                      "launch_ms": t_spmv * 1e3, "traffic": traffic.get("spmv"),
@@ -1064,6 +1073,38 @@ def batch_cpu(sample, e_p1, e_th):
                       f"Taylor-Hood ({n['th']} elements) instances of the batch, residual + "
                       f"Jacobian + VJP (Taylor-Hood VJP as J^T lam), per-element rates "
                       f"applied to the batch's {e_p1} P1 and {e_th} Taylor-Hood elements"}
+
+
+def reference_gpu_bar(torch, timer, args, p, coords, kappa, f, u, amap, pat, v64, r64):
+    """femx's own CUDA assembly (CudaAssembly.hpp:100-169, one block of 128
+    threads per element, FP64 atomics, quadrature from ElementQuadratureData
+    tables) for the kappa-weighted P1 operator, compiled from femx's sources
+    into oracle/_ref/gpu_bar.cubin, on this GPU: its time per assembly (zero
+    fill included, as femx's assemble does it) and its distance to the FP64
+    product kernel."""
+    from oracle import gpu_bar
+    reason = gpu_bar.unavailable_reason()
+    if reason is not None:
+        return {"unavailable": reason}
+    from oracle import pyoracle as orc
+    conn = torch.from_numpy(np.ascontiguousarray(p["conn"], dtype=np.int32)).cuda()
+    tables = orc.P1Quad(p["coords"], p["conn"]).tables()
+    view = {k: v.data_ptr() for k, v in amap.view().items()}
+    view.update(num_res=amap.numRes(), num_states=amap.numStates())
+    bar = gpu_bar.RefP1Assembly(torch, coords, conn, kappa, f, tables, view)
+    res = torch.zeros_like(r64)
+    vals = torch.zeros_like(v64)
+    stream = torch.cuda.current_stream().cuda_stream
+    t = timer.run(lambda: bar.assemble(u, res, vals, stream), args.steps, args.warmup)
+    bar.assemble(u, res, vals, stream)
+    torch.cuda.synchronize()
+    return {"what": "femx assembleKernel<KappaPoissonP1> (the reference's CUDA assembly), "
+                    "with its zero fill, on this GPU",
+            "kernel": bar.kernel[:120], "launch_ms": t * 1e3,
+            "elements_per_s": amap.numElems() / t,
+            "rel_err_vs_fp64_product": {
+                "jacobian": float((vals - v64).abs().max() / v64.abs().max()),
+                "residual": float((res - r64).abs().max() / r64.abs().max())}}
 
 
 def poisson_cpu(p, n, A, asm, bcs, rhs, jac, torch):

@@ -1202,6 +1202,18 @@ void orc_p1_quad_free(void* h)
   delete static_cast<P1Quad*>(h);
 }
 
+int orc_p1_quad_tables(const void* h, int* nq, const double** N, const double** dNdx,
+                       const double** JxW)
+{
+  return guarded([&] {
+    const P1Quad& q = *static_cast<const P1Quad*>(h);
+    *nq             = q.nq;
+    *N              = q.N.data();
+    *dNdx           = q.dNdx.data();
+    *JxW            = q.JxW.data();
+  });
+}
+
 int orc_assemble_p1_kappa(const void* mh, const void* qh, const int* conn,
                           const double* kappa, const double* f_nodal,
                           const double* u, double* res, double* vals)

@@ -73,6 +73,10 @@ void orc_matvec_t(int rows, int cols, const int* row_ptr, const int* col_ind,
 void* orc_p1_quad_create(int num_nodes, const double* coords, int num_elems,
                          const int* conn, int order);
 void  orc_p1_quad_free(void* quad);
+/* The tables themselves, in femx's ElementQuadratureData layout (N [nq][3],
+ * dNdx [E][nq][3][2], JxW [E][nq]); valid while the quad lives. */
+int   orc_p1_quad_tables(const void* quad, int* nq, const double** N, const double** dNdx,
+                         const double** JxW);
 
 /* ---- kappa-weighted P1 Poisson through the generic element loop --------
  * femx/assembly/Assembly.hpp:153-226 with a KappaPoissonP1 element operator

@@ -61,6 +61,8 @@ def lib():
         L.orc_p1_quad_create.restype = C.c_void_p
         L.orc_p1_quad_create.argtypes = [C.c_int, _f64p, C.c_int, _i32p, C.c_int]
         L.orc_p1_quad_free.argtypes = [C.c_void_p]
+        L.orc_p1_quad_tables.argtypes = [C.c_void_p, C.POINTER(C.c_int)] + [
+            C.POINTER(C.c_void_p)] * 3
         L.orc_assemble_p1_kappa.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, C.c_void_p, _f64p, _f64p, _f64p]
         L.orc_vjp_p1_kappa.argtypes = [C.c_void_p, C.c_void_p, _i32p, _f64p, _f64p, _f64p, C.c_void_p, C.c_void_p]
         L.orc_assemble_th_ns.argtypes = [C.c_void_p, C.c_int, _f64p, _i32p, C.c_double, _f64p, _f64p, _f64p]
@@ -208,6 +210,21 @@ class P1Quad:
         if not h:
             raise OracleError(lib().orc_last_error().decode())
         self.h = h
+
+    def tables(self):
+        """(N [nq, 3], dNdx [E, nq, 3, 2], JxW [E, nq]): femx's
+        ElementQuadratureData arrays (copies)."""
+        nq = C.c_int()
+        ptrs = [C.c_void_p() for _ in range(3)]
+        _check(lib().orc_p1_quad_tables(self.h, C.byref(nq), *[C.byref(q) for q in ptrs]))
+        ne, k = self.conn.shape[0], nq.value
+
+        def arr(ptr, shape):
+            n = int(np.prod(shape))
+            buf = (C.c_double * n).from_address(ptr.value)
+            return np.frombuffer(buf, dtype=np.float64, count=n).reshape(shape).copy()
+
+        return arr(ptrs[0], (k, 3)), arr(ptrs[1], (ne, k, 3, 2)), arr(ptrs[2], (ne, k))
 
     def __del__(self):
         if getattr(self, "h", None) and _lib is not None:
