@@ -794,6 +794,7 @@ def main():
                                               "element arithmetic, integer-pipe conversions",
                                               "fp64": "IEEE FP64 element arithmetic",
                                               "fp32_quad": "FP32 element arithmetic"}),
+            "generic_user_operator": generic_user_operator(POISSON_NX),
             "reference_gpu_assembly": dict(ref_bar, **({"speedup": {
                 "plain_fp64": ref_bar["launch_ms"] / (t_asm * 1e3),
                 "tiled_double_float": ref_bar["launch_ms"] / tiled["double_float"]["launch_ms"],
@@ -1073,6 +1074,36 @@ def batch_cpu(sample, e_p1, e_th):
                       f"Taylor-Hood ({n['th']} elements) instances of the batch, residual + "
                       f"Jacobian + VJP (Taylor-Hood VJP as J^T lam), per-element rates "
                       f"applied to the batch's {e_p1} P1 and {e_th} Taylor-Hood elements"}
+
+
+def generic_user_operator(nx):
+    """The header-only user-operator path (include/gbfem/generic_assembly.cuh,
+    femx's evalRow contract) for a P1 Laplacian written as a user functor,
+    against the KappaPoissonP1 tag on the same structured nx x nx mesh: both
+    timed inside one CUDA program (tests/cpp/generic_assembly_test.cu, compiled
+    here with nvcc against libgbfem), zero fill included."""
+    import subprocess
+    import tempfile
+    root = os.path.dirname(os.path.abspath(__file__))
+    try:
+        exe = os.path.join(tempfile.mkdtemp(), "generic_time")
+        subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O2",
+                        "-std=c++17", "-I" + os.path.join(root, "include"),
+                        os.path.join(root, "tests", "cpp", "generic_assembly_test.cu"),
+                        "-L" + os.path.join(root, "femx_gb300"), "-lgbfem",
+                        "-Xlinker", "-rpath," + os.path.join(root, "femx_gb300"), "-o", exe],
+                       check=True, capture_output=True, text=True, timeout=600)
+        out = subprocess.run([exe, "time", str(nx), "20"], check=True, capture_output=True,
+                             text=True, timeout=600).stdout
+        f = out.split("TIME", 1)[1].split()
+        gen, tag, ne = float(f[1]), float(f[3]), int(f[5])
+    except Exception as exc:  # no nvcc, or the program failed
+        return {"unavailable": str(exc).splitlines()[0][:200]}
+    return {"what": "user evalRow functor (P1 Laplacian) through generic_assembly.cuh vs the "
+                    "KappaPoissonP1 tag, FP64, zero fill included",
+            "mesh": f"structured {nx}x{nx}", "elements": ne,
+            "generic_ms": gen, "tag_ms": tag, "generic_elements_per_s": ne / (gen * 1e-3),
+            "tag_speedup": gen / tag}
 
 
 def reference_gpu_bar(torch, timer, args, p, coords, kappa, f, u, amap, pat, v64, r64):

@@ -9,13 +9,16 @@
 // other operator compiles here, in the user's translation unit, into a
 // templated kernel. Header-only, nvcc only; no CPU fallback.
 //
-// Kernel shape: one warp per element (the reference runs one 128-thread
-// block per element, CudaAssembly.hpp:100-214). The warp stages the element
-// inputs in shared memory, each lane evaluates rows lane, lane + 32, ...,
-// and the warp adds the element block into res and the CSR values with FP64
-// atomics through the AssemblyMap (jac_map, femx AssemblyMap.hpp:173-188).
-// Results equal femx's to rounding; FP64 atomics make the order of the
-// additions into one slot run-dependent.
+// Kernel shape: a group of G lanes per element, G the smallest power of two
+// not below the largest element row count (P1: 4 lanes, eight elements per
+// warp; Taylor-Hood and femx's NS element: 16 lanes, two per warp; 32 at
+// most); the reference runs one 128-thread block per element,
+// CudaAssembly.hpp:100-214. A group stages its element's inputs in shared
+// memory, its lanes evaluate rows sub, sub + G, ..., and the group adds the
+// element block into res and the CSR values with FP64 atomics through the
+// AssemblyMap (jac_map, femx AssemblyMap.hpp:173-188). Results equal femx's
+// to rounding; FP64 atomics make the order of the additions into one slot
+// run-dependent.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -70,14 +73,27 @@ namespace detail
 {
 constexpr int kGenericWarps = 4;
 
-/** Per-warp shared-memory staging, in doubles. */
+/** Per-element shared-memory staging, in doubles, and the lane group. */
 struct GenericLayout
 {
-  int in{0};  // element inputs (state + coordinates, or history + next)
-  int res{0}; // max_res
-  int jac{0}; // max_jac
-  __host__ __device__ int per_warp() const { return in + res + jac; }
+  int in{0};    // element inputs (state + coordinates, or history + next)
+  int res{0};   // max_res
+  int jac{0};   // max_jac
+  int group{32}; // lanes per element (a power of two, at most 32)
+  __host__ __device__ int per_elem() const { return in + res + jac; }
+  __host__ __device__ int per_warp() const { return per_elem() * (32 / group); }
 };
+
+/** Lanes per element: the smallest power of two not below max_res. */
+inline int genericGroup(int max_res)
+{
+  int g = 1;
+  while (g < max_res && g < 32)
+  {
+    g *= 2;
+  }
+  return g;
+}
 
 template <class T>
 __device__ __forceinline__ void atomicAddF64(T* addr, T v)
@@ -93,45 +109,49 @@ __global__ void __launch_bounds__(32 * kGenericWarps)
                           Real* __restrict__ vals, GenericLayout lay, int max_state)
 {
   extern __shared__ Real gbfem_generic_work[];
+  const int G    = lay.group;
   const int lane = threadIdx.x & 31;
+  const int sub  = lane & (G - 1);
   const int warp = threadIdx.x >> 5;
-  const int ie   = blockIdx.x * kGenericWarps + warp;
+  const int slot = warp * (32 / G) + lane / G;
+  const int ie   = blockIdx.x * kGenericWarps * (32 / G) + slot;
   if (ie >= map.num_elems)
   {
-    return; // whole warp; no block-level barrier follows
+    return; // no barrier follows: groups synchronise on their own lanes
   }
-  Real*       st = gbfem_generic_work + warp * lay.per_warp();
+  const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~(G - 1));
+  Real*       st = gbfem_generic_work + slot * lay.per_elem();
   Real*       xc = st + max_state;
   Real*       re = st + lay.in;
   Real*       jc = re + lay.res;
   const Index r0 = map.res_offsets[ie], nr = map.res_offsets[ie + 1] - r0;
   const Index s0 = map.state_offsets[ie], nc = map.state_offsets[ie + 1] - s0;
-  for (Index c = lane; c < nc; c += 32)
+  for (Index c = sub; c < nc; c += G)
   {
     st[c] = state[map.state_dofs[s0 + c]];
   }
-  for (Index i = lane; i < npe * dim; i += 32)
+  for (Index i = sub; i < npe * dim; i += G)
   {
     const Index node = conn[static_cast<long long>(ie) * npe + i / dim];
     xc[i]            = coords[static_cast<long long>(node) * dim + i % dim];
   }
-  __syncwarp();
+  __syncwarp(gmask);
   const ElementView ev{ie, dim, npe, {st, nc}, {xc, npe * dim}};
-  for (Index row = lane; row < nr; row += 32)
+  for (Index row = sub; row < nr; row += G)
   {
     Real r = 0.0;
     op.evalRow(ev, row, r, Span<Real>{jc + row * nc, nc});
     re[row] = r;
   }
-  __syncwarp();
-  for (Index row = lane; row < nr; row += 32)
+  __syncwarp(gmask);
+  for (Index row = sub; row < nr; row += G)
   {
     atomicAddF64(res + map.res_dofs[r0 + row], re[row]);
   }
   if (vals != nullptr)
   {
     const Index j0 = map.jac_offsets[ie];
-    for (Index i = lane; i < nr * nc; i += 32)
+    for (Index i = sub; i < nr * nc; i += G)
     {
       atomicAddF64(vals + map.jac_map[j0 + i], jc[i]);
     }
@@ -146,46 +166,50 @@ __global__ void __launch_bounds__(32 * kGenericWarps)
                       Real* __restrict__ vals, GenericLayout lay, int max_state)
 {
   extern __shared__ Real gbfem_generic_work[];
+  const int G    = lay.group;
   const int lane = threadIdx.x & 31;
+  const int sub  = lane & (G - 1);
   const int warp = threadIdx.x >> 5;
-  const int ie   = blockIdx.x * kGenericWarps + warp;
+  const int slot = warp * (32 / G) + lane / G;
+  const int ie   = blockIdx.x * kGenericWarps * (32 / G) + slot;
   if (ie >= map.num_elems)
   {
     return;
   }
-  Real*       hs = gbfem_generic_work + warp * lay.per_warp();
+  const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << (lane & ~(G - 1));
+  Real*       hs = gbfem_generic_work + slot * lay.per_elem();
   Real*       nx = hs + num_hist * max_state;
   Real*       re = hs + lay.in;
   Real*       jc = re + lay.res;
   const Index r0 = map.res_offsets[ie], nr = map.res_offsets[ie + 1] - r0;
   const Index s0 = map.state_offsets[ie], nc = map.state_offsets[ie + 1] - s0;
   // history lag-major with numStates() values per lag (Assembly.hpp:274-282)
-  for (Index i = lane; i < num_hist * nc; i += 32)
+  for (Index i = sub; i < num_hist * nc; i += G)
   {
     const Index lag = i / nc, col = i - lag * nc;
     hs[i] = hist[static_cast<long long>(lag) * map.num_states + map.state_dofs[s0 + col]];
   }
-  for (Index c = lane; c < nc; c += 32)
+  for (Index c = sub; c < nc; c += G)
   {
     nx[c] = nxt[map.state_dofs[s0 + c]];
   }
-  __syncwarp();
+  __syncwarp(gmask);
   const TimeElementView ev{ie, step, num_hist, {hs, num_hist * nc}, {nx, nc}};
-  for (Index row = lane; row < nr; row += 32)
+  for (Index row = sub; row < nr; row += G)
   {
     Real r = 0.0;
     op.evalRow(ev, wrt, row, r, Span<Real>{jc + row * nc, nc});
     re[row] = r;
   }
-  __syncwarp();
-  for (Index row = lane; row < nr; row += 32)
+  __syncwarp(gmask);
+  for (Index row = sub; row < nr; row += G)
   {
     atomicAddF64(res + map.res_dofs[r0 + row], re[row]);
   }
   if (vals != nullptr)
   {
     const Index j0 = map.jac_offsets[ie];
-    for (Index i = lane; i < nr * nc; i += 32)
+    for (Index i = sub; i < nr * nc; i += G)
     {
       atomicAddF64(vals + map.jac_map[j0 + i], jc[i]);
     }
@@ -249,14 +273,15 @@ void assemble(const Op& op, const DeviceGeometry& geom, const DeviceAssemblyMap&
   }
   const auto&           v = map.view();
   detail::GenericLayout lay;
-  lay.in  = v.max_state + geom.nodes_per_elem * geom.dim;
-  lay.res = v.max_res;
-  lay.jac = v.max_jac;
+  lay.in    = v.max_state + geom.nodes_per_elem * geom.dim;
+  lay.res   = v.max_res;
+  lay.jac   = v.max_jac;
+  lay.group = detail::genericGroup(v.max_res);
   size_t         smem    = 0;
   const auto     kernel  = detail::genericAssembleKernel<Op>;
   const unsigned threads = detail::prepareLaunch(kernel, lay, &smem);
-  const unsigned blocks =
-      (static_cast<unsigned>(map.numElems()) + detail::kGenericWarps - 1) / detail::kGenericWarps;
+  const unsigned per_blk = detail::kGenericWarps * (32 / lay.group);
+  const unsigned blocks  = (static_cast<unsigned>(map.numElems()) + per_blk - 1) / per_blk;
   kernel<<<blocks, threads, smem, s>>>(op, geom.dim, geom.nodes_per_elem, geom.coords, geom.conn,
                                        v, state.data(), res.data(), jac.vals, lay, v.max_state);
   detail::cudaCheckApi(cudaGetLastError(), "generic assembly launch");
@@ -304,14 +329,15 @@ void assemble(const Op& op, Index step, Index num_hist, VariableBlock wrt,
   }
   const auto&           v = map.view();
   detail::GenericLayout lay;
-  lay.in  = (num_hist + 1) * v.max_state;
-  lay.res = v.max_res;
-  lay.jac = v.max_jac;
+  lay.in    = (num_hist + 1) * v.max_state;
+  lay.res   = v.max_res;
+  lay.jac   = v.max_jac;
+  lay.group = detail::genericGroup(v.max_res);
   size_t         smem    = 0;
   const auto     kernel  = detail::genericTimeKernel<Op>;
   const unsigned threads = detail::prepareLaunch(kernel, lay, &smem);
-  const unsigned blocks =
-      (static_cast<unsigned>(map.numElems()) + detail::kGenericWarps - 1) / detail::kGenericWarps;
+  const unsigned per_blk = detail::kGenericWarps * (32 / lay.group);
+  const unsigned blocks  = (static_cast<unsigned>(map.numElems()) + per_blk - 1) / per_blk;
   kernel<<<blocks, threads, smem, s>>>(op, step, num_hist, wrt, v, hist.data(), nxt.data(),
                                        res.data(), jac.vals, lay, v.max_state);
   detail::cudaCheckApi(cudaGetLastError(), "generic time assembly launch");

@@ -423,6 +423,80 @@ void navierThroughTheCppLayer(const std::string& dir, Index nn, Index ne, gbfem:
   writeFile(dir + "/ns_vjp.f64", out.host());
   std::printf("NAVIER written\n");
 }
+// Times the user-operator path (PoissonRows through generic_assembly.cuh)
+// against the KappaPoissonP1 tag (FP64) on a structured nx x nx mesh, both
+// with their zero fill, CUDA events on the stream after three warm-ups:
+// prints "TIME generic <ms> tag <ms> elements <E>".
+void timeGenericAgainstTag(int nx, int reps, gbfem::CudaContext& ctx)
+{
+  const Index        nn = (nx + 1) * (nx + 1), ne = 2 * nx * nx;
+  std::vector<Real>  xy(2 * static_cast<size_t>(nn));
+  std::vector<Index> conn(3 * static_cast<size_t>(ne)), offs(ne + 1);
+  for (Index j = 0; j <= nx; ++j)
+  {
+    for (Index i = 0; i <= nx; ++i)
+    {
+      xy[2 * (j * (nx + 1) + i)]     = static_cast<Real>(i) / nx;
+      xy[2 * (j * (nx + 1) + i) + 1] = static_cast<Real>(j) / nx;
+    }
+  }
+  for (Index j = 0; j < nx; ++j)
+  {
+    for (Index i = 0; i < nx; ++i)
+    {
+      const Index a = j * (nx + 1) + i, b = a + 1, c = a + nx + 1, d = c + 1;
+      const Index e = 2 * (j * nx + i);
+      const Index t[6] = {a, b, d, a, d, c};
+      for (int k = 0; k < 6; ++k)
+      {
+        conn[3 * static_cast<size_t>(e) + k] = t[k];
+      }
+    }
+  }
+  for (Index e = 0; e <= ne; ++e)
+  {
+    offs[e] = 3 * e;
+  }
+  Dev<Real>  dxy(xy), du(std::vector<Real>(nn, 1.0)), ones(std::vector<Real>(ne, 1.0));
+  Dev<Index> dconn(conn), doffs(offs);
+  auto map = gbfem::makeAssemblyMap(nn, nn, ne, doffs.p, dconn.p, doffs.p, dconn.p, ctx);
+  const gbfem::DeviceGeometry geom{nn, ne, 3, dxy.p, dconn.p, 2};
+  Dev<Real>              res(nn), vals(map.pattern().nnz);
+  gbfem::DeviceCsrMatrix jac{map.pattern(), vals.p};
+  const auto             s = static_cast<cudaStream_t>(ctx.stream);
+  cudaEvent_t            e0, e1;
+  cuda(cudaEventCreate(&e0), "event");
+  cuda(cudaEventCreate(&e1), "event");
+  float ms[2];
+  for (int which = 0; which < 2; ++which)
+  {
+    auto run = [&] {
+      if (which == 0)
+      {
+        gbfem::assemble(PoissonRows{}, geom, map, du.cview(), res.view(), jac, ctx);
+      }
+      else
+      {
+        gbfem::assemble(gbfem::KappaPoissonP1{ones.p, nullptr, gbfem::Precision::FP64}, geom,
+                        map, du.cview(), res.view(), jac, ctx);
+      }
+    };
+    for (int w = 0; w < 3; ++w)
+    {
+      run();
+    }
+    cuda(cudaEventRecord(e0, s), "event");
+    for (int r = 0; r < reps; ++r)
+    {
+      run();
+    }
+    cuda(cudaEventRecord(e1, s), "event");
+    cuda(cudaEventSynchronize(e1), "event");
+    cuda(cudaEventElapsedTime(&ms[which], e0, e1), "event");
+    ms[which] /= static_cast<float>(reps);
+  }
+  std::printf("TIME generic %.6f tag %.6f elements %d\n", ms[0], ms[1], ne);
+}
 } // namespace
 
 int main(int argc, char** argv)
@@ -432,6 +506,12 @@ int main(int argc, char** argv)
   gbfem::CudaContext ctx{s};
   try
   {
+    if (argc == 4 && std::string(argv[1]) == "time")
+    {
+      timeGenericAgainstTag(std::atoi(argv[2]), std::atoi(argv[3]), ctx);
+      cuda(cudaStreamDestroy(s), "stream");
+      return 0;
+    }
     knownAnswers(ctx);
     if (argc == 5 && std::string(argv[1]) == "navier")
     {
