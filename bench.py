@@ -857,6 +857,8 @@ def main():
             "history_vjp": {"elements_per_s": world * e / t_vjp, "ms": t_vjp * 1e3,
                             "note": "femx computes this with Enzyme; reverse mode by hand here"},
         }
+        entry["reference_gpu_assembly"] = reference_gpu_ns_bar(
+            torch, timer, args, c2, k2, amap, prm, hist, nxt, jac.vals, res, t_asm)
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             from oracle import pyoracle as orc
             om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
@@ -1136,6 +1138,38 @@ def reference_gpu_bar(torch, timer, args, p, coords, kappa, f, u, amap, pat, v64
             "rel_err_vs_fp64_product": {
                 "jacobian": float((vals - v64).abs().max() / v64.abs().max()),
                 "residual": float((res - r64).abs().max() / r64.abs().max())}}
+
+
+def reference_gpu_ns_bar(torch, timer, args, c2, k2, amap, prm, hist, nxt, v_ours, r_ours,
+                         t_ours):
+    """femx's own GPU time assembly of its NS model (assembleTimeKernel with
+    femx's NavierOperator, CudaAssembly.hpp:171-236 and
+    femx/model/ns/Components.hpp:400-577, compiled from femx's sources into
+    oracle/_ref/gpu_bar.cubin), next-state block with its zero fill, on this
+    GPU, against the product's gbfem_assemble_navier on the same data."""
+    from oracle import gpu_bar
+    reason = gpu_bar.unavailable_reason()
+    if reason is not None:
+        return {"unavailable": reason}
+    from oracle import pyoracle as orc
+    view = {k: v.data_ptr() for k, v in amap.view().items()}
+    view.update(num_res=amap.numRes(), num_states=amap.numStates())
+    tables = orc.P1Quad(c2, k2, order=2).tables()
+    rho, mu, dt, step = prm
+    bar = gpu_bar.RefNavierAssembly(torch, tables, view, c2.shape[0], rho, mu, dt)
+    res, vals = torch.zeros_like(r_ours), torch.zeros_like(v_ours)
+    stream = torch.cuda.current_stream().cuda_stream
+    t = timer.run(lambda: bar.assemble(step, hist, nxt, res, vals, stream), args.steps,
+                  args.warmup)
+    bar.assemble(step, hist, nxt, res, vals, stream)
+    torch.cuda.synchronize()
+    return {"what": "femx assembleTimeKernel<NavierOperator> (the reference's CUDA NS "
+                    "assembly), next-state block with its zero fill, on this GPU",
+            "kernel": bar.kernel[:120], "ms": t * 1e3,
+            "elements_per_s": amap.numElems() / t, "ours_speedup": t / t_ours,
+            "rel_err_vs_product": {
+                "jacobian": float((vals - v_ours).abs().max() / v_ours.abs().max()),
+                "residual": float((res - r_ours).abs().max() / r_ours.abs().max())}}
 
 
 def poisson_cpu(p, n, A, asm, bcs, rhs, jac, torch):

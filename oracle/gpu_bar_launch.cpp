@@ -16,8 +16,7 @@
 
 namespace
 {
-CUmodule   g_mod  = nullptr;
-CUfunction g_func = nullptr;
+CUmodule    g_mod = nullptr;
 std::string g_err;
 
 int fail(const char* what, CUresult r)
@@ -34,10 +33,12 @@ extern "C" const char* refbar_last_error()
   return g_err.c_str();
 }
 
-// Loads `cubin` into the current context (the runtime's primary context) and
-// selects the first kernel whose name contains `name_part`; its name is
-// copied to `name_out` (capacity `cap`). 0 on success.
-extern "C" int refbar_load(const char* cubin, const char* name_part, char* name_out, int cap)
+// Loads `cubin` into the current context (the runtime's primary context)
+// once and returns in *func the first kernel whose name contains
+// `name_part`; its name is copied to `name_out` (capacity `cap`). 0 on
+// success.
+extern "C" int refbar_load(const char* cubin, const char* name_part, char* name_out, int cap,
+                           void** func)
 {
   CUresult r = cuInit(0);
   if (r != CUDA_SUCCESS)
@@ -75,7 +76,7 @@ extern "C" int refbar_load(const char* cubin, const char* name_part, char* name_
     if (cuFuncGetName(&name, fs[i]) == CUDA_SUCCESS && name != nullptr
         && std::strstr(name, name_part) != nullptr)
     {
-      g_func = fs[i];
+      *func = fs[i];
       if (name_out != nullptr && cap > 0)
       {
         std::strncpy(name_out, name, static_cast<size_t>(cap) - 1);
@@ -90,10 +91,11 @@ extern "C" int refbar_load(const char* cubin, const char* name_part, char* name_
 
 // Offset and size of kernel parameter `index` (from the module's own
 // parameter table), to cross-check the layout file.
-extern "C" int refbar_param(int index, long long* offset, long long* size)
+extern "C" int refbar_param(void* func, int index, long long* offset, long long* size)
 {
   size_t   o = 0, s = 0;
-  CUresult r = cuFuncGetParamInfo(g_func, static_cast<size_t>(index), &o, &s);
+  CUresult r = cuFuncGetParamInfo(static_cast<CUfunction>(func), static_cast<size_t>(index), &o,
+                                  &s);
   if (r != CUDA_SUCCESS)
   {
     return fail("cuFuncGetParamInfo", r);
@@ -103,16 +105,16 @@ extern "C" int refbar_param(int index, long long* offset, long long* size)
   return 0;
 }
 
-// Launches the selected kernel: `args[i]` points at the bytes of parameter i.
-extern "C" int refbar_launch(void** args, unsigned grid, unsigned block, unsigned smem,
-                             void* stream)
+// Launches `func`: `args[i]` points at the bytes of parameter i.
+extern "C" int refbar_launch(void* func, void** args, unsigned grid, unsigned block,
+                             unsigned smem, void* stream)
 {
-  if (g_func == nullptr)
+  if (func == nullptr)
   {
     g_err = "no kernel loaded";
     return 1;
   }
-  const CUresult r = cuLaunchKernel(g_func, grid, 1, 1, block, 1, 1, smem,
+  const CUresult r = cuLaunchKernel(static_cast<CUfunction>(func), grid, 1, 1, block, 1, 1, smem,
                                     static_cast<CUstream>(stream), args, nullptr);
   return r == CUDA_SUCCESS ? 0 : fail("cuLaunchKernel", r);
 }

@@ -15,6 +15,10 @@
 //     locating the sentinels in the object bytes; the launcher fills the
 //     same offsets with real device addresses and sizes.
 //
+// A second instantiation is femx's own NS time assembly: assembleTimeKernel
+// (CudaAssembly.hpp:171-236) with femx's NavierOperator<Device>
+// (femx/model/ns/Components.hpp:400-577), the operator of femx's NS model.
+//
 // The operator follows femx's Poisson example (examples/poisson/
 // PoissonComponents.hpp:35-64, quadrature over ElementQuadratureData) with
 // the per-element coefficient and the load of the oracle's KappaPoissonP1:
@@ -23,6 +27,7 @@
 #include <femx/assembly/CudaAssembly.hpp>
 #include <femx/fem/ElementQuadratureData.hpp>
 #include <femx/fem/Geometry.hpp>
+#include <femx/model/ns/Components.hpp>
 
 #ifdef REFBAR_LAYOUT
 #include <cstdint>
@@ -91,6 +96,11 @@ template __global__ void femx::assembly::detail::assembleKernel<refbar::KappaPoi
     refbar::KappaPoissonP1Dev, femx::fem::GeometryView<femx::MemorySpace::Device>,
     femx::assembly::AssemblyMapView<femx::MemorySpace::Device>, const femx::Real*,
     femx::Real*, femx::Real*);
+template __global__ void femx::assembly::detail::assembleTimeKernel<
+    femx::model::ns::NavierOperator<femx::MemorySpace::Device>>(
+    femx::model::ns::NavierOperator<femx::MemorySpace::Device>, femx::Index, femx::Index,
+    femx::state::VariableBlock, femx::assembly::AssemblyMapView<femx::MemorySpace::Device>,
+    const femx::Real*, const femx::Real*, femx::Real*, femx::Real*);
 #else
 namespace
 {
@@ -104,23 +114,43 @@ int sentI(int k)
   return 0x3c3c0000 | (k << 4) | 0x7;
 }
 
+// an 8-byte sentinel for a double field: the bit pattern of a finite double
+double sentD(int k)
+{
+  const std::uint64_t u = 0x4b4b000000000000ull | (std::uint64_t(k) << 8) | 0x33u;
+  double              d;
+  std::memcpy(&d, &u, 8);
+  return d;
+}
+
 template <class T>
 void dump(const char* param, const T& obj, int nfields, const char* const* names,
-          const bool* is_ptr, bool last)
+          const bool* is_ptr, bool last, const bool* is_dbl = nullptr)
 {
   unsigned char b[sizeof(T)];
   std::memcpy(b, &obj, sizeof(T));
   std::printf("  \"%s\": {\"size\": %zu, \"fields\": {", param, sizeof(T));
   for (int k = 0; k < nfields; ++k)
   {
-    long off = -1;
-    for (size_t o = 0; o + (is_ptr[k] ? 8 : 4) <= sizeof(T); o += 4)
+    long       off  = -1;
+    const bool dbl  = is_dbl != nullptr && is_dbl[k];
+    const bool wide = is_ptr[k] || dbl;
+    for (size_t o = 0; o + (wide ? 8 : 4) <= sizeof(T); o += 4)
     {
-      if (is_ptr[k])
+      if (wide)
       {
-        std::uint64_t v;
+        std::uint64_t v, want;
         std::memcpy(&v, b + o, 8);
-        if (v == sentP(k))
+        if (dbl)
+        {
+          const double d = sentD(k);
+          std::memcpy(&want, &d, 8);
+        }
+        else
+        {
+          want = sentP(k);
+        }
+        if (v == want)
         {
           off = long(o);
           break;
@@ -142,7 +172,8 @@ void dump(const char* param, const T& obj, int nfields, const char* const* names
       std::fprintf(stderr, "field %s of %s not found\n", names[k], param);
       std::exit(1);
     }
-    std::printf("%s\"%s\": [%ld, %d]", k ? ", " : "", names[k], off, is_ptr[k] ? 8 : 4);
+    std::printf("%s\"%s\": [%ld, %d%s]", k ? ", " : "", names[k], off, wide ? 8 : 4,
+                dbl ? ", \"f64\"" : "");
   }
   std::printf("}}%s\n", last ? "" : ",");
 }
@@ -207,7 +238,31 @@ int main()
                        "g_elem_offsets", "g_elem_offsets_size", "g_conn", "g_conn_size",
                        "kappa",       "f"};
     const bool  p[] = {0, 0, 0, 0, 1, 0, 1, 0, 1, 0, 0, 0, 0, 0, 1, 0, 1, 0, 1, 0, 1, 1};
-    dump("op", op, 22, n, p, true);
+    dump("op", op, 22, n, p, false);
+  }
+  {
+    using Nav = model::ns::NavierOperator<MemorySpace::Device>;
+    const Nav op(model::ns::NavierDataView<MemorySpace::Device>(
+                     sentI(0), sentI(1), sentI(2), sentI(3), vview<CR>(4, 5), vview<CR>(6, 7),
+                     vview<CR>(8, 9)),
+                 model::ns::KernelFluid{sentD(10), sentD(11)}, sentD(12));
+    const char* n[] = {"num_elems", "num_qpts", "num_nodes", "dim",  "N",   "N_size", "dNdx",
+                       "dNdx_size", "JxW",      "JxW_size",  "rho",  "mu",  "dt"};
+    const bool  p[] = {0, 0, 0, 0, 1, 0, 1, 0, 1, 0, 0, 0, 0};
+    const bool  d[] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1};
+    dump("navier_op", op, 13, n, p, false, d);
+  }
+  {
+    // the Jacobian block of femx's next-state assembly, as bytes
+    const state::VariableBlock w = state::VariableBlock::NextState;
+    unsigned char              b[sizeof(w)];
+    std::memcpy(b, &w, sizeof(w));
+    std::printf("  \"wrt_next\": [");
+    for (size_t i = 0; i < sizeof(w); ++i)
+    {
+      std::printf("%s%d", i ? ", " : "", b[i]);
+    }
+    std::printf("]\n");
   }
   std::printf("}\n");
   return 0;
