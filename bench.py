@@ -523,6 +523,22 @@ def main():
         t64, gu64, gm64 = res_v["fp64"]
         t32, gu32, gm32 = res_v["fp32_quad"]
         b_vjp = 28 * e + 40 * n
+        # the tiled residual VJPs (g_u row by row, g_m by each element's owner
+        # tile: no atomics, no zero fill), FP64-accurate
+        amap.enableTiles(coords)
+        vjp_tiled = {}
+        for prec in ("double_float", "fp64"):
+            tt = maxrank(timer.run(lambda: A.vjpP1Kappa(amap, coords, kappa, u, lam, g_u, g_m,
+                                                         precision=prec, tiled=True),
+                                   args.steps, args.warmup))
+            vjp_tiled[prec] = {
+                "ms_per_grad": tt * 1e3, "grads_per_s": 1.0 / tt,
+                "roofline": {"bound": "hbm", "achieved": b_vjp / tt / 1e9, "peak": hbm,
+                             "unit": "GB/s", "frac": b_vjp / tt / 1e9 / hbm},
+                "rel_err_vs_fp64_vjp": {
+                    "g_u": float((g_u - gu64).abs().max() / gu64.abs().max()),
+                    "g_m": float((g_m - gm64).abs().max() / gm64.abs().max())}}
+        launches += 2 * args.steps
         # Central differences of the FP64 residual (h = 1e-6) against the
         # FP32-quadrature VJP along 32 seeded unit directions in m and in u.
         from femx_gb300.autograd import p1_kappa_residual
@@ -610,6 +626,7 @@ def main():
             "grads_per_s": world / t32, "grads_per_s_fp64": world / t64,
             "ms_per_grad": t32 * 1e3, "ms_per_grad_fp64": t64 * 1e3,
             "elements": e,
+            "tiled": vjp_tiled,
             "rel_err_fp32_vs_fp64": {
                 "g_u": float((gu32 - gu64).abs().max() / gu64.abs().max()),
                 "g_m": float((gm32 - gm64).abs().max() / gm64.abs().max())},

@@ -354,7 +354,7 @@ def assembleP1Kappa(amap: AssemblyMap, coords, kappa, f_nodal, u, res, jac=None,
 
 
 def vjpP1Kappa(amap: AssemblyMap, coords, kappa, u, lam, g_u=None, g_m=None, conn=None,
-               precision: str = "fp64", coloured: bool = False):
+               precision: str = "fp64", coloured: bool = False, tiled: bool = False):
     coords = _dev(coords, torch.float64, "coords")
     kappa = _check_vec(kappa, amap.numElems(), "kappa")
     u = _check_vec(u, amap.numStates(), "state")
@@ -365,7 +365,8 @@ def vjpP1Kappa(amap: AssemblyMap, coords, kappa, u, lam, g_u=None, g_m=None, con
         g_m = _check_vec(g_m, amap.numElems(), "control gradient")
     conn = _dev(conn, torch.int32, "conn", allow_none=True)
     call("gbfem_vjp_p1_kappa", amap.handle, coords.shape[0], _ptr(coords), _ptr(conn),
-         _ptr(kappa), _ptr(u), _ptr(lam), _ptr(g_u), _ptr(g_m), _mode(precision, coloured),
+         _ptr(kappa), _ptr(u), _ptr(lam), _ptr(g_u), _ptr(g_m),
+         _mode(precision, coloured, tiled=tiled),
          _stream())
 
 

@@ -97,7 +97,9 @@ struct gbfem_assembly_map
   //                                 sentinel {0, rows, 0, slots} (tile_runs)
   //   tile_elem_off[t] .. [t + 1]   elements (tile_elems, ascending) and
   //                                 their vertices as tile-local indices,
-  //                                 three 10-bit fields (tile_conn)
+  //                                 three 10-bit fields (tile_conn; bit 30:
+  //                                 the tile owns the element, i.e. the row
+  //                                 of its first vertex)
   //   tile_vert_off[t] .. [t + 1]   tile vertices: DOF and geometry node
   //   slot_ref[s]                   CSR slot s of an owned row (r, c), c != r:
   //                                 the one or two element edges joining r

@@ -268,11 +268,57 @@ extern "C" int gbfem_vjp_p1_kappa(const gbfem_assembly_map* map, int num_nodes,
     require(lam != nullptr, "VJP adjoint input is null");
     require(g_u != lam && g_u != u && g_m != lam && g_m != u,
             "VJP outputs must not alias inputs");
-    require((precision & GBFEM_TILED) == 0, "the P1 VJP has no tiled form");
-    const bool col = (precision & GBFEM_COLOURED) != 0;
-    precision &= ~GBFEM_COLOURED;
+    const bool col   = (precision & GBFEM_COLOURED) != 0;
+    const bool tiled = (precision & GBFEM_TILED) != 0;
+    precision &= ~(GBFEM_COLOURED | GBFEM_TILED);
     require(precision >= GBFEM_PREC_FP64 && precision <= GBFEM_PREC_DOUBLE_FLOAT,
             "unknown precision mode");
+    if (tiled)
+    {
+      require(!col, "tiled and coloured assembly are exclusive");
+      require(precision != GBFEM_PREC_MIXED,
+              "tiled assembly runs in FP64, FP32_QUAD or DOUBLE_FLOAT");
+      require(map->tile_row_off != nullptr,
+              "tiled assembly needs gbfem_assembly_map_enable_tiles on the map");
+      require((conn != nullptr) == map->tile_sep_conn,
+              "tiled assembly: pass the geometry connectivity exactly when the tiles were "
+              "built with it");
+      P1TileArgs t{};
+      t.row_off   = map->tile_row_off;
+      t.row_info  = map->tile_row_info;
+      t.run_off   = map->tile_run_off;
+      t.runs      = map->tile_runs;
+      t.elem_off  = map->tile_elem_off;
+      t.elems     = map->tile_elems;
+      t.tconn     = map->tile_conn;
+      t.vert_off  = map->tile_vert_off;
+      t.vert_dof  = map->tile_vert_dof;
+      t.vert_node = map->tile_vert_node;
+      t.slot_ref  = map->slot_ref;
+      t.coords    = a.coords;
+      t.kappa     = kappa;
+      t.u         = lam;
+      t.u_state   = u;
+      t.res       = g_u;
+      t.g_m       = g_m;
+      t.status    = map->status;
+      // FP32 element gradients would put ~1e-7 relative noise on every g_m[e],
+      // which directional derivatives over many elements amplify: the tiled
+      // VJP runs FP64-accurate only
+      require(precision == GBFEM_PREC_DOUBLE_FLOAT || precision == GBFEM_PREC_FP64,
+              "the tiled P1 VJP runs in FP64 or DOUBLE_FLOAT");
+      cudaStream_t s = asStream(stream);
+      if (precision == GBFEM_PREC_DOUBLE_FLOAT)
+      {
+        launchP1Tiled<Dd, false, false, true>(t, map, s);
+      }
+      else
+      {
+        launchP1Tiled<double, false, false, true>(t, map, s);
+      }
+      cudaCheck(cudaGetLastError(), "tiled P1 VJP launch");
+      return;
+    }
     require(!col || map->num_elems == 0 || map->colour_elems != nullptr,
             "coloured assembly needs gbfem_assembly_map_enable_colouring on the map");
     cudaStream_t s = asStream(stream);

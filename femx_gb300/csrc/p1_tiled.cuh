@@ -66,6 +66,8 @@ struct P1TileArgs
   const double*        u;
   double*              res;
   double*              vals;
+  const double*        u_state; // residual VJP: the state (u is then the adjoint)
+  double*              g_m;     // residual VJP: per-element control gradient
   gbfem::DeviceStatus* status;
 };
 
@@ -348,13 +350,19 @@ constexpr int tileMinBlocks()
   return std::is_same<T, Dd>::value ? 5 : (std::is_same<T, float>::value ? 6 : 3);
 }
 
-template <class T, bool kLoad, bool kJac>
+// kVjp: the residual VJPs instead (no load, no Jacobian): u holds the
+// adjoint lambda, u_state the state; the row phase sums (K lambda)_r into
+// res (= g_u) and each element's owner tile writes g_m[e] = lambda_e^T K_e
+// u_e = -sum over its edges of K_ab (lambda_a - lambda_b)(u_a - u_b).
+template <class T, bool kLoad, bool kJac, bool kVjp = false>
 __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
     p1TiledKernel(P1TileArgs a, int max_verts, int max_elems, int max_slots, int max_runs)
 {
-  constexpr bool kStage = tileStaged<T>();
+  static_assert(!kVjp || (!kLoad && !kJac), "the VJP form has no load and no Jacobian");
+  constexpr bool kStage  = tileStaged<T>();
+  constexpr bool kSecond = kLoad || kVjp; // a second staged vertex field
   extern __shared__ __align__(16) unsigned char smem[];
-  const TileSmem<T> L(max_verts, max_elems, max_slots, kTileThreads, max_runs, kLoad);
+  const TileSmem<T> L(max_verts, max_elems, max_slots, kTileThreads, max_runs, kSecond);
   VertXY<T>*        sx = reinterpret_cast<VertXY<T>*>(smem + L.xy);
   T*                su = reinterpret_cast<T*>(smem + L.u);
   T*                sf = reinterpret_cast<T*>(smem + L.f);
@@ -387,13 +395,15 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
     w[k] = row.y + k < row.z ? a.slot_ref[row.y + k] : 0u;
   }
   unsigned ec[2];
+  int      eg[2];
   double   ek[2];
 #pragma unroll
   for (int h = 0; h < 2; ++h)
   {
     const int l = i + h * kTileThreads;
     ec[h]       = l < nel ? a.tconn[e0 + l] : 0u;
-    ek[h]       = l < nel ? a.kappa[a.elems[e0 + l]] : 0.0;
+    eg[h]       = l < nel ? a.elems[e0 + l] : 0;
+    ek[h]       = l < nel ? a.kappa[eg[h]] : 0.0;
   }
   const int4 run = kStage && i < nq ? a.runs[q0 + i] : make_int4(0, 0, 0, 0);
 
@@ -407,6 +417,10 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
     if (kLoad)
     {
       sf[j] = tSplit<T>(a.f[n]);
+    }
+    if (kVjp)
+    {
+      sf[j] = tSplit<T>(a.u_state[d]);
     }
   }
   if (kStage && i < nq)
@@ -425,7 +439,7 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
       break;
     }
     const unsigned c  = ec[h];
-    const int      i0 = c & 1023u, i1 = (c >> 10) & 1023u, i2 = c >> 20;
+    const int      i0 = c & 1023u, i1 = (c >> 10) & 1023u, i2 = (c >> 20) & 1023u;
     T              ax, ay, bx, by;
     edge<T>(sx[i0], sx[i1], ax, ay);
     edge<T>(sx[i0], sx[i2], bx, by);
@@ -433,7 +447,7 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
     T       adet = tAbs(det);
     if (!(tLead(adet) >= 1.0e-30f))
     {
-      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, a.elems[e0 + l]);
+      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, eg[h]);
       adet = T(1);
     }
     const T s   = tScale(tSplit<T>(ek[h]) * tRcp(adet), 0.5f);
@@ -453,6 +467,12 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
       rr1 -= cf * (f1 + fs);
       rr2 -= cf * (f2 + fs);
     }
+    if (kVjp && (c & 0x40000000u) && a.g_m != nullptr)
+    {
+      // this tile owns the element (its first vertex's row)
+      const T w0 = sf[i0], w1 = sf[i1], w2 = sf[i2];
+      a.g_m[eg[h]] = tJoin(-(P * (w1 - w0) + Q * (w2 - w0) + R * (w2 - w1)));
+    }
     se[3 * l + 0] = EdgeRec<T>{k12, rr1};
     se[3 * l + 1] = EdgeRec<T>{k02, rr2};
     se[3 * l + 2] = EdgeRec<T>{k01, rr0};
@@ -460,7 +480,7 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
   __syncthreads();
 
   // 2. rows, staged in shared memory
-  if (i < nr)
+  if (i < nr && (!kVjp || a.res != nullptr))
   {
     T    off = T(0), res = T(0);
     int  dk  = -1;
@@ -558,20 +578,20 @@ __global__ void __launch_bounds__(kTileThreads, tileMinBlocks<T>())
 }
 
 // Launch over all tiles of the map (gbfem_assembly_map_enable_tiles).
-template <class T, bool kLoad, bool kJac>
+template <class T, bool kLoad, bool kJac, bool kVjp = false>
 void launchP1Tiled(const P1TileArgs& a, const gbfem_assembly_map* m, cudaStream_t s)
 {
   const TileSmem<T> L(m->tile_max_verts, m->tile_max_elems, m->tile_max_slots, kTileThreads,
-                      m->tile_max_runs, kLoad);
+                      m->tile_max_runs, kLoad || kVjp);
   if (L.total > 48 * 1024)
   {
-    gbfem::cudaCheck(cudaFuncSetAttribute(p1TiledKernel<T, kLoad, kJac>,
+    gbfem::cudaCheck(cudaFuncSetAttribute(p1TiledKernel<T, kLoad, kJac, kVjp>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, L.total),
                      "tiled assembly shared memory");
   }
   if (m->num_tiles > 0)
   {
-    p1TiledKernel<T, kLoad, kJac><<<m->num_tiles, kTileThreads, L.total, s>>>(
+    p1TiledKernel<T, kLoad, kJac, kVjp><<<m->num_tiles, kTileThreads, L.total, s>>>(
         a, m->tile_max_verts, m->tile_max_elems, m->tile_max_slots, m->tile_max_runs);
   }
 }

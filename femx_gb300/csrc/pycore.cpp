@@ -665,7 +665,8 @@ PYBIND11_MODULE(_core, m)
       "vjp_p1_kappa",
       [](const AssemblyMap& a, const py::object& coords, const py::object& kappa,
          const py::object& u, const py::object& lam, const py::object& g_u,
-         const py::object& g_m, const py::object& conn, const std::string& precision) {
+         const py::object& g_m, const py::object& conn, const std::string& precision,
+         bool tiled) {
         const long long nn = numNodes(coords);
         const double*   xy = f64(coords, -1, "coords");
         const double*   kp = f64(kappa, a.v.num_elems, "kappa");
@@ -674,14 +675,14 @@ PYBIND11_MODULE(_core, m)
         double*         gu = f64(g_u, a.v.num_states, "g_u", true);
         double*         gm = f64(g_m, a.v.num_elems, "g_m", true);
         const int*      k  = i32(conn, 3LL * a.v.num_elems, "conn", true);
-        const int       mode = precisionMode(precision);
+        const int       mode = precisionMode(precision) | (tiled ? GBFEM_TILED : 0);
         void*           s    = currentStream();
         call([&] {
           return gbfem_vjp_p1_kappa(a.h, static_cast<int>(nn), xy, k, kp, x, l, gu, gm, mode, s);
         });
       },
       "assembly_map"_a, "coords"_a, "kappa"_a, "u"_a, "lam"_a, "g_u"_a = py::none(),
-      "g_m"_a = py::none(), "conn"_a = py::none(), "precision"_a = "fp64");
+      "g_m"_a = py::none(), "conn"_a = py::none(), "precision"_a = "fp64", "tiled"_a = false);
 
   // the Taylor-Hood P2/P1 Newton residual and Jacobian
   m.def(

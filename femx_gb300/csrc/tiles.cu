@@ -188,9 +188,12 @@ Tiles buildTiles(int ne, int nrows, const std::vector<int>& dofs,
     {
       const int* d = &dofs[3 * static_cast<size_t>(e)];
       T.elems.push_back(e);
+      // bit 30: this tile owns the element (the row of its first vertex),
+      // the one tile that writes per-element outputs
       T.conn.push_back(static_cast<unsigned>(vloc[d[0]])
                        | (static_cast<unsigned>(vloc[d[1]]) << 10)
-                       | (static_cast<unsigned>(vloc[d[2]]) << 20));
+                       | (static_cast<unsigned>(vloc[d[2]]) << 20)
+                       | (owner[d[0]] == t ? 0x40000000u : 0u));
     }
     T.max_rows  = std::max(T.max_rows, static_cast<int>(cur_rows.size()));
     T.max_elems = std::max(T.max_elems, static_cast<int>(cur_elems.size()));

@@ -71,7 +71,9 @@ extern "C" {
  * DOUBLE_FLOAT it is the FP64-accurate fast assembly: the element
  * arithmetic and every conversion run on the FP32 and integer pipes, FP64
  * instructions only form the coordinate differences. */
-#define GBFEM_TILED 0x400
+#define GBFEM_TILED 0x400 /* also for gbfem_vjp_p1_kappa (FP64 or DOUBLE_FLOAT): g_u
+                           * summed row by row, g_m written by each element's
+                           * owner tile, no atomics, no zero fill */
 
 GBFEM_API const char* gbfem_last_error(void);
 GBFEM_API int         gbfem_version(void);
