@@ -299,3 +299,29 @@ def test_tiled_vjp_refuses_fp32():
     with pytest.raises(_lib.GbfemError, match="FP64 or DOUBLE_FLOAT"):
         A.vjpP1Kappa(amap, dev(coords), dev(np.ones(e)), dev(np.zeros(n)), dev(np.zeros(n)), g,
                      None, precision="fp32_quad", tiled=True)
+
+
+def fan(nt):
+    """nt triangles around node 0 (a closed fan: a valid conforming mesh)."""
+    ang = 2 * np.pi * np.arange(nt) / nt
+    coords = np.vstack([[0.0, 0.0], np.stack([np.cos(ang), np.sin(ang)], 1)])
+    conn = np.array([[0, 1 + i, 1 + (i + 1) % nt] for i in range(nt)], dtype=np.int32)
+    return coords, conn
+
+
+def test_tiled_high_valence_row_fits_and_matches_oracle():
+    """A row with 300 incident elements (one tile holds up to 512): the row's
+    300 slots and its neighbours' are all written, against the oracle."""
+    coords, conn = fan(300)
+    p = setup(coords, conn, 5)
+    res, vals = run(p, "double_float")
+    assert rel_inf(vals, p["rvals"]) <= 1e-12 and rel_inf(res, p["rres"]) <= 1e-12
+
+
+def test_tiled_refuses_a_row_larger_than_a_tile():
+    coords, conn = fan(600)
+    n = coords.shape[0]
+    offs, dofs = meshes.scalar_elem_dofs(conn)
+    amap = A.makeAssemblyMap(n, n, dev(offs), dev(dofs), dev(offs), dev(dofs))
+    with pytest.raises(_lib.GbfemError, match="more elements than a tile holds"):
+        amap.enableTiles(dev(coords))
