@@ -25,14 +25,16 @@ __all__ = ["P1KappaResidual", "p1_kappa_residual", "TaylorHoodResidual",
 
 class P1KappaResidual(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, u, m, amap, coords, f, bc, bc_vals, precision):
+    def forward(ctx, u, m, amap, coords, f, bc, bc_vals, precision, tiled=False):
         kappa = torch.exp(m)
         res = torch.empty(amap.numRes(), dtype=torch.float64, device=u.device)
-        A.assembleP1Kappa(amap, coords, kappa, f, u, res, None, precision=precision)
+        A.assembleP1Kappa(amap, coords, kappa, f, u, res, None, precision=precision,
+                          tiled=tiled)
         if bc is not None:
             A.replaceRes(bc, u, bc_vals, res)
         ctx.save_for_backward(u, kappa)
         ctx.amap, ctx.coords, ctx.bc, ctx.precision = amap, coords, bc, precision
+        ctx.tiled = tiled
         return res
 
     @staticmethod
@@ -47,17 +49,20 @@ class P1KappaResidual(torch.autograd.Function):
         g_m = torch.empty_like(kappa) if ctx.needs_input_grad[1] else None
         if g_u is not None or g_m is not None:
             A.vjpP1Kappa(ctx.amap, ctx.coords, kappa, u, lam_t, g_u, g_m,
-                         precision=ctx.precision)
+                         precision=ctx.precision, tiled=ctx.tiled)
         if g_u is not None and ctx.bc is not None:
             rows = ctx.bc.view()["bc_rows"].long()
             g_u.index_add_(0, rows, lam.index_select(0, rows))
-        return g_u, g_m, None, None, None, None, None, None
+        return g_u, g_m, None, None, None, None, None, None, None
 
 
 def p1_kappa_residual(u, m, amap, coords, f=None, bc=None, bc_vals=None,
-                      precision: str = "fp64"):
-    """R(u, m) as a differentiable function of the state u and the control m."""
-    return P1KappaResidual.apply(u, m, amap, coords, f, bc, bc_vals, precision)
+                      precision: str = "fp64", tiled: bool = False):
+    """R(u, m) as a differentiable function of the state u and the control m.
+    tiled=True (amap.enableTiles(coords) first; precision "fp64" or
+    "double_float"): the owner-computes tiled residual and VJPs, no atomics,
+    bitwise reproducible forward and backward."""
+    return P1KappaResidual.apply(u, m, amap, coords, f, bc, bc_vals, precision, tiled)
 
 
 class TaylorHoodResidual(torch.autograd.Function):

@@ -285,3 +285,35 @@ def test_taylor_hood_gradcheck_small():
     assert torch.autograd.gradcheck(
         lambda ss, nn: taylor_hood_residual(ss, nn, amap, coords_d, c6, bc, g), (s, nu),
         eps=1e-6, atol=1e-8, rtol=1e-6, nondet_tol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "double_float"])
+def test_tiled_autograd_gradcheck_and_reproducible(precision):
+    """The tiled residual and VJPs behind the autograd function: gradcheck
+    against its own finite differences (with no atomics the forward is
+    deterministic, so nondet_tol is 0), backward bitwise equal over runs,
+    and equal to the atomic FP64 path's gradients to rounding."""
+    coords, conn, amap, bc, bdofs = setup(6, 4)
+    rng = np.random.default_rng(4)
+    n, e = coords.shape[0], conn.shape[0]
+    coords_d, f_d = dev(coords), dev(meshes.fourier_source(coords, 3))
+    amap.enableTiles(coords_d)
+    g = dev(rng.standard_normal(len(bdofs)))
+    u0, m0 = rng.standard_normal(n), 0.3 * rng.standard_normal(e)
+    u = dev(u0).requires_grad_()
+    m = dev(m0).requires_grad_()
+    assert torch.autograd.gradcheck(
+        lambda uu, mm: p1_kappa_residual(uu, mm, amap, coords_d, f_d, bc, g,
+                                         precision=precision, tiled=True), (u, m),
+        eps=1e-6, atol=1e-8, rtol=1e-6, nondet_tol=0.0)
+    lam = dev(rng.standard_normal(n))
+    grads = []
+    for tiled in (True, True, False):
+        uu, mm = dev(u0).requires_grad_(), dev(m0).requires_grad_()
+        r = p1_kappa_residual(uu, mm, amap, coords_d, f_d, bc, g,
+                              precision=precision if tiled else "fp64", tiled=tiled)
+        (r * lam).sum().backward()
+        grads.append((uu.grad.cpu().numpy(), mm.grad.cpu().numpy()))
+    assert np.array_equal(grads[0][0], grads[1][0]) and np.array_equal(grads[0][1], grads[1][1])
+    assert rel_inf(grads[0][0], grads[2][0]) <= 1e-13
+    assert rel_inf(grads[0][1], grads[2][1]) <= 1e-13
