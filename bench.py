@@ -462,7 +462,7 @@ def main():
                 "e2e": {"value": world * e / t_e2e_df, "ms_per_step": t_e2e_df * 1e3},
                 "rel_err_vs_oracle_full_size": {"jacobian": err_df_v, "residual": err_df_r,
                                                 "gate": 1e-12},
-                "kernel": "thKernelDd<true>", "launch_ms": t_kern_df * 1e3,
+                "kernel": "thElemKernelDd<false>", "launch_ms": t_kern_df * 1e3,
                 "roofline": {"bound": "hbm", "achieved": b_th / t_kern_df / 1e9, "peak": hbm,
                              "unit": "GB/s", "frac": b_th / t_kern_df / 1e9 / hbm},
                 "precision": "FP64-accurate: element arithmetic in double-float (float "

@@ -209,10 +209,11 @@ struct SideStream
 };
 SideStream& sideStream(); // this thread's, ensured for the current device
 
-// A launch as a dependent (dependent = true) or an ordinary one.
+// A launch as a dependent (dependent = true) or an ordinary one, with
+// `smem` bytes of dynamic shared memory.
 template <class... P, class... A>
-void launchMaybeDependent(bool dependent, void (*kernel)(P...), unsigned grid, unsigned block,
-                          cudaStream_t s, A&&... args)
+void launchMaybeDependentSmem(bool dependent, void (*kernel)(P...), unsigned grid,
+                              unsigned block, unsigned smem, cudaStream_t s, A&&... args)
 {
   cudaLaunchConfig_t  cfg{};
   cudaLaunchAttribute attr[1];
@@ -220,11 +221,18 @@ void launchMaybeDependent(bool dependent, void (*kernel)(P...), unsigned grid, u
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.gridDim                                        = dim3(grid);
   cfg.blockDim                                       = dim3(block);
-  cfg.dynamicSmemBytes                               = 0;
+  cfg.dynamicSmemBytes                               = smem;
   cfg.stream                                         = s;
   cfg.attrs                                          = attr;
   cfg.numAttrs                                       = dependent ? 1 : 0;
   cudaCheck(cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...), "kernel launch");
+}
+
+template <class... P, class... A>
+void launchMaybeDependent(bool dependent, void (*kernel)(P...), unsigned grid, unsigned block,
+                          cudaStream_t s, A&&... args)
+{
+  launchMaybeDependentSmem(dependent, kernel, grid, block, 0u, s, static_cast<A&&>(args)...);
 }
 
 template <class... P, class... A>

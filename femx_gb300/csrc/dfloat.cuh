@@ -261,7 +261,7 @@ __device__ __forceinline__ Dd ddSplitInt(double x)
 // is counted in those units. Faithful (within one unit of the last FP64
 // place) for |hi| >= 2^-103; below that lo is dropped (the result is hi).
 // Zero and subnormal hi give 0; an infinite or NaN hi is widened as it is.
-__device__ __forceinline__ double ddJoinInt(Dd v)
+static __device__ __noinline__ double ddJoinIntWide(Dd v)
 {
   const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
   const unsigned ha = hb & 0x7fffffffu, la = lb & 0x7fffffffu;
@@ -285,6 +285,36 @@ __device__ __forceinline__ double ddJoinInt(Dd v)
   const unsigned long long bits =
       eh != 0u ? (w | (static_cast<unsigned long long>(hb & 0x80000000u) << 32)) : 0ull;
   return __longlong_as_double(static_cast<long long>(bits));
+}
+
+// The same conversion with fewer integer operations for 2^-74 <= |hi| <
+// 2^126 (every other hi takes ddJoinIntWide): lo times sign(hi) is scaled by
+// a power of two into units of the last FP64 place of hi (of the binade
+// below when hi is a power of two and lo has the other sign), exactly, and
+// truncated to an integer (|t| < 2^30) by one float-to-integer conversion;
+// that count is added to hi's widened bit pattern. hi + lo stays inside that
+// binade (|lo| <= ulp(hi)/2), so the result is faithful: it lies between
+// hi + lo and hi, within one unit of the last FP64 place of hi + lo.
+__device__ __forceinline__ double ddJoinInt(Dd v)
+{
+  const unsigned hb = __float_as_uint(v.hi);
+  const unsigned ha = hb & 0x7fffffffu;
+  const unsigned eh = ha >> 23;
+  if (eh - 53u > 199u)
+  {
+    return ddJoinIntWide(v);
+  }
+  const unsigned sg = hb & 0x80000000u;
+  const unsigned dn =
+      ((ha & 0x7fffffu) == 0u && ((hb ^ __float_as_uint(v.lo)) & 0x80000000u) != 0u) ? 1u : 0u;
+  // 2^(52 - E + dn) sign(hi), E = eh - 127 the exponent of hi
+  const float              scale = __uint_as_float(((306u + dn - eh) << 23) | sg);
+  const int                t     = __float2int_rz(__fmul_rn(v.lo, scale));
+  const unsigned long long w =
+      (static_cast<unsigned long long>((ha >> 3) + 0x38000000u) << 32) | (ha << 29);
+  const unsigned long long m = w + static_cast<unsigned long long>(static_cast<long long>(t));
+  return __longlong_as_double(
+      static_cast<long long>(m | (static_cast<unsigned long long>(sg) << 32)));
 }
 
 // 1/x in double-float: a float reciprocal refined by one Newton step,

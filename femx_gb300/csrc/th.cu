@@ -27,6 +27,8 @@
 // row as one record instead and a row pass (gather.cuh) sums each CSR row's
 // records in element order — no atomics, no zero-fill, bitwise
 // reproducible, about 1.5x the time of the atomic path.
+#include <atomic>
+
 #include "gather.cuh"
 #include "th_elem.cuh"
 
@@ -289,6 +291,339 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
   }
 }
 
+// Double-float reference tables in constant memory (warp-uniform operands).
+__constant__ ThRef<gbfem::Dd> kRefCDd = castRef<gbfem::Dd>();
+
+// x y in double-float, left unnormalised: TwoProduct of the leading parts
+// with the cross terms in the trailing part, the first term of a Dot2 sum
+// (mac adds the others).
+__device__ __forceinline__ gbfem::Dd ddProd(gbfem::Dd x, gbfem::Dd y)
+{
+  const float p  = __fmul_rn(x.hi, y.hi);
+  float       lo = __fmaf_rn(x.hi, y.hi, -p);
+  lo             = __fmaf_rn(x.hi, y.lo, lo);
+  lo             = __fmaf_rn(x.lo, y.hi, lo);
+  return {p, lo};
+}
+
+// A normalised double-float as the double it stands for (integer pipe).
+__device__ __forceinline__ double ddOut(gbfem::Dd x)
+{
+  return gbfem::ddJoinInt(accNorm(x));
+}
+
+constexpr int kThDdThreads = 128;
+// dynamic shared memory of thElemKernelDd: each thread's convection matrix
+constexpr int kThDdConvBytes = 36 * kThDdThreads * static_cast<int>(sizeof(float2));
+
+// FP64-accurate Jacobian + residual, one thread per element, in double-float
+// arithmetic on the FP32 pipe: the element of thElemKernel64 with every
+// product-sum a Dot2 accumulation (ddProd, then mac; normalised once at its
+// end), so that FP64 issue (1/64 of the FP32 rate on GB300) no longer bounds
+// it. FP64 is left for the geometry (about 30 operations per element); the
+// state, the geometry factors and every output cross between double and
+// double-float on the integer pipe (ddSplitInt, ddJoinInt). The convection
+// matrix A_ab = sum_q w_q N^_a (dN^_b . ut_q) is formed once per element
+// into shared memory (a column of 36 double-floats per thread, read back
+// conflict-free) so that the row loop holds only the state, the vertex
+// gradients and the geometry factors in registers. Rows are staged and added
+// row-coalesced as in thElemKernel64. kPlain: a coloured pass, as there.
+template <bool kPlain = false>
+__global__ void __launch_bounds__(kThDdThreads, 4)
+    thElemKernelDd(ThArgs a, const unsigned char* pos_rows)
+{
+  using gbfem::Dd;
+  extern __shared__ float2 sConv[]; // [36][kThDdThreads]
+  __shared__ double buf[4][32][17];
+  __shared__ int    rsb[4][32];
+  __shared__ uint4  posb[4][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e0   = blockIdx.x * kThDdThreads + warp * 32;
+  const int idx  = e0 + lane;
+  bool      live = idx < a.ne;
+  const int e    = (kPlain && live) ? a.elems[idx] : idx;
+  const ThRef<Dd>& R = kRefCDd;
+
+  double aInvJd[4] = {0, 0, 0, 0}, G3d[3] = {0, 0, 0};
+  if (live)
+  {
+    for (int k = 0; k < 6; ++k)
+    {
+      if (static_cast<unsigned>(a.conn6[6 * e + k]) >= static_cast<unsigned>(a.num_nodes))
+      {
+        gbfem::devFail(a.status, gbfem::kDevNodeRange, e);
+        live = false;
+      }
+    }
+  }
+  if (live)
+  {
+    const double2 x0 = a.coords[a.conn6[6 * e + 0]];
+    const double2 x1 = a.coords[a.conn6[6 * e + 1]];
+    const double2 x2 = a.coords[a.conn6[6 * e + 2]];
+    const double  j00 = x1.x - x0.x, j01 = x2.x - x0.x;
+    const double  j10 = x1.y - x0.y, j11 = x2.y - x0.y;
+    const double  det = j00 * j11 - j01 * j10;
+    const double  ad  = det < 0.0 ? -det : det;
+    if (ad >= 1.0e-30)
+    {
+      const double inv = gbfem::rcpF64(det);
+      const double i00 = j11 * inv, i01 = -j01 * inv, i10 = -j10 * inv, i11 = j00 * inv;
+      aInvJd[0]        = ad * i00;
+      aInvJd[1]        = ad * i01;
+      aInvJd[2]        = ad * i10;
+      aInvJd[3]        = ad * i11;
+      const double nad = a.nu * ad;
+      G3d[0]           = nad * (i00 * i00 + i01 * i01);
+      G3d[1]           = nad * (i10 * i10 + i11 * i11);
+      G3d[2]           = nad * (i00 * i10 + i01 * i11);
+    }
+    else
+    {
+      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+      live = false;
+    }
+  }
+  Dd iJ[4], G3[3], st[15];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+  {
+    iJ[k] = gbfem::ddSplitInt(aInvJd[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    G3[k] = gbfem::ddSplitInt(G3d[k]);
+  }
+#pragma unroll
+  for (int l = 0; l < 15; ++l)
+  {
+    st[l] = gbfem::ddSplitInt(live ? a.state[a.dofs[15 * e + l]] : 0.0);
+  }
+
+  // vertex gradients of the velocity, G_v[c][k]
+  Dd Gv[3][2][2];
+#pragma unroll
+  for (int v = 0; v < 3; ++v)
+  {
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+    {
+      Dd g0 = ddProd(st[c], R.dNv[v][0][0]), g1 = ddProd(st[c], R.dNv[v][0][1]);
+#pragma unroll
+      for (int s2 = 1; s2 < 6; ++s2)
+      {
+        g0 = mac(g0, st[2 * s2 + c], R.dNv[v][s2][0]);
+        g1 = mac(g1, st[2 * s2 + c], R.dNv[v][s2][1]);
+      }
+      g0          = accNorm(g0);
+      g1          = accNorm(g1);
+      Gv[v][c][0] = accNorm(mac(ddProd(g0, iJ[0]), g1, iJ[2]));
+      Gv[v][c][1] = accNorm(mac(ddProd(g0, iJ[1]), g1, iJ[3]));
+    }
+  }
+  // quadrature-point transforms ut_q = |det| J^-1 u_q
+  Dd ut[kNq][2];
+#pragma unroll
+  for (int q = 0; q < kNq; ++q)
+  {
+    Dd u0 = ddProd(R.N[q][0], st[0]), u1 = ddProd(R.N[q][0], st[1]);
+#pragma unroll
+    for (int s2 = 1; s2 < 6; ++s2)
+    {
+      u0 = mac(u0, R.N[q][s2], st[2 * s2]);
+      u1 = mac(u1, R.N[q][s2], st[2 * s2 + 1]);
+    }
+    u0       = accNorm(u0);
+    u1       = accNorm(u1);
+    ut[q][0] = accNorm(mac(ddProd(iJ[0], u0), iJ[1], u1));
+    ut[q][1] = accNorm(mac(ddProd(iJ[2], u0), iJ[3], u1));
+  }
+  // convection matrix A[sa][b] = sum_q wN[q][sa] (dN^_b(q) . ut_q), one
+  // column b at a time, into this thread's column of sConv
+  float2* const colA = sConv + threadIdx.x;
+#pragma unroll 1
+  for (int b = 0; b < 6; ++b)
+  {
+    Dd vq[kNq];
+#pragma unroll
+    for (int q = 0; q < kNq; ++q)
+    {
+      vq[q] = accNorm(mac(ddProd(R.dNr[q][b][0], ut[q][0]), R.dNr[q][b][1], ut[q][1]));
+    }
+#pragma unroll
+    for (int sa = 0; sa < 6; ++sa)
+    {
+      Dd t = ddProd(R.wN[0][sa], vq[0]);
+#pragma unroll
+      for (int q = 1; q < kNq; ++q)
+      {
+        t = mac(t, R.wN[q][sa], vq[q]);
+      }
+      t                                   = accNorm(t);
+      colA[(6 * sa + b) * kThDdThreads] = make_float2(t.hi, t.lo);
+    }
+  }
+
+  const bool jac = a.vals != nullptr;
+  // row l: CSR start and positions (loaded ahead of the values)
+  auto rowRef = [&](int l, int& rs, uint4& pw) {
+    rs = -1;
+    pw = make_uint4(0, 0, 0, 0);
+    if (live && jac)
+    {
+      rs = a.row_ptr[a.dofs[15 * e + l]];
+      if (pos_rows != nullptr)
+      {
+        pw = *reinterpret_cast<const uint4*>(pos_rows + (15LL * e + l) * 16);
+      }
+    }
+  };
+  double* const bv    = buf[warp][lane];
+  auto          stage = [&](int l, int rs, const uint4& pw, double r) {
+    gbfem::awaitPrerequisites(); // the outputs' zero fill may still be running
+    if (live)
+    {
+      gbfem::addTo<kPlain>(a.res + a.dofs[15 * e + l], r);
+    }
+    if (jac)
+    {
+      rsb[warp][lane]  = rs;
+      posb[warp][lane] = pw;
+    }
+  };
+  auto scatterRow = [&](int l) {
+    if (!jac)
+    {
+      return;
+    }
+    __syncwarp();
+    const int j = lane & 15;
+#pragma unroll 4
+    for (int t2 = 0; t2 < 16; ++t2)
+    {
+      const int t  = 2 * t2 + (lane >> 4);
+      const int rs = rsb[warp][t];
+      if (j < 15 && rs >= 0 && (l < 12 || j < 12))
+      {
+        const int slot = pos_rows != nullptr
+                             ? rs + reinterpret_cast<const unsigned char*>(&posb[warp][t])[j]
+                             : a.jac_map[225LL * (e0 + t) + 15 * l + j];
+        gbfem::addTo<kPlain>(a.vals + slot, buf[warp][t][j]);
+      }
+    }
+    __syncwarp();
+  };
+
+  // velocity rows (sa, c)
+#pragma unroll 1
+  for (int sa = 0; sa < 6; ++sa)
+  {
+    Dd da[6]; // diffusion + convection, D_ab + A_ab
+#pragma unroll
+    for (int b = 0; b < 6; ++b)
+    {
+      const float2 cv = colA[(6 * sa + b) * kThDdThreads];
+      Dd           d  = mac(Dd(cv.x, cv.y), G3[0], R.S00[sa][b]);
+      d               = mac(d, G3[1], R.S11[sa][b]);
+      da[b]           = accNorm(mac(d, G3[2], R.S01[sa][b]));
+    }
+    // the two component rows share everything but the component: one
+    // rolled loop over c (half the code of an unrolled pair, which the
+    // instruction cache does not hold), the component's operands selected
+#pragma unroll 1
+    for (int c = 0; c < 2; ++c)
+    {
+      int   rs;
+      uint4 pw;
+      rowRef(2 * sa + c, rs, pw);
+      const bool c1 = c != 0;
+      Dd         gcc[3], gco[3]; // G_v[c][c], G_v[c][other]
+#pragma unroll
+      for (int v = 0; v < 3; ++v)
+      {
+        gcc[v] = c1 ? Gv[v][1][1] : Gv[v][0][0];
+        gco[v] = c1 ? Gv[v][1][0] : Gv[v][0][1];
+      }
+      const Dd      jc = c1 ? iJ[1] : iJ[0], jc2 = c1 ? iJ[3] : iJ[2];
+      double* const own = bv + c;
+      double* const oth = bv + (c ^ 1);
+      Dd            r;
+#pragma unroll
+      for (int b = 0; b < 6; ++b)
+      {
+        const Dd sb = c1 ? st[2 * b + 1] : st[2 * b];
+        r           = b == 0 ? ddProd(da[0], sb) : mac(r, da[b], sb);
+        const Dd t0 = R.T[0][sa][b], t1 = R.T[1][sa][b], t2 = R.T[2][sa][b];
+        Dd       mcc = mac(da[b], t0, gcc[0]);
+        mcc          = mac(mac(mcc, t1, gcc[1]), t2, gcc[2]);
+        Dd mco       = ddProd(t0, gco[0]);
+        mco          = mac(mac(mco, t1, gco[1]), t2, gco[2]);
+        own[2 * b]   = ddOut(mcc);
+        oth[2 * b]   = ddOut(mco);
+      }
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+      {
+        const Dd vp = -accNorm(mac(ddProd(jc, R.C[0][sa][b]), jc2, R.C[1][sa][b]));
+        bv[12 + b]  = gbfem::ddJoinInt(vp);
+        r           = mac(r, vp, st[12 + b]);
+      }
+      stage(2 * sa + c, rs, pw, ddOut(r));
+      scatterRow(2 * sa + c);
+    }
+  }
+  // pressure rows b: the negative divergence block, the same values as the
+  // pressure columns above
+#pragma unroll 1
+  for (int b = 0; b < 3; ++b)
+  {
+    int   rs;
+    uint4 pw;
+    rowRef(12 + b, rs, pw);
+    Dd r;
+#pragma unroll
+    for (int sa = 0; sa < 6; ++sa)
+    {
+      const Dd c0 = R.C[0][sa][b], c1 = R.C[1][sa][b];
+      const Dd v0 = -accNorm(mac(ddProd(iJ[0], c0), iJ[2], c1));
+      const Dd v1 = -accNorm(mac(ddProd(iJ[1], c0), iJ[3], c1));
+      bv[2 * sa]     = gbfem::ddJoinInt(v0);
+      bv[2 * sa + 1] = gbfem::ddJoinInt(v1);
+      r              = sa == 0 ? ddProd(v0, st[0]) : mac(r, v0, st[2 * sa]);
+      r              = mac(r, v1, st[2 * sa + 1]);
+    }
+    bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    stage(12 + b, rs, pw, ddOut(r));
+    scatterRow(12 + b);
+  }
+}
+
+// thElemKernelDd takes more than the default 48 KB of shared memory per
+// block (its convection columns are dynamic shared memory): allow that, and
+// ask for the largest shared-memory carveout so that four blocks fit on an
+// SM. Once per device.
+void thDdPrepare()
+{
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  gbfem::cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
+  const unsigned long long bit = 1ull << (dev & 63);
+  if ((done.load(std::memory_order_acquire) & bit) != 0)
+  {
+    return;
+  }
+  for (auto k : {thElemKernelDd<false>, thElemKernelDd<true>})
+  {
+    gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kThDdConvBytes),
+              "Taylor-Hood double-float kernel shared memory");
+    gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared),
+              "Taylor-Hood double-float kernel carveout");
+  }
+  done.fetch_or(bit, std::memory_order_acq_rel);
+}
+
 } // namespace
 
 namespace gbfem
@@ -442,11 +777,15 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
     {
       if (jac)
       {
+        require(!col || map->jac_pos_rows != nullptr,
+                "coloured Taylor-Hood assembly needs the compact position map");
+        thDdPrepare();
         pass(
             [&](const ThArgs& x, bool d, bool plain) {
-              plain ? launchMaybeDependent(d, thKernelColour<gbfem::Dd, true, true>, gb(x),
-                                           kThreads, s, x)
-                    : launchMaybeDependent(d, thKernelDd<true>, gb(x), kThreads, s, x);
+              plain ? launchMaybeDependentSmem(d, thElemKernelDd<true>, eb(x), kThDdThreads,
+                                               kThDdConvBytes, s, x, map->jac_pos_rows)
+                    : launchMaybeDependentSmem(d, thElemKernelDd<false>, eb(x), kThDdThreads,
+                                               kThDdConvBytes, s, x, map->jac_pos_rows);
             },
             dep);
       }

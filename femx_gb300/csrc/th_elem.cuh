@@ -950,17 +950,6 @@ __global__ void __launch_bounds__(kThreads, 12) thKernel(ThArgs a)
   thBlock<T, kJac, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
 }
 
-// FP64-accurate Jacobian (and residual) in double-float arithmetic on the
-// FP32 pipe, the 16-lane layout of the FP32 kernel.
-template <bool kRes>
-__global__ void __launch_bounds__(kThreads, 6) thKernelDd(ThArgs a)
-{
-  __shared__ ThSmem<gbfem::Dd> sm;
-  thStageRef(sm, a.status);
-  __syncthreads();
-  thBlock<gbfem::Dd, true, kRes, false>(a, blockIdx.x * kElemsPerBlock, sm);
-}
-
 // Coloured passes (one launch per colour, a.elems = the colour's
 // elements): plain read-add-writes instead of FP64 reductions.
 template <class T, bool kJac, bool kRes>
