@@ -251,67 +251,38 @@ __device__ __forceinline__ Dd ddSplitInt(double x)
   return Dd(e > 896u ? __uint_as_float(hb) : 0.0f, e >= 920u ? lo : 0.0f);
 }
 
-// double-float -> double on the integer pipe, for a normalised pair
-// (|lo| <= ulp(hi)/2, as every Dd operation leaves it). hi is widened
-// exactly into the FP64 bit pattern; lo, expressed in units of the last
-// FP64 place of hi (fewer than 2^29 of them, truncated toward zero), is
-// added to that pattern as a 64-bit integer. The sum stays inside hi's
-// binade except when hi is a power of two and lo of the other sign: the
-// result then lies in the binade below, whose unit is half as large, so lo
-// is counted in those units. Faithful (within one unit of the last FP64
-// place) for |hi| >= 2^-103; below that lo is dropped (the result is hi).
-// Zero and subnormal hi give 0; an infinite or NaN hi is widened as it is.
-static __device__ __noinline__ double ddJoinIntWide(Dd v)
-{
-  const unsigned hb = __float_as_uint(v.hi), lb = __float_as_uint(v.lo);
-  const unsigned ha = hb & 0x7fffffffu, la = lb & 0x7fffffffu;
-  const unsigned eh = ha >> 23, el = la >> 23;
-  if (eh == 0xffu)
-  {
-    return f32ToF64Slow(v.hi);
-  }
-  // lo = ml 2^(max(el,1)-150) (subnormal lo without the implicit one); the
-  // FP64 unit of hi is 2^(eh-179), so lo counts ml 2^(max(el,1)-eh+29) units
-  const unsigned ml  = (la & 0x7fffffu) | (el != 0u ? 0x800000u : 0u);
-  const unsigned ee  = el != 0u ? el : 1u;
-  const bool     neg = ((hb ^ lb) & 0x80000000u) != 0u;
-  const unsigned dn  = (neg && (ha & 0x7fffffu) == 0u) ? 1u : 0u; // into the binade below
-  const unsigned t   = __funnelshift_rc(ml << 6, 0u, eh - ee - 23u - dn);
-  const unsigned long long w =
-      ((static_cast<unsigned long long>((ha >> 3) + 0x38000000u) << 32)
-       | static_cast<unsigned long long>(ha << 29))
-      + static_cast<unsigned long long>(neg ? -static_cast<long long>(t)
-                                            : static_cast<long long>(t));
-  const unsigned long long bits =
-      eh != 0u ? (w | (static_cast<unsigned long long>(hb & 0x80000000u) << 32)) : 0ull;
-  return __longlong_as_double(static_cast<long long>(bits));
-}
-
-// The same conversion with fewer integer operations for 2^-74 <= |hi| <
-// 2^126 (every other hi takes ddJoinIntWide): lo times sign(hi) is scaled by
-// a power of two into units of the last FP64 place of hi (of the binade
-// below when hi is a power of two and lo has the other sign), exactly, and
-// truncated to an integer (|t| < 2^30) by one float-to-integer conversion;
-// that count is added to hi's widened bit pattern. hi + lo stays inside that
-// binade (|lo| <= ulp(hi)/2), so the result is faithful: it lies between
-// hi + lo and hi, within one unit of the last FP64 place of hi + lo.
+// double-float -> double, for a normalised pair (|lo| <= ulp(hi)/2, as
+// every Dd operation leaves it), with no FP64 instruction and no branch. hi
+// is widened exactly into the FP64 bit pattern on the integer pipe; lo times
+// sign(hi) is scaled by a power of two into units of the last FP64 place of
+// hi, exactly, truncated to an integer (|t| < 2^30) by one float-to-integer
+// conversion and added to that pattern as a 64-bit integer. hi + lo stays
+// inside hi's binade except when hi is a power of two and lo has the other
+// sign: the result then lies in the binade below, whose unit is half as
+// large, and the scale counts lo in those units. Faithful (between hi + lo
+// and hi, within one unit of the last FP64 place of hi + lo) for 2^-74 <=
+// |hi| < 2^128; for smaller normal hi the scale is capped at 2^127, so lo
+// counts less than its value (an error below |lo| <= 2^-98). Zero and
+// subnormal hi give a zero of hi's sign; an infinite or NaN hi is widened
+// as it is (lo ignored).
 __device__ __forceinline__ double ddJoinInt(Dd v)
 {
   const unsigned hb = __float_as_uint(v.hi);
   const unsigned ha = hb & 0x7fffffffu;
-  const unsigned eh = ha >> 23;
-  if (eh - 53u > 199u)
-  {
-    return ddJoinIntWide(v);
-  }
+  const unsigned eh = ha >> 23; // biased exponent of hi
   const unsigned sg = hb & 0x80000000u;
   const unsigned dn =
       ((ha & 0x7fffffu) == 0u && ((hb ^ __float_as_uint(v.lo)) & 0x80000000u) != 0u) ? 1u : 0u;
+  const bool sp = eh == 0u || eh == 0xffu;
   // 2^(52 - E + dn) sign(hi), E = eh - 127 the exponent of hi
-  const float              scale = __uint_as_float(((306u + dn - eh) << 23) | sg);
-  const int                t     = __float2int_rz(__fmul_rn(v.lo, scale));
+  const unsigned se    = min(306u + dn - eh, 254u);
+  const float    scale = __uint_as_float((se << 23) | sg);
+  const int      t     = sp ? 0 : __float2int_rz(__fmul_rn(v.lo, scale));
+  // float exponent bias 127 -> FP64 bias 1023 (896 << 20); all ones stays all ones
+  const unsigned off = eh == 0u ? 0u : (eh == 0xffu ? 0x70000000u : 0x38000000u);
+  const unsigned hx  = eh == 0u ? 0u : ha;
   const unsigned long long w =
-      (static_cast<unsigned long long>((ha >> 3) + 0x38000000u) << 32) | (ha << 29);
+      (static_cast<unsigned long long>((hx >> 3) + off) << 32) | (hx << 29);
   const unsigned long long m = w + static_cast<unsigned long long>(static_cast<long long>(t));
   return __longlong_as_double(
       static_cast<long long>(m | (static_cast<unsigned long long>(sg) << 32)));

@@ -320,9 +320,9 @@ constexpr int kThDdConvBytes = 36 * kThDdThreads * static_cast<int>(sizeof(float
 // arithmetic on the FP32 pipe: the element of thElemKernel64 with every
 // product-sum a Dot2 accumulation (ddProd, then mac; normalised once at its
 // end), so that FP64 issue (1/64 of the FP32 rate on GB300) no longer bounds
-// it. FP64 is left for the geometry (about 30 operations per element); the
-// state, the geometry factors and every output cross between double and
-// double-float on the integer pipe (ddSplitInt, ddJoinInt). The convection
+// it. FP64 is left for the four edge subtractions; the state, the edges and
+// every output cross between double and double-float on the integer pipe
+// (ddSplitInt, ddJoinInt). The convection
 // matrix A_ab = sum_q w_q N^_a (dN^_b . ut_q) is formed once per element
 // into shared memory (a column of 36 double-floats per thread, read back
 // conflict-free) so that the row loop holds only the state, the vertex
@@ -344,7 +344,10 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
   const int e    = (kPlain && live) ? a.elems[idx] : idx;
   const ThRef<Dd>& R = kRefCDd;
 
-  double aInvJd[4] = {0, 0, 0, 0}, G3d[3] = {0, 0, 0};
+  // geometry: the edges by FP64 subtraction (the coordinates can be far
+  // larger than the edges), everything else in double-float; |det| J^-1 =
+  // sign(det) adj(J) needs no division, nu |det| J^-1 J^-T one reciprocal
+  Dd e00 = Dd(0.0f, 0.0f), e01 = e00, e10 = e00, e11 = e00;
   if (live)
   {
     for (int k = 0; k < 6; ++k)
@@ -361,39 +364,29 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
     const double2 x0 = a.coords[a.conn6[6 * e + 0]];
     const double2 x1 = a.coords[a.conn6[6 * e + 1]];
     const double2 x2 = a.coords[a.conn6[6 * e + 2]];
-    const double  j00 = x1.x - x0.x, j01 = x2.x - x0.x;
-    const double  j10 = x1.y - x0.y, j11 = x2.y - x0.y;
-    const double  det = j00 * j11 - j01 * j10;
-    const double  ad  = det < 0.0 ? -det : det;
-    if (ad >= 1.0e-30)
-    {
-      const double inv = gbfem::rcpF64(det);
-      const double i00 = j11 * inv, i01 = -j01 * inv, i10 = -j10 * inv, i11 = j00 * inv;
-      aInvJd[0]        = ad * i00;
-      aInvJd[1]        = ad * i01;
-      aInvJd[2]        = ad * i10;
-      aInvJd[3]        = ad * i11;
-      const double nad = a.nu * ad;
-      G3d[0]           = nad * (i00 * i00 + i01 * i01);
-      G3d[1]           = nad * (i10 * i10 + i11 * i11);
-      G3d[2]           = nad * (i00 * i10 + i01 * i11);
-    }
-    else
-    {
-      gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
-      live = false;
-    }
+    e00              = gbfem::ddSplitInt(x1.x - x0.x);
+    e01              = gbfem::ddSplitInt(x2.x - x0.x);
+    e10              = gbfem::ddSplitInt(x1.y - x0.y);
+    e11              = gbfem::ddSplitInt(x2.y - x0.y);
   }
-  Dd iJ[4], G3[3], st[15];
-#pragma unroll
-  for (int k = 0; k < 4; ++k)
+  const Dd   det = accNorm(mac(ddProd(e00, e11), -e01, e10));
+  const bool neg = det.hi < 0.0f;
+  const Dd   ad  = neg ? -det : det;
+  if (live && !(ad.hi >= 1.0e-30f))
   {
-    iJ[k] = gbfem::ddSplitInt(aInvJd[k]);
+    gbfem::devFail(a.status, gbfem::kDevSingularJacobian, e);
+    live = false;
   }
-#pragma unroll
-  for (int k = 0; k < 3; ++k)
+  Dd iJ[4], G3[3], st[15]; // |det| J^-1 (row-major), nu |det| J^-1 J^-T (00, 11, 01)
+  iJ[0] = neg ? -e11 : e11;
+  iJ[1] = neg ? e01 : -e01;
+  iJ[2] = neg ? e10 : -e10;
+  iJ[3] = neg ? -e00 : e00;
   {
-    G3[k] = gbfem::ddSplitInt(G3d[k]);
+    const Dd nur = live ? gbfem::ddSplitInt(a.nu) * gbfem::ddRcp(ad) : Dd(0.0f, 0.0f);
+    G3[0]        = accNorm(mac(ddProd(e11, e11), e01, e01)) * nur;
+    G3[1]        = accNorm(mac(ddProd(e10, e10), e00, e00)) * nur;
+    G3[2]        = -(accNorm(mac(ddProd(e11, e10), e01, e00)) * nur);
   }
 #pragma unroll
   for (int l = 0; l < 15; ++l)
@@ -516,6 +509,7 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
   };
 
   // velocity rows (sa, c)
+  Dd rp[3] = {Dd(0.0f, 0.0f), Dd(0.0f, 0.0f), Dd(0.0f, 0.0f)}; // pressure residual
 #pragma unroll 1
   for (int sa = 0; sa < 6; ++sa)
   {
@@ -548,11 +542,12 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
       const Dd      jc = c1 ? iJ[1] : iJ[0], jc2 = c1 ? iJ[3] : iJ[2];
       double* const own = bv + c;
       double* const oth = bv + (c ^ 1);
-      Dd            r;
+      Dd            r, ssa = Dd(0.0f, 0.0f); // ssa: this row's own state value
 #pragma unroll
       for (int b = 0; b < 6; ++b)
       {
         const Dd sb = c1 ? st[2 * b + 1] : st[2 * b];
+        ssa         = b == sa ? sb : ssa;
         r           = b == 0 ? ddProd(da[0], sb) : mac(r, da[b], sb);
         const Dd t0 = R.T[0][sa][b], t1 = R.T[1][sa][b], t2 = R.T[2][sa][b];
         Dd       mcc = mac(da[b], t0, gcc[0]);
@@ -562,38 +557,41 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
         own[2 * b]   = ddOut(mcc);
         oth[2 * b]   = ddOut(mco);
       }
+      // the pressure columns B_(sa,c),b; the pressure rows are their
+      // transpose: the values go to the column slots of A[sa][.] (read into
+      // da above, free now), slot 6 sa + 3 c + b, and the pressure residual
+      // R_p(b) = sum B_(sa,c),b u_(sa,c) accumulates here
+      double* const bslot = reinterpret_cast<double*>(colA) + (6 * sa + 3 * c) * kThDdThreads;
 #pragma unroll
       for (int b = 0; b < 3; ++b)
       {
-        const Dd vp = -accNorm(mac(ddProd(jc, R.C[0][sa][b]), jc2, R.C[1][sa][b]));
-        bv[12 + b]  = gbfem::ddJoinInt(vp);
-        r           = mac(r, vp, st[12 + b]);
+        const Dd     vp = -accNorm(mac(ddProd(jc, R.C[0][sa][b]), jc2, R.C[1][sa][b]));
+        const double vj = gbfem::ddJoinInt(vp);
+        bv[12 + b]                 = vj;
+        bslot[b * kThDdThreads]    = vj;
+        r                          = mac(r, vp, st[12 + b]);
+        rp[b]                      = mac(rp[b], vp, ssa);
       }
       stage(2 * sa + c, rs, pw, ddOut(r));
       scatterRow(2 * sa + c);
     }
   }
-  // pressure rows b: the negative divergence block, the same values as the
-  // pressure columns above
+  // pressure rows b: the negative divergence block, the pressure columns
+  // staged above (slot 6 sa + 3 c + b = 3 k + b for column k = 2 sa + c)
+  const double* const colB = reinterpret_cast<const double*>(colA);
 #pragma unroll 1
   for (int b = 0; b < 3; ++b)
   {
     int   rs;
     uint4 pw;
     rowRef(12 + b, rs, pw);
-    Dd r;
 #pragma unroll
-    for (int sa = 0; sa < 6; ++sa)
+    for (int k = 0; k < 12; ++k)
     {
-      const Dd c0 = R.C[0][sa][b], c1 = R.C[1][sa][b];
-      const Dd v0 = -accNorm(mac(ddProd(iJ[0], c0), iJ[2], c1));
-      const Dd v1 = -accNorm(mac(ddProd(iJ[1], c0), iJ[3], c1));
-      bv[2 * sa]     = gbfem::ddJoinInt(v0);
-      bv[2 * sa + 1] = gbfem::ddJoinInt(v1);
-      r              = sa == 0 ? ddProd(v0, st[0]) : mac(r, v0, st[2 * sa]);
-      r              = mac(r, v1, st[2 * sa + 1]);
+      bv[k] = colB[(3 * k + b) * kThDdThreads];
     }
     bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    const Dd r = b == 0 ? rp[0] : (b == 1 ? rp[1] : rp[2]);
     stage(12 + b, rs, pw, ddOut(r));
     scatterRow(12 + b);
   }

@@ -39,7 +39,8 @@ GBFEM_API int gbfem_probe_rcp(int n, const double* in, double* out, int rsqrt, v
 /* Test hook for the integer-pipe double-float conversions of the tiled
  * FP64-accurate assembly: (hi[i], lo[i]) = split of in[i] (hi + lo within
  * 2^-46 |in[i]|), joined[i] = the double nearest below or above
- * jhi[i] + jlo[i] (a normalised pair), computed the way the kernels do. */
+ * jhi[i] + jlo[i] (a normalised pair with |jhi[i]| >= 2^-74; smaller
+ * magnitudes count jlo[i] in part), computed the way the kernels do. */
 GBFEM_API int gbfem_probe_dd(int n, const double* in, float* hi, float* lo, const float* jhi,
                              const float* jlo, double* joined, void* stream);
 

@@ -123,10 +123,30 @@ def test_double_float_join_is_faithful():
     jlo = np.concatenate([jlo, pl, np.zeros(4096, np.float32), -pl, np.float32([0.0, 0.0])])
     _, _, out = dd_probe(np.zeros(jhi.size), jhi, jlo)
     exact = jhi.astype(np.float64) + jlo.astype(np.float64)    # exact in FP64
-    big = np.abs(jhi) >= 2.0 ** -103                           # below, lo is dropped
+    big = np.abs(jhi) >= 2.0 ** -74                            # faithful
+    tiny = np.abs(jhi) < 2.0 ** -103                           # lo is dropped
+    mid = ~big & ~tiny                                         # lo partly counted
     assert np.all(np.abs(out - exact)[big] <= np.spacing(np.abs(exact))[big])
-    assert np.all(out[~big] == jhi[~big].astype(np.float64))
+    assert np.all(out[tiny] == jhi[tiny].astype(np.float64))
+    assert np.all(np.abs(out - exact)[mid] <= np.abs(jlo[mid]))
+    assert mid.sum() > 1000 and big.sum() > 100000
     assert out[-2] == 0.0 and out[-1] == 1.5
+
+
+def test_double_float_join_special_values():
+    """Infinite and NaN hi widen as they are; zero and subnormal hi give a
+    zero of hi's sign."""
+    f32 = np.float32
+    jhi = np.array([np.inf, -np.inf, np.nan, -0.0, 1e-40, -1e-40, 2.0 ** 127, -(2.0 ** -126)],
+                   dtype=f32)
+    jlo = np.array([0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 2.0 ** 100, 0.0], dtype=f32)
+    _, _, out = dd_probe(np.zeros(jhi.size), jhi, jlo)
+    assert out[0] == np.inf and out[1] == -np.inf and np.isnan(out[2])
+    assert out[3] == 0.0 and np.signbit(out[3])
+    assert out[4] == 0.0 and not np.signbit(out[4])
+    assert out[5] == 0.0 and np.signbit(out[5])
+    assert out[6] == 2.0 ** 127 + 2.0 ** 100
+    assert out[7] == -(2.0 ** -126)
 
 
 # --- parity ----------------------------------------------------------------
