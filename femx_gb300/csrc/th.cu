@@ -611,14 +611,15 @@ void thDdPrepare()
   {
     return;
   }
-  for (auto k : {thElemKernelDd<false>, thElemKernelDd<true>})
-  {
-    gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kThDdConvBytes),
-              "Taylor-Hood double-float kernel shared memory");
+  auto set = [](auto k, int bytes) {
+    gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                     "Taylor-Hood double-float kernel shared memory");
     gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                   cudaSharedmemCarveoutMaxShared),
-              "Taylor-Hood double-float kernel carveout");
-  }
+                                          cudaSharedmemCarveoutMaxShared),
+                     "Taylor-Hood double-float kernel carveout");
+  };
+  set(thElemKernelDd<false>, kThDdConvBytes);
+  set(thElemKernelDd<true>, kThDdConvBytes);
   done.fetch_or(bit, std::memory_order_acq_rel);
 }
 
