@@ -59,6 +59,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "NS P2/P1 Jacobian elems/s & VJP grads/s vs plain FP64 GPU path at stated rel err"
 TH_NX, NU = 256, 1.0e-3
+# Thread instructions per element of the double-float Taylor-Hood kernel
+# (thElemKernelDd), counted by ncu (inst_executed x 32 / elements, 256x256
+# cavity): the numerator of its issue roofline.
+DF_INSTR_PER_ELEM = 28619
 VJP_NX = 512
 POISSON_NX, NSPMV, SPMV_SCALE = 1024, 10, 0.125
 NS_NX = 256
@@ -428,6 +432,10 @@ def main():
         nnz = pat.nnz
         np2 = t["coords"].shape[0]
         b_th = 8 * nnz + 16 * nd + 60 * e + 24 * e + 16 * np2
+        clk_sum = clk.summary()
+        sm_mhz = clk_sum["sm_mhz"] or clk_sum["sm_max_mhz"] or 2070.0
+        issue_peak = torch.cuda.get_device_properties(local).multi_processor_count * 128 \
+            * sm_mhz * 1e6
         # FP64-pipe instructions of the plain kernel per element (counted from
         # the kernel: geometry 36, vertex gradients 168, quadrature transforms
         # 168, 12 velocity rows x 111, 3 pressure rows x 36), set against the
@@ -465,6 +473,15 @@ def main():
                 "kernel": "thElemKernelDd<false>", "launch_ms": t_kern_df * 1e3,
                 "roofline": {"bound": "hbm", "achieved": b_th / t_kern_df / 1e9, "peak": hbm,
                              "unit": "GB/s", "frac": b_th / t_kern_df / 1e9 / hbm},
+                "issue": {"binding_resource": "instruction issue (all pipes), not HBM",
+                          "thread_instructions_per_element": DF_INSTR_PER_ELEM,
+                          "achieved_tinstr_per_s": DF_INSTR_PER_ELEM * e / t_kern_df,
+                          "peak_tinstr_per_s": issue_peak,
+                          "frac": DF_INSTR_PER_ELEM * e / t_kern_df / issue_peak,
+                          "peak_source": "one warp instruction per SM sub-partition per clock "
+                                         "(4 x 32 lanes per SM) at the median SM clock sampled "
+                                         "in the timed region",
+                          "count_source": "ncu inst_executed of the kernel x 32 / elements"},
                 "precision": "FP64-accurate: element arithmetic in double-float (float "
                              "pairs, ~48 significant bits) on the FP32 pipe; accumulation, "
                              "scatter and vectors FP64"},
@@ -499,7 +516,7 @@ def main():
                                    "kernel": "thKernel<float,true>",
                                    "launch_ms": t_kern * 1e3, "algorithmic_bytes": b_th},
             "fp64_fma_peak_tflops_measured": fp64,
-            "clocks": clk.summary(),
+            "clocks": clk_sum,
         })
         del amap, bc, jac, res, j64, r64
 
