@@ -63,6 +63,9 @@ TH_NX, NU = 256, 1.0e-3
 # (thElemKernelDd), counted by ncu (inst_executed x 32 / elements, 256x256
 # cavity): the numerator of its issue roofline.
 DF_INSTR_PER_ELEM = 28619
+# FP64 instructions per element of the plain FP64 Taylor-Hood kernel
+# (thElemKernel64), counted by ncu the same way: DFMA + DMUL + DADD.
+FP64_INSTR_PER_ELEM = 1190
 VJP_NX = 512
 POISSON_NX, NSPMV, SPMV_SCALE = 1024, 10, 0.125
 NS_NX = 256
@@ -436,12 +439,12 @@ def main():
         sm_mhz = clk_sum["sm_mhz"] or clk_sum["sm_max_mhz"] or 2070.0
         issue_peak = torch.cuda.get_device_properties(local).multi_processor_count * 128 \
             * sm_mhz * 1e6
-        # FP64-pipe instructions of the plain kernel per element (counted from
-        # the kernel: geometry 36, vertex gradients 168, quadrature transforms
-        # 168, 12 velocity rows x 111, 3 pressure rows x 36), set against the
-        # measured FMA issue rate (fp64 = TFLOP/s with FMA = 2).
+        # FP64 instructions of the plain kernel per element, counted by ncu
+        # on the 256x256 cavity (DFMA 846 + DMUL 230 + DADD 114 thread
+        # instructions per element), set against the measured FMA issue rate
+        # (fp64 = TFLOP/s with FMA = 2).
         fp64 = fp64_peak_tflops(torch, L)
-        i64 = 1812 * e  # FP64 instructions per launch of the plain kernel
+        i64 = FP64_INSTR_PER_ELEM * e  # FP64 instructions per launch of the plain kernel
         line.update({
             "metric": METRIC, "value": world * e / t_plain, "unit": "elements/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -503,7 +506,7 @@ def main():
                          "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
                          "binding_resource": "FP64 issue (see fp64_issue)"},
             "fp64_issue": {"kernel": "thElemKernel64 (thread per element)",
-                           "instructions_per_element": 1812,
+                           "instructions_per_element": FP64_INSTR_PER_ELEM,
                            "achieved_ginstr_per_s": i64 / t_kern64 / 1e9,
                            "peak_ginstr_per_s": fp64 / 2 * 1e3,
                            "frac": i64 / t_kern64 / 1e12 / (fp64 / 2),
