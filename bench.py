@@ -475,7 +475,8 @@ def main():
                                                 "gate": 1e-12},
                 "kernel": "thElemKernelDd<false>", "launch_ms": t_kern_df * 1e3,
                 "roofline": {"bound": "hbm", "achieved": b_th / t_kern_df / 1e9, "peak": hbm,
-                             "unit": "GB/s", "frac": b_th / t_kern_df / 1e9 / hbm},
+                             "unit": "GB/s", "frac": b_th / t_kern_df / 1e9 / hbm,
+                             "traffic": traffic.get("th_double_float")},
                 "issue": {"binding_resource": "instruction issue (all pipes), not HBM",
                           "thread_instructions_per_element": DF_INSTR_PER_ELEM,
                           "achieved_tinstr_per_s": DF_INSTR_PER_ELEM * e / t_kern_df,
