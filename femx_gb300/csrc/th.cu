@@ -19,9 +19,13 @@
 // The residual follows from the same blocks: R_(a,c) = sum_b (D+A)_ab
 // u_(b,c) + sum_b B_(a,c),b p_b, R_p(b) = sum_(a,e) B_(a,e),b u_(a,e).
 //
-// Layout: a 16-lane group owns one element; shared stages compute the
-// geometry, the quadrature-point transforms and the vertex gradients once;
-// then lane l produces local row l (15 entries + residual).
+// Layouts: FP32 quadrature (thKernel, th_elem.cuh) gives a 16-lane group
+// one element — shared stages compute the geometry, the quadrature-point
+// transforms and the vertex gradients once, then lane l produces local row l
+// (15 entries + residual). Plain FP64 (thElemKernel64) and FP64-accurate
+// double-float (thElemKernelDd) give one thread one element (below): FP64
+// issue, resp. the double-float instruction count, is their bound, and a
+// thread per element keeps every lane of every instruction busy.
 // Output: lanes scatter-add with FP64 reductions at L2 through the compact
 // in-row position map (fastest). With GBFEM_DETERMINISTIC, lane l writes its
 // row as one record instead and a row pass (gather.cuh) sums each CSR row's
