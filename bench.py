@@ -392,6 +392,24 @@ def main():
         # accuracy of the fast path against the plain FP64 path at full size
         A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision="fp64")
         j64, r64 = jac.vals.clone(), res.clone()
+        # the Taylor-Hood state VJP g = J(u)^T lam without forming J (the
+        # transpose action behind the autograd wrapper), against J^T lam of
+        # the FP64 Jacobian just assembled (gbfem_spmv_t)
+        lam_th = torch.from_numpy(np.random.default_rng(7).standard_normal(nd)).cuda()
+        g_ref = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        A.matvecT(jac, lam_th, g_ref)
+        g_th = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        th_vjp = {"workload": f"J(u)^T lam, Taylor-Hood {nx}x{nx} cavity, {e} elements",
+                  "check": "against J^T lam of the assembled FP64 Jacobian (CSR SpMV-T)"}
+        for prec in ("fp64", "double_float", "fp32_quad"):
+            tv = maxrank(timer.run(lambda: A.vjpTaylorHood(amap, coords, conn6, NU, state, lam_th,
+                                                           g_th, precision=prec),
+                                   args.steps, args.warmup))
+            th_vjp[prec] = {"ms_per_grad": tv * 1e3, "grads_per_s": 1.0 / tv,
+                            "elements_per_s": world * e / tv,
+                            "rel_err_vs_fp64_jt_lam":
+                                float((g_th - g_ref).abs().max() / g_ref.abs().max())}
+        launches += 6 * args.steps
         A.assembleTaylorHood(amap, coords, conn6, NU, state, res, jac, precision="fp32_quad")
         err_j = float((jac.vals - j64).abs().max() / j64.abs().max())
         err_r = float((res - r64).abs().max() / r64.abs().max())
@@ -520,6 +538,7 @@ def main():
                                    "kernel": "thKernel<float,true>",
                                    "launch_ms": t_kern * 1e3, "algorithmic_bytes": b_th},
             "fp64_fma_peak_tflops_measured": fp64,
+            "th_state_vjp": th_vjp,
             "clocks": clk_sum,
         })
         del amap, bc, jac, res, j64, r64

@@ -125,7 +125,11 @@ constexpr int kTh64PresBytes = 36 * 128 * static_cast<int>(sizeof(double));
 // us), and the reaction terms accumulate onto D + A by FMA (349 -> 331 us).
 // kPlain: a coloured pass (a.elems = the colour's elements, which share no
 // DOF): plain read-add-writes instead of FP64 reductions; needs pos_rows.
-template <bool kPlain = false>
+// kVjp: the state VJP g += J^T lam without forming J: each row's values are
+// multiplied by the row's adjoint value and summed into the thread's staging
+// row (its 15 entries of J_e^T lam_e), added to g_state at the end; no
+// residual, no CSR write.
+template <bool kPlain = false, bool kVjp = false>
 __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigned char* pos_rows)
 {
   extern __shared__ double sB64[]; // [36][128]: pressure columns, slot 6 sa + 3 c + b
@@ -225,11 +229,17 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     }
   }
 
-  const bool jac = a.vals != nullptr;
-  // row l: CSR start and positions (loaded ahead of the values)
-  auto rowRef = [&](int l, int& rs, uint4& pw) {
+  const bool jac = !kVjp && a.vals != nullptr;
+  // row l: CSR start and positions (loaded ahead of the values); VJP: the
+  // row's adjoint value
+  double lrow = 0.0;
+  auto   rowRef = [&](int l, int& rs, uint4& pw) {
     rs = -1;
     pw = make_uint4(0, 0, 0, 0);
+    if constexpr (kVjp)
+    {
+      lrow = live ? a.lam[a.dofs[15 * e + l]] : 0.0;
+    }
     if (live && jac)
     {
       rs = a.row_ptr[a.dofs[15 * e + l]];
@@ -240,9 +250,32 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
     }
   };
   // row values go straight to this lane's staging row bv (not held in
-  // registers: the row loop is register-bound)
+  // registers: the row loop is register-bound); VJP: bv accumulates J_e^T
+  // lam_e
   double* const bv = buf[warp][lane];
+  if constexpr (kVjp)
+  {
+#pragma unroll
+    for (int j = 0; j < 15; ++j)
+    {
+      bv[j] = 0.0;
+    }
+  }
+  auto put = [&](int j, double x) {
+    if constexpr (kVjp)
+    {
+      bv[j] += x * lrow;
+    }
+    else
+    {
+      bv[j] = x;
+    }
+  };
   auto stage = [&](int l, int rs, const uint4& pw, double r) {
+    if constexpr (kVjp)
+    {
+      return;
+    }
     gbfem::awaitPrerequisites(); // the outputs' zero fill may still be running
     if (live)
     {
@@ -349,14 +382,14 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
         mcc += R.T[2][sa][b] * Gv[2][c][c];
         const double mco = R.T[0][sa][b] * Gv[0][c][oc] + R.T[1][sa][b] * Gv[1][c][oc]
                            + R.T[2][sa][b] * Gv[2][c][oc];
-        bv[2 * b + c]  = mcc;
-        bv[2 * b + oc] = mco;
+        put(2 * b + c, mcc);
+        put(2 * b + oc, mco);
         r += da[b] * st[2 * b + c];
       }
       staticFor<3>([&](auto B) {
         constexpr int b  = decltype(B)::value;
         const double  vp = -presCol<sa, b>(aInvJ[c], aInvJ[2 + c]);
-        bv[12 + b]       = vp;
+        put(12 + b, vp);
         sB64[(6 * sa + 3 * c + b) * 128 + threadIdx.x] = vp;
         r += vp * st[12 + b];
         rp[b] += vp * st[2 * sa + c];
@@ -373,12 +406,27 @@ __global__ void __launch_bounds__(128, 4) thElemKernel64(ThArgs a, const unsigne
 #pragma unroll
     for (int k = 0; k < 12; ++k)
     {
-      bv[k] = sB64[(3 * k + b) * 128 + threadIdx.x];
+      put(k, sB64[(3 * k + b) * 128 + threadIdx.x]);
     }
-    bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    if constexpr (!kVjp)
+    {
+      bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    }
     stage(12 + b, rs, pw, rp[b]);
     scatterRow(12 + b);
   });
+  if constexpr (kVjp)
+  {
+    gbfem::awaitPrerequisites(); // the gradient's zero fill may still be running
+    if (live)
+    {
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        gbfem::addTo<kPlain>(a.g_state + a.dofs[15 * e + j], bv[j]);
+      }
+    }
+  }
 }
 
 // Double-float reference tables in constant memory (warp-uniform operands).
@@ -418,7 +466,10 @@ constexpr int kThDdConvBytes = 36 * kThDdThreads * static_cast<int>(sizeof(float
 // conflict-free) so that the row loop holds only the state, the vertex
 // gradients and the geometry factors in registers. Rows are staged and added
 // row-coalesced as in thElemKernel64. kPlain: a coloured pass, as there.
-template <bool kPlain = false>
+// kVjp: the state VJP g += J^T lam, as in thElemKernel64 (each row's values
+// times the row's adjoint value summed into the thread's staging row, here
+// as double-float pairs; joined and added to g_state at the end).
+template <bool kPlain = false, bool kVjp = false>
 __global__ void __launch_bounds__(kThDdThreads, 4)
     thElemKernelDd(ThArgs a, const unsigned char* pos_rows)
 {
@@ -548,11 +599,17 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
     }
   }
 
-  const bool jac = a.vals != nullptr;
-  // row l: CSR start and positions (loaded ahead of the values)
+  const bool jac = !kVjp && a.vals != nullptr;
+  // row l: CSR start and positions (loaded ahead of the values); VJP: the
+  // row's adjoint value
+  Dd   lrow   = Dd(0.0f, 0.0f);
   auto rowRef = [&](int l, int& rs, uint4& pw) {
     rs = -1;
     pw = make_uint4(0, 0, 0, 0);
+    if constexpr (kVjp)
+    {
+      lrow = gbfem::ddSplitInt(live ? a.lam[a.dofs[15 * e + l]] : 0.0);
+    }
     if (live && jac)
     {
       rs = a.row_ptr[a.dofs[15 * e + l]];
@@ -562,8 +619,35 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
       }
     }
   };
-  double* const bv    = buf[warp][lane];
-  auto          stage = [&](int l, int rs, const uint4& pw, double r) {
+  double* const bv  = buf[warp][lane];
+  float2* const bvd = reinterpret_cast<float2*>(bv); // VJP: J_e^T lam_e as pairs
+  if constexpr (kVjp)
+  {
+#pragma unroll
+    for (int j = 0; j < 15; ++j)
+    {
+      bvd[j] = make_float2(0.0f, 0.0f);
+    }
+  }
+  // entry j of the current row: staged as a double, or (VJP) times the row's
+  // adjoint value into the thread's J_e^T lam_e
+  auto put = [&](int j, Dd x) {
+    if constexpr (kVjp)
+    {
+      const float2 g = bvd[j];
+      const Dd     t = mac(Dd(g.x, g.y), x, lrow);
+      bvd[j]         = make_float2(t.hi, t.lo);
+    }
+    else
+    {
+      bv[j] = ddOut(x);
+    }
+  };
+  auto stage = [&](int l, int rs, const uint4& pw, double r) {
+    if constexpr (kVjp)
+    {
+      return;
+    }
     gbfem::awaitPrerequisites(); // the outputs' zero fill may still be running
     if (live)
     {
@@ -629,10 +713,8 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
         gcc[v] = c1 ? Gv[v][1][1] : Gv[v][0][0];
         gco[v] = c1 ? Gv[v][1][0] : Gv[v][0][1];
       }
-      const Dd      jc = c1 ? iJ[1] : iJ[0], jc2 = c1 ? iJ[3] : iJ[2];
-      double* const own = bv + c;
-      double* const oth = bv + (c ^ 1);
-      Dd            r, ssa = Dd(0.0f, 0.0f); // ssa: this row's own state value
+      const Dd jc = c1 ? iJ[1] : iJ[0], jc2 = c1 ? iJ[3] : iJ[2];
+      Dd       r, ssa = Dd(0.0f, 0.0f); // ssa: this row's own state value
 #pragma unroll
       for (int b = 0; b < 6; ++b)
       {
@@ -644,8 +726,8 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
         mcc          = mac(mac(mcc, t1, gcc[1]), t2, gcc[2]);
         Dd mco       = ddProd(t0, gco[0]);
         mco          = mac(mac(mco, t1, gco[1]), t2, gco[2]);
-        own[2 * b]   = ddOut(mcc);
-        oth[2 * b]   = ddOut(mco);
+        put(2 * b + c, mcc);
+        put(2 * b + 1 - c, mco);
       }
       // the pressure columns B_(sa,c),b; the pressure rows are their
       // transpose: the values go to the column slots of A[sa][.] (read into
@@ -655,12 +737,20 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
 #pragma unroll
       for (int b = 0; b < 3; ++b)
       {
-        const Dd     vp = -accNorm(mac(ddProd(jc, R.C[0][sa][b]), jc2, R.C[1][sa][b]));
-        const double vj = gbfem::ddJoinInt(vp);
-        bv[12 + b]                 = vj;
-        bslot[b * kThDdThreads]    = vj;
-        r                          = mac(r, vp, st[12 + b]);
-        rp[b]                      = mac(rp[b], vp, ssa);
+        const Dd vp = -accNorm(mac(ddProd(jc, R.C[0][sa][b]), jc2, R.C[1][sa][b]));
+        if constexpr (kVjp)
+        {
+          put(12 + b, vp);
+          reinterpret_cast<float2*>(bslot)[b * kThDdThreads] = make_float2(vp.hi, vp.lo);
+        }
+        else
+        {
+          const double vj         = gbfem::ddJoinInt(vp);
+          bv[12 + b]              = vj;
+          bslot[b * kThDdThreads] = vj;
+        }
+        r     = mac(r, vp, st[12 + b]);
+        rp[b] = mac(rp[b], vp, ssa);
       }
       stage(2 * sa + c, rs, pw, ddOut(r));
       scatterRow(2 * sa + c);
@@ -678,12 +768,36 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
 #pragma unroll
     for (int k = 0; k < 12; ++k)
     {
-      bv[k] = colB[(3 * k + b) * kThDdThreads];
+      if constexpr (kVjp)
+      {
+        const float2 v = reinterpret_cast<const float2*>(colB)[(3 * k + b) * kThDdThreads];
+        put(k, Dd(v.x, v.y));
+      }
+      else
+      {
+        bv[k] = colB[(3 * k + b) * kThDdThreads];
+      }
     }
-    bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    if constexpr (!kVjp)
+    {
+      bv[12] = bv[13] = bv[14] = 0.0; // structurally present, nothing added
+    }
     const Dd r = b == 0 ? rp[0] : (b == 1 ? rp[1] : rp[2]);
     stage(12 + b, rs, pw, ddOut(r));
     scatterRow(12 + b);
+  }
+  if constexpr (kVjp)
+  {
+    gbfem::awaitPrerequisites(); // the gradient's zero fill may still be running
+    if (live)
+    {
+#pragma unroll
+      for (int j = 0; j < 15; ++j)
+      {
+        const float2 g = bvd[j];
+        gbfem::addTo<kPlain>(a.g_state + a.dofs[15 * e + j], ddOut(Dd(g.x, g.y)));
+      }
+    }
   }
 }
 
@@ -710,8 +824,12 @@ void thDdPrepare()
   };
   set(thElemKernelDd<false>, kThDdConvBytes);
   set(thElemKernelDd<true>, kThDdConvBytes);
+  set(thElemKernelDd<false, true>, kThDdConvBytes);
+  set(thElemKernelDd<true, true>, kThDdConvBytes);
   set(thElemKernel64<false>, kTh64PresBytes);
   set(thElemKernel64<true>, kTh64PresBytes);
+  set(thElemKernel64<false, true>, kTh64PresBytes);
+  set(thElemKernel64<true, true>, kTh64PresBytes);
   done.fetch_or(bit, std::memory_order_acq_rel);
 }
 
@@ -977,6 +1095,7 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
     cudaStream_t s = asStream(stream);
+    thDdPrepare();
     // the VJP kernel is launched as a dependent of this zero fill
     zeroForNext(g_state, map->num_states, nullptr, 0, s);
     if (map->num_elems == 0)
@@ -1003,14 +1122,21 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
       const bool     plain  = x.elems != nullptr;
       if (precision == GBFEM_PREC_FP64)
       {
-        plain ? launchMaybeDependent(d, thVjpKernelColour<double, false>, blocks, kThreads, s, x)
-              : launchMaybeDependent(d, thVjpKernel<double, false>, blocks, kThreads, s, x);
+        // one thread per element (the FP64 Jacobian kernel in VJP mode)
+        const unsigned eb = blocksFor(x.ne, 128);
+        plain ? launchMaybeDependentSmem(d, thElemKernel64<true, true>, eb, 128, kTh64PresBytes,
+                                         s, x, nullptr)
+              : launchMaybeDependentSmem(d, thElemKernel64<false, true>, eb, 128,
+                                         kTh64PresBytes, s, x, nullptr);
       }
       else if (precision == GBFEM_PREC_DOUBLE_FLOAT)
       {
-        plain ? launchMaybeDependent(d, thVjpKernelColour<gbfem::Dd, false>, blocks, kThreads,
-                                     s, x)
-              : launchMaybeDependent(d, thVjpKernel<gbfem::Dd, false>, blocks, kThreads, s, x);
+        // one thread per element (the double-float Jacobian kernel in VJP mode)
+        const unsigned eb = blocksFor(x.ne, kThDdThreads);
+        plain ? launchMaybeDependentSmem(d, thElemKernelDd<true, true>, eb, kThDdThreads,
+                                         kThDdConvBytes, s, x, nullptr)
+              : launchMaybeDependentSmem(d, thElemKernelDd<false, true>, eb, kThDdThreads,
+                                         kThDdConvBytes, s, x, nullptr);
       }
       else
       {
