@@ -219,10 +219,6 @@ __device__ __forceinline__ double toF64(Dd x)
   return f32ToF64(x.hi) + f32ToF64(x.lo);
 }
 
-__device__ __forceinline__ double toF64Ftz(Dd x)
-{
-  return toF64(x);
-}
 
 // double -> double-float entirely on the integer and FP32 pipes (no FP64
 // instruction, no hardware conversion): hi takes the leading 24 significant

@@ -212,24 +212,12 @@ __device__ __forceinline__ const ThRef<float>* refTables(float)
 {
   return &kRefF;
 }
-__device__ const ThRef<gbfem::Dd> kRefDd = castRef<gbfem::Dd>();
-__device__ __forceinline__ const ThRef<gbfem::Dd>* refTables(gbfem::Dd)
-{
-  return &kRefDd;
-}
 
-// Lane shuffle within an element's 16 lanes, for the element's arithmetic
-// type (a double-float moves as its two floats).
+// Lane shuffle within an element's 16 lanes.
 template <class T>
 __device__ __forceinline__ T laneShfl(T v, int src)
 {
   return __shfl_sync(0xffffffffu, v, src, kLanes);
-}
-template <>
-__device__ __forceinline__ gbfem::Dd laneShfl<gbfem::Dd>(gbfem::Dd v, int src)
-{
-  return {__shfl_sync(0xffffffffu, v.hi, src, kLanes),
-          __shfl_sync(0xffffffffu, v.lo, src, kLanes)};
 }
 
 // acc + x y: a fused multiply-add in float and double; in double-float the
