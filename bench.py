@@ -65,7 +65,7 @@ TH_NX, NU = 256, 1.0e-3
 DF_INSTR_PER_ELEM = 28619
 # FP64 instructions per element of the plain FP64 Taylor-Hood kernel
 # (thElemKernel64), counted by ncu the same way: DFMA + DMUL + DADD.
-FP64_INSTR_PER_ELEM = 1118
+FP64_INSTR_PER_ELEM = 1023
 VJP_NX = 512
 POISSON_NX, NSPMV, SPMV_SCALE = 1024, 10, 0.125
 NS_NX = 256
