@@ -485,7 +485,7 @@ def test_taylor_hood_state_vjp_matches_oracle(precision, tol):
 
 
 @pytest.mark.parametrize("precision,det", [("fp64", False), ("fp32_quad", False), ("mixed", False),
-                                           ("fp32_quad", True)])
+                                           ("fp32_quad", True), ("double_float", False)])
 def test_taylor_hood_degenerate_element_is_reported(precision, det):
     """A zero-area element is reported through the map's status word (femx
     throws "Singular 2D Jacobian." from ElementValues::invJacobian) and adds
@@ -506,6 +506,15 @@ def test_taylor_hood_degenerate_element_is_reported(precision, det):
         m.check()
     m.check()
     assert torch.isfinite(res).all() and torch.isfinite(jac.vals).all()
+    if not det:
+        # the state VJP reports the same element
+        g = torch.zeros(nd, dtype=torch.float64, device="cuda")
+        lam = dev(np.random.default_rng(2).standard_normal(nd))
+        A.vjpTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), lam, g,
+                        precision=precision)
+        with pytest.raises(A.GbfemError, match="Singular 2D Jacobian"):
+            m.check()
+        assert torch.isfinite(g).all()
 
 
 def test_navier_degenerate_element_is_reported():
