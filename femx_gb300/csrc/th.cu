@@ -873,20 +873,20 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
 // carveout so that four blocks fit on an SM. Once per device.
 void thDdPrepare()
 {
-  static std::atomic<unsigned long long> done{0};
+  static std::atomic<unsigned long long> done{0}; // one bit per device below 64
   int dev = 0;
   gbfem::cudaCheck(cudaGetDevice(&dev), "cudaGetDevice");
-  const unsigned long long bit = 1ull << (dev & 63);
-  if ((done.load(std::memory_order_acquire) & bit) != 0)
+  const unsigned long long bit = dev < 64 ? 1ull << dev : 0ull; // others: set every time
+  if (bit != 0 && (done.load(std::memory_order_acquire) & bit) != 0)
   {
     return;
   }
   auto set = [](auto k, int bytes) {
     gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
-                     "Taylor-Hood double-float kernel shared memory");
+                     "Taylor-Hood element kernel shared memory");
     gbfem::cudaCheck(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                                           cudaSharedmemCarveoutMaxShared),
-                     "Taylor-Hood double-float kernel carveout");
+                     "Taylor-Hood element kernel carveout");
   };
   set(thElemKernelDd<false>, kThDdConvBytes);
   set(thElemKernelDd<true>, kThDdConvBytes);
