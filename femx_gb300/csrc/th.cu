@@ -871,7 +871,7 @@ __global__ void __launch_bounds__(kThDdThreads, 4)
 // shared memory per block (the convection columns, the pressure columns are
 // dynamic shared memory): allow that, and ask for the largest shared-memory
 // carveout so that four blocks fit on an SM. Once per device.
-void thDdPrepare()
+void thPrepareSharedMemory()
 {
   static std::atomic<unsigned long long> done{0}; // one bit per device below 64
   int dev = 0;
@@ -1039,7 +1039,7 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
     {
       require(!col || map->jac_pos_rows != nullptr,
               "coloured Taylor-Hood assembly needs the compact position map");
-      thDdPrepare();
+      thPrepareSharedMemory();
       pass(
           [&](const ThArgs& x, bool d, bool plain) {
             plain ? launchMaybeDependentSmem(d, thElemKernel64<true>, eb(x), 128,
@@ -1055,7 +1055,7 @@ void assembleTaylorHood(const gbfem_assembly_map* map, int num_p2_nodes, const d
       {
         require(!col || map->jac_pos_rows != nullptr,
                 "coloured Taylor-Hood assembly needs the compact position map");
-        thDdPrepare();
+        thPrepareSharedMemory();
         pass(
             [&](const ThArgs& x, bool d, bool plain) {
               plain ? launchMaybeDependentSmem(d, thElemKernelDd<true>, eb(x), kThDdThreads,
@@ -1161,7 +1161,7 @@ extern "C" int gbfem_vjp_th_ns(const gbfem_assembly_map* map, int num_p2_nodes,
     require((reinterpret_cast<uintptr_t>(coords) & 15) == 0,
             "Geometry coordinates must be 16-byte aligned");
     cudaStream_t s = asStream(stream);
-    thDdPrepare();
+    thPrepareSharedMemory();
     // the VJP kernel is launched as a dependent of this zero fill
     zeroForNext(g_state, map->num_states, nullptr, 0, s);
     if (map->num_elems == 0)
