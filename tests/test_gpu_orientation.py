@@ -109,3 +109,48 @@ def test_p1_on_clockwise_elements(precision, tiled):
     m.check()
     assert rel_inf(host(jac.vals), rvals) <= TOL[precision]
     assert rel_inf(host(res), rres) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "double_float", "fp32_quad"])
+def test_translated_and_scaled_mesh(precision):
+    """Coordinates far from the origin (offset 1e3, element size 1e-4): the
+    edges are formed by FP64 subtraction before any conversion, so every
+    precision keeps its gate; the double-float state is scaled by 1e6 as
+    well (relative accuracy)."""
+    c3, k3 = meshes.jittered_tri(8, seed=33)
+    c3 = c3 * 8e-4 + np.array([1.0e3, -2.5e2])
+    cp2, conn6, nv = meshes.p2_mesh(c3, k3)
+    offs, dofs, nd = meshes.th_elem_dofs(conn6, cp2.shape[0])
+    state = 1.0e6 * np.random.default_rng(33).standard_normal(nd)
+    om = orc.AssemblyMap(nd, nd, offs, dofs, offs, dofs)
+    rres, rvals = orc.assemble_th_ns(om, cp2, conn6, 1e-2, state)
+    m = A.makeAssemblyMap(nd, nd, dev(offs, torch.int32), dev(dofs, torch.int32),
+                          dev(offs, torch.int32), dev(dofs, torch.int32))
+    res = torch.zeros(nd, dtype=torch.float64, device="cuda")
+    jac = A.CsrMatrix(m.pattern())
+    A.assembleTaylorHood(m, dev(cp2), dev(conn6, torch.int32), 1e-2, dev(state), res, jac,
+                         precision=precision)
+    m.check()
+    assert rel_inf(host(jac.vals), rvals) <= TOL[precision]
+    assert rel_inf(host(res), rres) <= TOL[precision]
+
+    coords, conn = meshes.jittered_tri(16, seed=34)
+    coords = coords * 1e-3 + np.array([-7.0e2, 3.0e3])
+    n, e = coords.shape[0], conn.shape[0]
+    rng = np.random.default_rng(34)
+    kappa = np.exp(rng.standard_normal(e))
+    f = meshes.fourier_source(coords, 1)
+    u = 1.0e6 * rng.standard_normal(n)
+    offs1, dofs1 = meshes.scalar_elem_dofs(conn)
+    om1 = orc.AssemblyMap(n, n, offs1, dofs1, offs1, dofs1)
+    rr1, rv1 = orc.assemble_p1_kappa(om1, orc.P1Quad(coords, conn), kappa, f, u)
+    m1 = A.makeAssemblyMap(n, n, dev(offs1), dev(dofs1), dev(offs1), dev(dofs1))
+    m1.enableTiles(dev(coords))
+    for tiled in (False, True):
+        r1 = torch.zeros(n, dtype=torch.float64, device="cuda")
+        j1 = A.CsrMatrix(m1.pattern())
+        A.assembleP1Kappa(m1, dev(coords), dev(kappa), dev(f), dev(u), r1, j1,
+                          precision=precision, tiled=tiled)
+        m1.check()
+        assert rel_inf(host(j1.vals), rv1) <= TOL[precision]
+        assert rel_inf(host(r1), rr1) <= TOL[precision]
