@@ -510,7 +510,8 @@ __device__ __forceinline__ gbfem::Dd ddProd(gbfem::Dd x, gbfem::Dd y)
   return {p, lo};
 }
 
-// A normalised double-float as the double it stands for (integer pipe).
+// A double-float as the double it stands for (normalised, then joined
+// without FP64 instructions).
 __device__ __forceinline__ double ddOut(gbfem::Dd x)
 {
   return gbfem::ddJoinInt(accNorm(x));
