@@ -62,7 +62,7 @@ TH_NX, NU = 256, 1.0e-3
 # Thread instructions per element of the double-float Taylor-Hood kernel
 # (thElemKernelDd), counted by ncu (inst_executed x 32 / elements, 256x256
 # cavity): the numerator of its issue roofline.
-DF_INSTR_PER_ELEM = 28619
+DF_INSTR_PER_ELEM = 27446
 # FP64 instructions per element of the plain FP64 Taylor-Hood kernel
 # (thElemKernel64), counted by ncu the same way: DFMA + DMUL + DADD.
 FP64_INSTR_PER_ELEM = 1023
