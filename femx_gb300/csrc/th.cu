@@ -141,6 +141,32 @@ constexpr PairSlots makePairSlots()
 constexpr PairSlots kPairSlots = makePairSlots();
 static_assert(kPairSlots.groups * 4 <= 36, "reaction slots exceed the staging area");
 
+// Two pairs that share a group are never live together: one is read back
+// (in row b) no later than the other is formed (in its row a). Row a reads
+// its pairs (b < a) before it forms its own (b > a).
+constexpr bool pairSlotsDisjoint()
+{
+  for (int a0 = 0; a0 < 6; ++a0)
+  {
+    for (int b0 = a0 + 1; b0 < 6; ++b0)
+    {
+      for (int a1 = 0; a1 < 6; ++a1)
+      {
+        for (int b1 = a1 + 1; b1 < 6; ++b1)
+        {
+          const bool same = a0 == a1 && b0 == b1;
+          if (!same && kPairSlots.g[a0][b0] == kPairSlots.g[a1][b1] && !(b0 <= a1 || b1 <= a0))
+          {
+            return false;
+          }
+        }
+      }
+    }
+  }
+  return true;
+}
+static_assert(pairSlotsDisjoint(), "two live reaction pairs share a slot group");
+
 // dynamic shared memory of thElemKernel64: each thread's reaction entries
 constexpr int kTh64PresBytes = 36 * 128 * static_cast<int>(sizeof(double));
 
